@@ -1,0 +1,821 @@
+/*
+ * TEST INFRASTRUCTURE ONLY -- see fvm_oracle.h.  CPU restatement of the
+ * reference's explicit FVM step, written to reproduce its FP64 results bit for
+ * bit: every expression keeps the reference's operation order, including
+ * products with the zero components of axis normals.  Build with
+ * -ffp-contract=off (no FMA contraction) and without fast-math.
+ */
+#include "fvm_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NV 5
+
+typedef struct { double x, y, z; } vec3;
+
+static inline double dot3(vec3 a, vec3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+
+/* ------------------------------------------------------------------------ */
+/* Grid: cell centres by accumulation, grid.h:124-344.                      */
+/* ------------------------------------------------------------------------ */
+
+static void axis_grid(const orc_config* c, int a, int n, int g, double length, double* X, double* H) {
+    /* CompressionX starts as one default BlockNode (pos 0, q 1, N -1) and
+       InitLocal appends a closing BlockNode(L) (grid.h:165). */
+    double pos[ORC_MAX_BLOCKS + 1], q[ORC_MAX_BLOCKS + 1];
+    int nc[ORC_MAX_BLOCKS + 1];
+    int nb = c->n_blocks[a];
+    if (nb <= 0) {
+        nb = 1;
+        pos[0] = 0.0; q[0] = 1.0; nc[0] = -1;
+    } else {
+        for (int b = 0; b < nb; ++b) { pos[b] = c->block_pos[a][b]; q[b] = c->block_q[a][b]; nc[b] = c->block_cells[a][b]; }
+    }
+    pos[nb] = length; q[nb] = 1.0; nc[nb] = -1;
+    int nnodes = nb + 1;
+
+    double stp = 1.0;
+    if (nc[0] < 1) {
+        stp = length / n;
+        nc[0] = n;
+    } else {
+        double bl_len = pos[1] - pos[0];
+        int ncells = nc[0];
+        if (q[0] == 1.0) stp = bl_len / ncells;
+        else stp = bl_len * (1.0 - q[0]) / (1.0 - pow(q[0], ncells));
+    }
+    double xc = -(g * stp) + 0.5 * stp;
+    int ci = 0;
+    for (; ci < g; ++ci) { X[ci] = xc; H[ci] = stp; xc += stp; }
+    for (int b = 1; b < nnodes; ++b) {
+        double qb = q[b - 1];
+        for (int i = 0; i < nc[b - 1]; ++i) {
+            X[ci + i] = xc;
+            H[ci + i] = stp;
+            xc += 0.5 * stp * (1.0 + qb);
+            stp *= qb;
+        }
+        ci += nc[b - 1];
+        if (nc[b] > 0) {
+            double new_len = pos[b + 1] - pos[b];
+            int new_nc = nc[b];
+            double new_q = q[b];
+            if (new_q == 1.0) stp = new_len / new_nc;
+            else stp = new_len * (1.0 - new_q) / (1.0 - pow(new_q, new_nc));
+            xc = pos[b] + 0.5 * stp;
+        }
+    }
+    for (int i = 0; i < g; ++i) { X[ci + i] = xc; H[ci + i] = stp; xc += stp; }
+}
+
+void orc_dims(const orc_config* c, int* nxa, int* nya, int* nza) {
+    *nxa = c->nx + 2;
+    *nya = c->ndims > 1 ? c->ny + 2 : 1;
+    *nza = c->ndims > 2 ? c->nz + 2 : 1;
+}
+
+int orc_grid(const orc_config* c, double* x, double* hx, double* y, double* hy, double* z, double* hz) {
+    int nxa, nya, nza;
+    orc_dims(c, &nxa, &nya, &nza);
+    axis_grid(c, 0, c->nx, 1, c->length[0], x, hx);
+    if (c->ndims > 1) axis_grid(c, 1, c->ny, 1, c->length[1], y, hy);
+    else { y[0] = 0.0; hy[0] = 1.0; }
+    if (c->ndims > 2) axis_grid(c, 2, c->nz, 1, c->length[2], z, hz);
+    else { z[0] = 0.0; hz[0] = 1.0; }
+    (void)nxa; (void)nya; (void)nza;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Working context                                                          */
+/* ------------------------------------------------------------------------ */
+
+typedef struct {
+    const orc_config* c;
+    int nxa, nya, nza, ncells;
+    int gx, gy, gz;            /* ghost offsets per axis (1 if active) */
+    int imin, imax, jmin, jmax, kmin, kmax;
+    double *x, *hx, *y, *hy, *z, *hz;
+    double* vol;               /* grid.h:347-360 */
+    double* spectral;          /* per cell, ExplicitRungeKuttaFVM.h:31 */
+    double* resid;             /* AoS like values */
+    /* reconstruction objects, one per cell of the values array
+       (ExplicitRungeKuttaFVM.h:36,61-72): vals, grads[3][5], lim[5] */
+    double* rvals;
+    double* rgrad;
+    double* rlim;
+    double* eps2;              /* Venkatakrishnan eps^2 per cell (Limiters.h:93-96) */
+} orc_ctx;
+
+static inline int cidx(const orc_ctx* w, int i, int j, int k) {
+    return (k * w->nya + j) * w->nxa + i;
+}
+
+/* ------------------------------------------------------------------------ */
+/* EOS helpers                                                              */
+/* ------------------------------------------------------------------------ */
+
+/* Pressure from conserved variables: ideal gas as RoeSolverPerfectGasEOS.h:49;
+   stiffened gas p = (g-1)(rhoE - rho|u|^2/2) - g p_inf (not in the reference). */
+static inline double eos_pressure(const orc_config* c, double ro, double vx, double vy, double vz, double roE) {
+    double p = (c->gamma - 1.0) * (roE - ro * (vx * vx + vy * vy + vz * vz) / 2.0);
+    if (c->eos == ORC_EOS_STIFFENED) p = p - c->gamma * c->p_inf;
+    return p;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Boundary conditions, BCGeneral.h:100-268                                 */
+/* ------------------------------------------------------------------------ */
+
+static void bc_dummy_values(const orc_config* c, int side, const double* in, vec3 n, double* out) {
+    int t = c->bc_type[side];
+    switch (t) {
+    case ORC_BC_SYMMETRY: { /* BCGeneral.h:214-226 */
+        vec3 rv = {in[1], in[2], in[3]};
+        double s = dot3(n, rv);
+        vec3 rn = {s * n.x, s * n.y, s * n.z};
+        for (int v = 0; v < NV; ++v) out[v] = in[v];
+        out[1] -= 2.0 * rn.x;
+        out[2] -= 2.0 * rn.y;
+        out[3] -= 2.0 * rn.z;
+        break;
+    }
+    case ORC_BC_WALL: /* BCGeneral.h:229-238 */
+        for (int v = 0; v < NV; ++v) out[v] = in[v];
+        out[1] *= (-1);
+        out[2] *= (-1);
+        out[3] *= (-1);
+        break;
+    case ORC_BC_MOVING_WALL: { /* BCGeneral.h:241-268 */
+        double rho = in[0];
+        vec3 vin = {in[1] / rho, in[2] / rho, in[3] / rho};
+        double rhoe = in[4] - 0.5 * rho * dot3(vin, vin);
+        vec3 vb = {c->bc_velocity[side][0], c->bc_velocity[side][1], c->bc_velocity[side][2]};
+        vec3 vd = {2.0 * vb.x - vin.x, 2.0 * vb.y - vin.y, 2.0 * vb.z - vin.z};
+        out[0] = rho;
+        out[1] = rho * vd.x;
+        out[2] = rho * vd.y;
+        out[3] = rho * vd.z;
+        out[4] = rhoe + 0.5 * rho * dot3(vd, vd);
+        break;
+    }
+    case ORC_BC_SUBSONIC_INLET: { /* BCGeneral.h:186-196 */
+        double r = c->bc_density[side];
+        vec3 vv = {c->bc_velocity[side][0], c->bc_velocity[side][1], c->bc_velocity[side][2]};
+        out[0] = r;
+        out[1] = r * vv.x;
+        out[2] = r * vv.y;
+        out[3] = r * vv.z;
+        double eint = c->bc_pstatic[side] / (c->gamma - 1);
+        if (c->eos == ORC_EOS_STIFFENED) eint = eint + c->gamma * c->p_inf / (c->gamma - 1);
+        out[4] = eint + 0.5 * r * dot3(vv, vv);
+        break;
+    }
+    default: /* Natural (BCGeneral.h:207-211), SubsonicOutlet (:200-204) */
+        for (int v = 0; v < NV; ++v) out[v] = in[v];
+        break;
+    }
+}
+
+/* ExchangeValues (kernel.h:334-690) on one rank, then ComputeDummyCellValues
+   (kernel.h:693-915): periodic axes copy the opposite interior layer, other
+   axes apply the side's BC to the mirror cell with faceNormalL on both sides
+   (kernel.h:760,829,899). */
+static void fill_ghosts(orc_ctx* w, double* U) {
+    const orc_config* c = w->c;
+    double out[NV];
+    /* x */
+    for (int k = w->kmin; k <= w->kmax; ++k)
+        for (int j = w->jmin; j <= w->jmax; ++j) {
+            double* lo = U + (size_t)cidx(w, w->imin - 1, j, k) * NV;
+            double* hi = U + (size_t)cidx(w, w->imax + 1, j, k) * NV;
+            const double* first = U + (size_t)cidx(w, w->imin, j, k) * NV;
+            const double* last = U + (size_t)cidx(w, w->imax, j, k) * NV;
+            if (c->periodic[0]) {
+                memcpy(hi, first, sizeof(double) * NV);
+                memcpy(lo, last, sizeof(double) * NV);
+            } else {
+                vec3 nl = {-1.0, 0.0, 0.0};
+                bc_dummy_values(c, 0, first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, 1, last, nl, out); memcpy(hi, out, sizeof out);
+            }
+        }
+    if (c->ndims < 2) return;
+    for (int i = w->imin; i <= w->imax; ++i)
+        for (int k = w->kmin; k <= w->kmax; ++k) {
+            double* lo = U + (size_t)cidx(w, i, w->jmin - 1, k) * NV;
+            double* hi = U + (size_t)cidx(w, i, w->jmax + 1, k) * NV;
+            const double* first = U + (size_t)cidx(w, i, w->jmin, k) * NV;
+            const double* last = U + (size_t)cidx(w, i, w->jmax, k) * NV;
+            if (c->periodic[1]) {
+                memcpy(hi, first, sizeof(double) * NV);
+                memcpy(lo, last, sizeof(double) * NV);
+            } else {
+                vec3 nl = {0.0, -1.0, 0.0};
+                bc_dummy_values(c, 2, first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, 3, last, nl, out); memcpy(hi, out, sizeof out);
+            }
+        }
+    if (c->ndims < 3) return;
+    for (int i = w->imin; i <= w->imax; ++i)
+        for (int j = w->jmin; j <= w->jmax; ++j) {
+            double* lo = U + (size_t)cidx(w, i, j, w->kmin - 1) * NV;
+            double* hi = U + (size_t)cidx(w, i, j, w->kmax + 1) * NV;
+            const double* first = U + (size_t)cidx(w, i, j, w->kmin) * NV;
+            const double* last = U + (size_t)cidx(w, i, j, w->kmax) * NV;
+            if (c->periodic[2]) {
+                memcpy(hi, first, sizeof(double) * NV);
+                memcpy(lo, last, sizeof(double) * NV);
+            } else {
+                vec3 nl = {0.0, 0.0, -1.0};
+                bc_dummy_values(c, 4, first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, 5, last, nl, out); memcpy(hi, out, sizeof out);
+            }
+        }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Reconstruction, ExplicitRungeKuttaFVM.h:879-925 and src/Reconstruction   */
+/* ------------------------------------------------------------------------ */
+
+/* BarsJespersen l-function, Limiters.h:80-82: std::min(1.0, r). */
+static inline double lim_bj(double um, double ui, double d2) {
+    double r = (um - ui) / d2;
+    return (r < 1.0) ? r : 1.0;
+}
+
+/* Venkatakrishnan l-function, Limiters.h:102-115. */
+static inline double lim_venkat(double um, double ui, double d2, double umax, double umin, double eps2) {
+    double un = 0.5 * (umax - umin);
+    um /= un;
+    ui /= un;
+    d2 /= un;
+    double dm = um - ui;
+    return ((dm * dm + eps2) + 2 * d2 * dm) / (dm * dm + 2 * d2 * d2 + dm * d2 + eps2);
+}
+
+static void reconstruct_cell(orc_ctx* w, const double* U, int i, int j, int k) {
+    const orc_config* c = w->c;
+    int nd = c->ndims;
+    int ci = cidx(w, i, j, k);
+    const double* val = U + (size_t)ci * NV;
+    double* rv = w->rvals + (size_t)ci * NV;
+    double* rg = w->rgrad + (size_t)ci * 3 * NV; /* [axis][var] */
+    double* rl = w->rlim + (size_t)ci * NV;
+    for (int v = 0; v < NV; ++v) { rv[v] = val[v]; rl[v] = 1.0; }
+    for (int a = 0; a < 3 * NV; ++a) rg[a] = 0.0;
+    if (c->recon == ORC_RECON_PWC) return;
+
+    /* stencil x-, x+, y-, y+, z-, z+ (ExplicitRungeKuttaFVM.h:898-916) */
+    const double* st[6];
+    double sc[6]; /* neighbour centre coordinate along its axis */
+    st[0] = U + (size_t)cidx(w, i - 1, j, k) * NV; sc[0] = w->x[i - 1];
+    st[1] = U + (size_t)cidx(w, i + 1, j, k) * NV; sc[1] = w->x[i + 1];
+    if (nd > 1) {
+        st[2] = U + (size_t)cidx(w, i, j - 1, k) * NV; sc[2] = w->y[j - 1];
+        st[3] = U + (size_t)cidx(w, i, j + 1, k) * NV; sc[3] = w->y[j + 1];
+    }
+    if (nd > 2) {
+        st[4] = U + (size_t)cidx(w, i, j, k - 1) * NV; sc[4] = w->z[k - 1];
+        st[5] = U + (size_t)cidx(w, i, j, k + 1) * NV; sc[5] = w->z[k + 1];
+    }
+    double cc[3] = {w->x[i], w->y[j], w->z[k]};
+
+    if (c->recon == ORC_RECON_ENO2) {
+        /* ENO2PointsStencil.h:202-239 */
+        for (int a = 0; a < nd; ++a) {
+            for (int v = 0; v < NV; ++v) {
+                double gl = (val[v] - st[2 * a][v]) / (cc[a] - sc[2 * a]);
+                double gr = (st[2 * a + 1][v] - val[v]) / (sc[2 * a + 1] - cc[a]);
+                rg[a * NV + v] = (fabs(gl) < fabs(gr)) ? gl : gr;
+            }
+        }
+        return;
+    }
+
+    /* Linear2PointsStencil.h:147-178: central slopes on conserved variables */
+    for (int a = 0; a < nd; ++a) {
+        double d = sc[2 * a + 1] - sc[2 * a];
+        for (int v = 0; v < NV; ++v) rg[a * NV + v] = (st[2 * a + 1][v] - st[2 * a][v]) / d;
+    }
+    if (c->recon == ORC_RECON_LINEAR2) return;
+
+    /* Linear2psLim.h:305-374: projections to the 2*nDim face centres,
+       SampleSolution(point) - vals with the full 3-component dot product. */
+    double h[3] = {w->hx[i], w->hy[j], w->hz[k]};
+    double proj[6][NV];
+    for (int f = 0; f < 2 * nd; ++f) {
+        int a = f / 2;
+        double s = (f & 1) ? 0.5 * h[a] : -0.5 * h[a];
+        vec3 p = {a == 0 ? s : 0.0, a == 1 ? s : 0.0, a == 2 ? s : 0.0};
+        for (int v = 0; v < NV; ++v) {
+            vec3 g = {rg[0 * NV + v], rg[1 * NV + v], rg[2 * NV + v]};
+            proj[f][v] = (val[v] + dot3(g, p)) - val[v];
+        }
+    }
+    /* Limiter::ComputeLimiterValues, Limiters.h:28-67 */
+    double eps2 = w->eps2 ? w->eps2[ci] : 0.0;
+    for (int v = 0; v < NV; ++v) {
+        double umax = val[v], umin = val[v];
+        for (int nb = 0; nb < 2 * nd; ++nb) {
+            double vn = st[nb][v];
+            if (umax < vn) umax = vn;
+            if (umin > vn) umin = vn;
+        }
+        if (umax - umin < 3.0 * DBL_MIN) continue;
+        double lmin = 1.0;
+        for (int f = 0; f < 2 * nd; ++f) {
+            double lv = 1.0;
+            double d2 = proj[f][v];
+            if (c->limiter == ORC_LIM_VENKAT) {
+                if (d2 > 0) lv = lim_venkat(umax, val[v], d2, umax, umin, eps2);
+                if (d2 < 0) lv = lim_venkat(umin, val[v], d2, umax, umin, eps2);
+            } else {
+                if (d2 > 0) lv = lim_bj(umax, val[v], d2);
+                if (d2 < 0) lv = lim_bj(umin, val[v], d2);
+            }
+            if (lmin > lv) lmin = lv;
+        }
+        rl[v] = lmin;
+    }
+}
+
+/* SampleSolution at a face offset along axis a (PiecewiseConstant.h:15,
+   Linear2PointsStencil.h:26-30, Linear2psLim.h:17-21), with the ghost-cell
+   copy semantics of ExchangeReconstructions (:928-1147) handled by the
+   caller passing the source cell. */
+static void sample(const orc_ctx* w, int ci, int a, double s, double* out) {
+    const orc_config* c = w->c;
+    const double* rv = w->rvals + (size_t)ci * NV;
+    if (c->recon == ORC_RECON_PWC) { for (int v = 0; v < NV; ++v) out[v] = rv[v]; return; }
+    const double* rg = w->rgrad + (size_t)ci * 3 * NV;
+    const double* rl = w->rlim + (size_t)ci * NV;
+    vec3 p = {a == 0 ? s : 0.0, a == 1 ? s : 0.0, a == 2 ? s : 0.0};
+    for (int v = 0; v < NV; ++v) {
+        vec3 g = {rg[0 * NV + v], rg[1 * NV + v], rg[2 * NV + v]};
+        if (c->recon == ORC_RECON_LINEAR2_LIM) out[v] = rv[v] + rl[v] * dot3(g, p);
+        else out[v] = rv[v] + dot3(g, p);
+    }
+}
+
+/* Ghost reconstruction objects on periodic axes are deserialised copies of
+   the opposite interior cell's object (ExchangeReconstructions on one rank);
+   only vals, the active-axis gradients and the limiter travel
+   (Linear2PointsStencil.h:117-143, Linear2psLim.h:279-301). */
+static void exchange_recon(orc_ctx* w) {
+    const orc_config* c = w->c;
+    int nd = c->ndims;
+    size_t g3 = 3 * NV;
+#define COPY_RECON(dst, src)                                                              \
+    do {                                                                                  \
+        memcpy(w->rvals + (size_t)(dst) * NV, w->rvals + (size_t)(src) * NV, sizeof(double) * NV); \
+        for (int a_ = 0; a_ < nd; ++a_)                                                   \
+            memcpy(w->rgrad + (size_t)(dst) * g3 + a_ * NV, w->rgrad + (size_t)(src) * g3 + a_ * NV, \
+                   sizeof(double) * NV);                                                  \
+        memcpy(w->rlim + (size_t)(dst) * NV, w->rlim + (size_t)(src) * NV, sizeof(double) * NV); \
+    } while (0)
+    if (c->periodic[0])
+        for (int j = w->jmin; j <= w->jmax; ++j)
+            for (int k = w->kmin; k <= w->kmax; ++k) {
+                COPY_RECON(cidx(w, w->imax + 1, j, k), cidx(w, w->imin, j, k));
+                COPY_RECON(cidx(w, w->imin - 1, j, k), cidx(w, w->imax, j, k));
+            }
+    if (nd > 1 && c->periodic[1])
+        for (int i = w->imin; i <= w->imax; ++i)
+            for (int k = w->kmin; k <= w->kmax; ++k) {
+                COPY_RECON(cidx(w, i, w->jmax + 1, k), cidx(w, i, w->jmin, k));
+                COPY_RECON(cidx(w, i, w->jmin - 1, k), cidx(w, i, w->jmax, k));
+            }
+    if (nd > 2 && c->periodic[2])
+        for (int i = w->imin; i <= w->imax; ++i)
+            for (int j = w->jmin; j <= w->jmax; ++j) {
+                COPY_RECON(cidx(w, i, j, w->kmax + 1), cidx(w, i, j, w->kmin));
+                COPY_RECON(cidx(w, i, j, w->kmin - 1), cidx(w, i, j, w->kmax));
+            }
+#undef COPY_RECON
+}
+
+/* ------------------------------------------------------------------------ */
+/* Riemann solvers                                                          */
+/* ------------------------------------------------------------------------ */
+
+/* Physical flux F(U).n, RoeSolverPerfectGasEOS.h:41-58 (+ stiffened p). */
+static void phys_flux(const orc_config* c, const double* U, vec3 n, double* res) {
+    double ro = U[0];
+    double vx = U[1] / ro;
+    double vy = U[2] / ro;
+    double vz = U[3] / ro;
+    double roE = U[4];
+    double p = eos_pressure(c, ro, vx, vy, vz, roE);
+    double vn = vx * n.x + vy * n.y + vz * n.z;
+    res[0] = ro * vn;
+    res[1] = ro * vn * vx + n.x * p;
+    res[2] = ro * vn * vy + n.y * p;
+    res[3] = ro * vn * vz + n.z * p;
+    res[4] = vn * (roE + p);
+}
+
+static inline double harten(double z, double eps) {
+    z = fabs(z);
+    if (z < eps) z = ((z * z) / eps + eps) * 0.5;
+    return z;
+}
+
+/* RoeSolverPerfectGasEOS::ComputeFlux, RoeSolverPerfectGasEOS.h:74-160.
+   The stiffened-gas variant (not in the reference) only changes the
+   enthalpy, h = (E + p)/rho, through the -g p_inf/rho term. */
+static double roe_flux(const orc_config* c, const double* UL, const double* UR, vec3 fn, double* flux) {
+    const double g = c->gamma;
+    double FL[NV], FR[NV];
+    phys_flux(c, UL, fn, FL);
+    phys_flux(c, UR, fn, FR);
+    for (int i = 0; i < NV; ++i) flux[i] = FL[i] + FR[i];
+    double ro_l = UL[0];
+    double ro_r = UR[0];
+    vec3 vl = {UL[1] / ro_l, UL[2] / ro_l, UL[3] / ro_l};
+    vec3 vr = {UR[1] / ro_r, UR[2] / ro_r, UR[3] / ro_r};
+    double e_l = UL[4] / ro_l;
+    double e_r = UR[4] / ro_r;
+    double k = 0.5 * dot3(vl, vl);
+    double h_l = (e_l - k) * g + k;
+    k = 0.5 * dot3(vr, vr);
+    double h_r = (e_r - k) * g + k;
+    if (c->eos == ORC_EOS_STIFFENED) {
+        h_l = h_l - g * c->p_inf / ro_l;
+        h_r = h_r - g * c->p_inf / ro_r;
+    }
+    double ql = sqrt(ro_l) / (sqrt(ro_l) + sqrt(ro_r));
+    double qr = sqrt(ro_r) / (sqrt(ro_l) + sqrt(ro_r));
+    vec3 vel = {ql * vl.x + qr * vr.x, ql * vl.y + qr * vr.y, ql * vl.z + qr * vr.z};
+    double h = ql * h_l + qr * h_r;
+    double phi2 = 0.5 * (g - 1) * dot3(vel, vel);
+    double dn = 1.0;
+    double cs = sqrt((g - 1) * h - phi2);
+    double uw = dot3(vel, fn);
+    double eig_max = fabs(uw) + cs * dn;
+    double AA1 = harten(uw, c->eps * eig_max);
+    double AA3 = harten(uw + cs * dn, c->eps * eig_max);
+    double AA4 = harten(uw - cs * dn, c->eps * eig_max);
+    double Eig1 = AA1;
+    double Eiga = (AA3 - AA4) * 0.5 / (dn * cs);
+    double Eigb = (AA3 + AA4) * 0.5 - AA1;
+    double Qa[NV] = {0, fn.x, fn.y, fn.z, uw};
+    double Qb[NV] = {1, vel.x, vel.y, vel.z, h};
+    vec3 dvr = {vr.x - vel.x, vr.y - vel.y, vr.z - vel.z};
+    vec3 dvl = {vl.x - vel.x, vl.y - vel.y, vl.z - vel.z};
+    vec3 rfr = {ro_r * fn.x, ro_r * fn.y, ro_r * fn.z};
+    vec3 rfl = {ro_l * fn.x, ro_l * fn.y, ro_l * fn.z};
+    double R1 = phi2 * ro_r - (g - 1) * ro_r * (dot3(vel, vr) - e_r);
+    double D1 = dot3(rfr, dvr);
+    double R2 = phi2 * ro_l - (g - 1) * ro_l * (dot3(vel, vl) - e_l);
+    double D2 = dot3(rfl, dvl);
+    double C2 = 1.0 / (cs * cs);
+    double DN2 = 1.0 / (dn * dn);
+    for (int i = 0; i < NV; ++i) {
+        flux[i] += (Eig1 * UL[i] + Eiga * (R2 * Qa[i] + D2 * Qb[i]) + Eigb * (R2 * Qb[i] * C2 + D2 * Qa[i] * DN2)
+                    - Eig1 * UR[i] - Eiga * (R1 * Qa[i] + D1 * Qb[i]) - Eigb * (R1 * Qb[i] * C2 + D1 * Qa[i] * DN2));
+        flux[i] *= 0.5;
+    }
+    return eig_max;
+}
+
+/* HLLC flux (Toro, ch. 10.4, eqs. 10.37-10.39) with Einfeldt-type wave
+   speeds from Roe averages (Toro eq. 10.52).  Not in the reference: this
+   restatement is its oracle.  MaxEigenvalue = max(|S_L|, |S_R|). */
+static double hllc_flux(const orc_config* c, const double* UL, const double* UR, int a, double* flux) {
+    const double g = c->gamma;
+    const double pinf = (c->eos == ORC_EOS_STIFFENED) ? c->p_inf : 0.0;
+    int m = 1 + a;
+    double rl = UL[0], rr = UR[0];
+    double ul = UL[m] / rl, ur = UR[m] / rr;
+    double vlx = UL[1] / rl, vly = UL[2] / rl, vlz = UL[3] / rl;
+    double vrx = UR[1] / rr, vry = UR[2] / rr, vrz = UR[3] / rr;
+    double pl = eos_pressure(c, rl, vlx, vly, vlz, UL[4]);
+    double pr = eos_pressure(c, rr, vrx, vry, vrz, UR[4]);
+    double cl = sqrt(g * (pl + pinf) / rl);
+    double cr = sqrt(g * (pr + pinf) / rr);
+    double hl = (UL[4] + pl) / rl;
+    double hr = (UR[4] + pr) / rr;
+    double sl = sqrt(rl), sr = sqrt(rr);
+    double wl = sl / (sl + sr), wr = sr / (sl + sr);
+    double ut = wl * ul + wr * ur;
+    double vtx = wl * vlx + wr * vrx, vty = wl * vly + wr * vry, vtz = wl * vlz + wr * vrz;
+    double ht = wl * hl + wr * hr;
+    double ct = sqrt((g - 1) * (ht - 0.5 * (vtx * vtx + vty * vty + vtz * vtz)));
+    double SL = fmin(ul - cl, ut - ct);
+    double SR = fmax(ur + cr, ut + ct);
+    double lam = fmax(fabs(SL), fabs(SR));
+    double ml = rl * (SL - ul), mr = rr * (SR - ur);
+    double sstar = (pr - pl + ul * ml - ur * mr) / (ml - mr);
+    double FL[NV], FR[NV];
+    vec3 n = {a == 0 ? 1.0 : 0.0, a == 1 ? 1.0 : 0.0, a == 2 ? 1.0 : 0.0};
+    if (SL >= 0.0) {
+        phys_flux(c, UL, n, flux);
+    } else if (SR <= 0.0) {
+        phys_flux(c, UR, n, flux);
+    } else if (sstar >= 0.0) {
+        phys_flux(c, UL, n, FL);
+        double coef = ml / (SL - sstar);
+        double us[NV];
+        us[0] = coef;
+        us[1] = coef * vlx; us[2] = coef * vly; us[3] = coef * vlz;
+        us[m] = coef * sstar;
+        us[4] = coef * (UL[4] / rl + (sstar - ul) * (sstar + pl / ml));
+        for (int v = 0; v < NV; ++v) flux[v] = FL[v] + SL * (us[v] - UL[v]);
+    } else {
+        phys_flux(c, UR, n, FR);
+        double coef = mr / (SR - sstar);
+        double us[NV];
+        us[0] = coef;
+        us[1] = coef * vrx; us[2] = coef * vry; us[3] = coef * vrz;
+        us[m] = coef * sstar;
+        us[4] = coef * (UR[4] / rr + (sstar - ur) * (sstar + pr / mr));
+        for (int v = 0; v < NV; ++v) flux[v] = FR[v] + SR * (us[v] - UR[v]);
+    }
+    return lam;
+}
+
+static double riemann(const orc_config* c, const double* UL, const double* UR, int a, double* flux) {
+    vec3 fn = {a == 0 ? 1.0 : 0.0, a == 1 ? 1.0 : 0.0, a == 2 ? 1.0 : 0.0};
+    if (c->solver == ORC_RS_HLLC) return hllc_flux(c, UL, UR, a, flux);
+    return roe_flux(c, UL, UR, fn, flux);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Residual, ExplicitRungeKuttaFVM.h:1150-1424                              */
+/* ------------------------------------------------------------------------ */
+
+/* One line of faces along axis a through the transverse cell (t1,t2). */
+static void residual_line(orc_ctx* w, int a, int p, int q) {
+    const orc_config* c = w->c;
+    int lo = a == 0 ? w->imin : (a == 1 ? w->jmin : w->kmin);
+    int hi = a == 0 ? w->imax : (a == 1 ? w->jmax : w->kmax);
+    const double* hh = a == 0 ? w->hx : (a == 1 ? w->hy : w->hz);
+    double fS;
+    int i, j, k;
+    /* (p,q) are (j,k) for x faces, (i,k) for y faces, (i,j) for z faces. */
+    if (a == 0) {
+        j = p; k = q;
+        fS = 0;
+        if (c->ndims == 1) fS = 1.0;
+        if (c->ndims == 2) fS = w->hy[j];
+        if (c->ndims == 3) fS = w->hy[j] * w->hz[k];
+    } else if (a == 1) {
+        i = p; k = q;
+        fS = w->hx[i];
+        if (c->ndims == 3) fS = w->hx[i] * w->hz[k];
+    } else {
+        i = p; j = q;
+        fS = w->hx[i] * w->hy[j];
+    }
+    double fl[NV] = {0, 0, 0, 0, 0}, fr[NV], UL[NV], UR[NV];
+    vec3 fn = {a == 0 ? 1.0 : 0.0, a == 1 ? 1.0 : 0.0, a == 2 ? 1.0 : 0.0};
+    for (int s = lo; s <= hi + 1; ++s) {
+        if (a == 0) i = s; else if (a == 1) j = s; else k = s;
+        int cm = a == 0 ? cidx(w, s - 1, j, k) : (a == 1 ? cidx(w, i, s - 1, k) : cidx(w, i, j, s - 1));
+        int cp = cidx(w, i, j, k);
+        double hl = 0.5 * hh[s - 1];
+        double hr = -0.5 * hh[s];
+        if (s == lo && !c->periodic[a]) {
+            sample(w, cp, a, hr, UR);
+            bc_dummy_values(c, 2 * a, UR, fn, UL);
+        } else if (s == hi + 1 && !c->periodic[a]) {
+            sample(w, cm, a, hl, UL);
+            bc_dummy_values(c, 2 * a + 1, UL, fn, UR);
+        } else {
+            sample(w, cm, a, hl, UL);
+            sample(w, cp, a, hr, UR);
+        }
+        double lam = riemann(c, UL, UR, a, fr);
+        for (int v = 0; v < NV; ++v) fr[v] -= 0.0; /* fvisc = 0 (inviscid) */
+        w->spectral[cp] += fS * lam;
+        if (s > lo) {
+            for (int v = 0; v < NV; ++v) w->resid[(size_t)cm * NV + v] -= (fr[v] - fl[v]) * fS;
+            w->spectral[cm] += fS * lam;
+            /* viscous spectral-radius term with zero viscosity (:1239-1248) */
+            double roFace = sqrt(UL[0] * UR[0]);
+            double t1 = 4.0 / (3.0 * roFace), t2 = c->gamma / roFace;
+            double vsr = (t1 < t2) ? t2 : t1;
+            vsr *= 0.0 / 1.0;
+            vsr *= fS * fS;
+            vsr /= w->vol[cm];
+            w->spectral[cm] += vsr;
+        }
+        for (int v = 0; v < NV; ++v) fl[v] = fr[v];
+    }
+}
+
+static void compute_residual(orc_ctx* w) {
+    const orc_config* c = w->c;
+    memset(w->spectral, 0, sizeof(double) * w->ncells);
+    memset(w->resid, 0, sizeof(double) * (size_t)w->ncells * NV);
+    int nj = w->jmax - w->jmin + 1, nk = w->kmax - w->kmin + 1, ni = w->imax - w->imin + 1;
+    /* I step (k outer, j inner); lines are independent */
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < nj * nk; ++t) residual_line(w, 0, w->jmin + t % nj, w->kmin + t / nj);
+    if (c->ndims > 1) {
+#pragma omp parallel for schedule(static)
+        for (int t = 0; t < ni * nk; ++t) residual_line(w, 1, w->imin + t % ni, w->kmin + t / ni);
+    }
+    if (c->ndims > 2) {
+#pragma omp parallel for schedule(static)
+        for (int t = 0; t < ni * nj; ++t) residual_line(w, 2, w->imin + t % ni, w->jmin + t / ni);
+    }
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step: ExplicitRungeKuttaFVM::IterationStep, :1440-1491                   */
+/* ------------------------------------------------------------------------ */
+
+static void iteration_step(orc_ctx* w, double* U, orc_step_info* info) {
+    const orc_config* c = w->c;
+    fill_ghosts(w, U);
+    if (c->recon != ORC_RECON_PWC) {
+        int ni = w->imax - w->imin + 1, nj = w->jmax - w->jmin + 1, nk = w->kmax - w->kmin + 1;
+#pragma omp parallel for schedule(static)
+        for (int t = 0; t < ni * nj * nk; ++t) {
+            int i = w->imin + t % ni, j = w->jmin + (t / ni) % nj, k = w->kmin + t / (ni * nj);
+            reconstruct_cell(w, U, i, j, k);
+        }
+    } else {
+        for (int k = w->kmin; k <= w->kmax; ++k)
+            for (int j = w->jmin; j <= w->jmax; ++j)
+                for (int i = w->imin; i <= w->imax; ++i) reconstruct_cell(w, U, i, j, k);
+    }
+    exchange_recon(w);
+    compute_residual(w);
+
+    /* ComputeTimeStep, :1427-1437: (volumes / spectralRadius).min() * CFL,
+       min in libstdc++'s __valarray_min order. */
+    double m = w->vol[0] / w->spectral[0];
+    for (int t = 1; t < w->ncells; ++t) {
+        double r = w->vol[t] / w->spectral[t];
+        if (r < m) m = r;
+    }
+    double dt = m * c->cfl;
+    if ((c->save_solution_time > 0) && (info->next_solution_time < info->time + dt)) dt = info->next_solution_time - info->time;
+    if ((c->save_slice_time > 0) && (info->next_slice_time < info->time + dt)) dt = info->next_slice_time - info->time;
+    info->dt = dt;
+
+    /* UpdateSolution, kernel.h:319-331 */
+#pragma omp parallel for schedule(static)
+    for (int t = 0; t < w->ncells; ++t)
+        for (int v = 0; v < NV; ++v) U[(size_t)t * NV + v] += dt * (w->resid[(size_t)t * NV + v] / w->vol[t]);
+    /* residual norms: (volumes * abs(R)).sum() on a valarray expression,
+       which libstdc++ accumulates from the last element down */
+    for (int v = 0; v < NV; ++v) {
+        int t = w->ncells - 1;
+        double s = w->vol[t] * fabs(w->resid[(size_t)t * NV + v]);
+        while (t != 0) { --t; s += w->vol[t] * fabs(w->resid[(size_t)t * NV + v]); }
+        info->residual[v] = s;
+    }
+    info->time += dt;
+    info->iteration++;
+}
+
+int orc_advance(const orc_config* c, double* values, int n_steps, orc_step_info* info) {
+#ifdef _OPENMP
+    if (c->threads > 0) omp_set_num_threads(c->threads);
+#endif
+    orc_ctx w;
+    memset(&w, 0, sizeof w);
+    w.c = c;
+    orc_dims(c, &w.nxa, &w.nya, &w.nza);
+    w.ncells = w.nxa * w.nya * w.nza;
+    w.gx = 1; w.gy = c->ndims > 1; w.gz = c->ndims > 2;
+    w.imin = 1; w.imax = c->nx;
+    w.jmin = w.gy; w.jmax = c->ndims > 1 ? c->ny : 0;
+    w.kmin = w.gz; w.kmax = c->ndims > 2 ? c->nz : 0;
+    w.x = malloc(sizeof(double) * w.nxa); w.hx = malloc(sizeof(double) * w.nxa);
+    w.y = malloc(sizeof(double) * w.nya); w.hy = malloc(sizeof(double) * w.nya);
+    w.z = malloc(sizeof(double) * w.nza); w.hz = malloc(sizeof(double) * w.nza);
+    orc_grid(c, w.x, w.hx, w.y, w.hy, w.z, w.hz);
+    w.vol = malloc(sizeof(double) * w.ncells);
+    w.spectral = malloc(sizeof(double) * w.ncells);
+    w.resid = malloc(sizeof(double) * (size_t)w.ncells * NV);
+    w.rvals = calloc((size_t)w.ncells * NV, sizeof(double));
+    w.rgrad = calloc((size_t)w.ncells * 3 * NV, sizeof(double));
+    w.rlim = calloc((size_t)w.ncells * NV, sizeof(double));
+    if (!w.vol || !w.spectral || !w.resid || !w.rvals || !w.rgrad || !w.rlim) return 1;
+    for (int k = 0; k < w.nza; ++k)
+        for (int j = 0; j < w.nya; ++j)
+            for (int i = 0; i < w.nxa; ++i) w.vol[cidx(&w, i, j, k)] = w.hx[i] * w.hy[j] * w.hz[k];
+    if (c->recon == ORC_RECON_LINEAR2_LIM && c->limiter == ORC_LIM_VENKAT) {
+        /* limVenkatar::SendCellInfo, Limiters.h:93-96, K = 5 (Constants.h:11) */
+        w.eps2 = malloc(sizeof(double) * w.ncells);
+        for (int k = 0; k < w.nza; ++k)
+            for (int j = 0; j < w.nya; ++j)
+                for (int i = 0; i < w.nxa; ++i) {
+                    double dx = pow(w.hx[i] * w.hy[j] * w.hz[k], 1.0 / c->ndims);
+                    w.eps2[cidx(&w, i, j, k)] = pow(5.0 * dx, 3.0);
+                }
+    }
+    if (n_steps >= 0) {
+        for (int s = 0; s < n_steps; ++s) iteration_step(&w, values, info);
+    } else {
+        /* Kernel::Run, kernel.h:1701-1850 */
+        for (;;) {
+            iteration_step(&w, values, info);
+            if ((c->save_solution_time > 0) && (info->next_solution_time == info->time))
+                info->next_solution_time += c->save_solution_time;
+            if ((c->save_slice_time > 0) && (info->next_slice_time == info->time))
+                info->next_slice_time += c->save_slice_time;
+            if (info->iteration == c->max_iteration) break;
+            if (info->time >= c->max_time) break;
+        }
+    }
+    free(w.x); free(w.hx); free(w.y); free(w.hy); free(w.z); free(w.hz);
+    free(w.vol); free(w.spectral); free(w.resid); free(w.rvals); free(w.rgrad); free(w.rlim); free(w.eps2);
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Exact Riemann solver (Toro ch. 4) for a stiffened gas                    */
+/* ------------------------------------------------------------------------ */
+
+static void pressure_fn(double g, double pinf, double p, double rk, double pk, double ck, double* f, double* fd) {
+    double pp = p + pinf, pkk = pk + pinf;
+    if (p <= pk) { /* rarefaction */
+        double pr = pp / pkk;
+        *f = 2.0 * ck / (g - 1.0) * (pow(pr, (g - 1.0) / (2.0 * g)) - 1.0);
+        *fd = (1.0 / (rk * ck)) * pow(pr, -(g + 1.0) / (2.0 * g));
+    } else { /* shock */
+        double A = 2.0 / ((g + 1.0) * rk);
+        double B = (g - 1.0) / (g + 1.0) * pkk;
+        double qrt = sqrt(A / (pp + B));
+        *f = (p - pk) * qrt;
+        *fd = (1.0 - 0.5 * (p - pk) / (B + pp)) * qrt;
+    }
+}
+
+int orc_exact_riemann(double g, double pinf, double rl, double ul, double pl, double rr, double ur, double pr,
+                      double s, double* rho, double* u, double* p) {
+    double cl = sqrt(g * (pl + pinf) / rl), cr = sqrt(g * (pr + pinf) / rr);
+    /* two-rarefaction initial guess in p + p_inf, Toro eq. 4.46 */
+    double z = (g - 1.0) / (2.0 * g);
+    double num = cl + cr - 0.5 * (g - 1.0) * (ur - ul);
+    double den = cl / pow(pl + pinf, z) + cr / pow(pr + pinf, z);
+    double ps = pow(num / den, 1.0 / z) - pinf;
+    if (!(ps > -pinf)) ps = 0.5 * (pl + pr);
+    int it = 0;
+    for (; it < 200; ++it) {
+        double fl, fdl, fr, fdr;
+        pressure_fn(g, pinf, ps, rl, pl, cl, &fl, &fdl);
+        pressure_fn(g, pinf, ps, rr, pr, cr, &fr, &fdr);
+        double pn = ps - (fl + fr + ur - ul) / (fdl + fdr);
+        if (pn + pinf <= 0.0) pn = 0.5 * (ps + pinf) - pinf; /* keep p + p_inf positive */
+        double ch = 2.0 * fabs(pn - ps) / fabs(pn + ps + 2.0 * pinf);
+        ps = pn;
+        if (ch < 1e-15) break;
+    }
+    double fl, fdl, fr, fdr;
+    pressure_fn(g, pinf, ps, rl, pl, cl, &fl, &fdl);
+    pressure_fn(g, pinf, ps, rr, pr, cr, &fr, &fdr);
+    double us = 0.5 * (ul + ur) + 0.5 * (fr - fl);
+    double gm = (g - 1.0) / (g + 1.0);
+    double PS = ps + pinf, PL = pl + pinf, PR = pr + pinf;
+    if (s <= us) {
+        if (ps > pl) { /* left shock */
+            double sh = ul - cl * sqrt((g + 1.0) / (2.0 * g) * PS / PL + (g - 1.0) / (2.0 * g));
+            if (s <= sh) { *rho = rl; *u = ul; *p = pl; }
+            else { *rho = rl * (PS / PL + gm) / (gm * PS / PL + 1.0); *u = us; *p = ps; }
+        } else { /* left rarefaction */
+            double shl = ul - cl;
+            double cs = cl * pow(PS / PL, z);
+            double stl = us - cs;
+            if (s <= shl) { *rho = rl; *u = ul; *p = pl; }
+            else if (s >= stl) { *rho = rl * pow(PS / PL, 1.0 / g); *u = us; *p = ps; }
+            else {
+                double cc = 2.0 / (g + 1.0) + gm / cl * (ul - s);
+                *rho = rl * pow(cc, 2.0 / (g - 1.0));
+                *u = 2.0 / (g + 1.0) * (cl + 0.5 * (g - 1.0) * ul + s);
+                *p = PL * pow(cc, 2.0 * g / (g - 1.0)) - pinf;
+            }
+        }
+    } else {
+        if (ps > pr) { /* right shock */
+            double sh = ur + cr * sqrt((g + 1.0) / (2.0 * g) * PS / PR + (g - 1.0) / (2.0 * g));
+            if (s >= sh) { *rho = rr; *u = ur; *p = pr; }
+            else { *rho = rr * (PS / PR + gm) / (gm * PS / PR + 1.0); *u = us; *p = ps; }
+        } else { /* right rarefaction */
+            double shr = ur + cr;
+            double cs = cr * pow(PS / PR, z);
+            double str = us + cs;
+            if (s >= shr) { *rho = rr; *u = ur; *p = pr; }
+            else if (s <= str) { *rho = rr * pow(PS / PR, 1.0 / g); *u = us; *p = ps; }
+            else {
+                double cc = 2.0 / (g + 1.0) - gm / cr * (ur - s);
+                *rho = rr * pow(cc, 2.0 / (g - 1.0));
+                *u = 2.0 / (g + 1.0) * (-cr + 0.5 * (g - 1.0) * ur + s);
+                *p = PR * pow(cc, 2.0 * g / (g - 1.0)) - pinf;
+            }
+        }
+    }
+    return it;
+}
