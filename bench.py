@@ -1,0 +1,346 @@
+#!/usr/bin/env python
+"""Benchmark of the explicit FVM residual + stage update on one GB300.
+
+Workload (the configuration the headline metric is quoted on): 3D ideal-gas
+blast on a 256^3 grid with reflective (Symmetry) walls, FP64 state,
+background rho = 1 (+-1% seeded noise), p = 0.1, sphere of radius 0.1 at the
+centre with p = 10; limited linear reconstruction (Linear2psLim, Barth-
+Jespersen), Roe flux, RK1 (the reference's only stage), CFL 0.4.  A "step" is
+one RK step over the whole grid; one cell-update is one cell advanced by one
+stage.  The state (687 MB FP64 per copy) is larger than L2, so no flush is
+needed between steps.
+
+Lines printed (rank 0, one JSON line):
+  --impl ours       value  = cell-updates/s with the state resident in HBM,
+                             device-timed with CUDA events on the library stream
+                    e2e    = same metric through the C ABI with host buffers
+                             (pinned H2D of the initial state, K steps, D2H of
+                             the final state) timed on the host
+                    roofline, cpu_baseline (oracle port on this host's cores),
+                    clocks, fp64 plain-path rate and mixed-vs-FP64 errors
+  --impl reference  the reference algorithm's CPU implementation (the
+                    oracle port, all host threads) on a bounded sample of the
+                    same workload: each step is one RK step over a
+                    256x256x16 slab of the blast.
+With torchrun (N>1) every rank advances its own replica (weak scaling).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "cell-updates/s"
+N_DEFAULT = 256
+BLAST = [1.0, 0.1, 10.0, 0.1, 0.01]  # rho, p_out, p_in, radius, noise
+SEED = 2024
+BYTES_PER_CELL_UPDATE = 80  # one FP64 read + one FP64 write of the 5 conserved values
+
+
+def workload_case(capi, n, nz=None, periodic_z=False):
+    sym = (capi.BC_SYMMETRY, 0.0, (0.0, 0.0, 0.0), 0.0)
+    return capi.make_case(ndims=3, nx=n, ny=n, nz=nz or n, periodic=(0, 0, 1 if periodic_z else 0),
+                          recon=capi.RECON_LINEAR2_LIM, limiter=capi.LIM_BJ, solver=capi.RS_ROE, cfl=0.4,
+                          eps=0.0, max_iter=200, max_time=1e30, bc=[sym] * 6)
+
+
+def workload_config(n, precision, steps):
+    return {"workload": f"3D ideal-gas blast {n}^3, Symmetry walls, Linear2psLim(BJ)+Roe, RK1, CFL 0.4",
+            "grid": [n, n, n], "cells": n ** 3, "steps_timed": steps, "precision": precision,
+            "state": "FP64 SoA in HBM (687 MB per copy at 256^3)",
+            "l2": "inputs larger than L2 (129 MB); no flush needed", "parallelism": "replicas"}
+
+
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    if ws <= 1:
+        return 0, 1, 0, None
+    import torch
+    import torch.distributed as dist
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(lr)
+    dist.init_process_group("nccl")
+    return dist.get_rank(), ws, lr, dist
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+    Q = ("uuid,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, uuid):
+        self.uuid = uuid
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(", ") for r in self.f.read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        rows = [r for r in rows if len(r) >= 9 and (self.uuid is None or r[0].strip() in self.uuid)]
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].strip().lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": float(rows[0][2]) if rows[0][2].strip().replace(".", "").isdigit() else None,
+                "samples": len(rows), "reasons": reasons}
+
+
+def gpu_uuid(dev):
+    try:
+        import torch
+        u = torch.cuda.get_device_properties(dev).uuid
+        return "GPU-" + str(u)
+    except Exception:
+        return None
+
+
+def measured_peak():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+def profile_traffic(kernel):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except Exception:
+        return None
+
+
+def oracle_sample_rate(steps, warmup, threads, nz=16, n=N_DEFAULT):
+    """The reference algorithm on the CPU (oracle port, OpenMP): cell-updates/s
+    of RK steps over a 256 x 256 x nz slab through the blast centre."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from turbostructred_gb300 import capi
+    case = workload_case(capi, n, nz=nz, periodic_z=True)
+    full_case = workload_case(capi, n)
+    ic = capi.fill_scenario(full_case, capi.SCENARIO_BLAST, SEED, BLAST)
+    k0 = n // 2 - nz // 2
+    sub = np.ascontiguousarray(ic[k0:k0 + nz])
+    full = O.embed(case, sub)
+    ocase = dict(case)
+    if warmup:
+        full, _ = O.advance(ocase, full, warmup, threads=threads)
+    t0 = time.perf_counter()
+    full, info = O.advance(ocase, full, steps, threads=threads)
+    dt = time.perf_counter() - t0
+    cells = n * n * nz
+    return cells * steps / dt, dt, f"{steps} RK step(s) over a {n}x{n}x{nz} slab of the {n}^3 blast (planes {k0}-{k0 + nz - 1}), z periodic"
+
+
+def run_reference(args, rank, ws):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rate, secs, sample = oracle_sample_rate(args.steps, args.warmup, threads)
+    line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": workload_config(args.n, "fp64", args.steps),
+            "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def rel_errors(a, b):
+    import numpy as np
+    out = {}
+    for name, v in (("rho", 0), ("mom", slice(1, 4)), ("E", 4)):
+        x, y = a[..., v], b[..., v]
+        out[f"L1_{name}"] = float(np.abs(x - y).sum() / max(np.abs(y).sum(), 1e-300))
+        out[f"Linf_{name}"] = float(np.abs(x - y).max() / max(np.abs(y).max(), 1e-300))
+    return out
+
+
+def run_ours(args, rank, ws, lr, dist):
+    import numpy as np
+    import torch
+
+    from turbostructred_gb300 import build, capi
+    if rank == 0 or dist is None:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    capi.load()
+    n = args.n
+    case = workload_case(capi, n)
+    ic = capi.fill_scenario(case, capi.SCENARIO_BLAST, SEED + rank, BLAST)
+    cells = n ** 3
+
+    precision = args.precision
+    if precision == "auto":
+        try:
+            with capi.Solver(workload_case(capi, 8), capi.PRECISION_MIXED, device=lr):
+                precision = "mixed"
+        except capi.TsError:
+            precision = "fp64"
+    prec_id = capi.PRECISION_MIXED if precision == "mixed" else capi.PRECISION_FP64
+
+    solver = capi.Solver(case, prec_id, device=lr)
+    solver.set_state(ic)
+    if args.warmup:
+        solver.step(args.warmup)
+    solver.synchronize()
+    uuid = gpu_uuid(lr)
+    sampler = ClockSampler(uuid)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    info, timing = solver.step_timed(args.steps)
+    torch.cuda.synchronize()
+    if dist is not None:
+        dist.barrier()
+    clocks = sampler.stop()
+    t_ms = timing["total_ms"]
+    if dist is not None:
+        t = torch.tensor([t_ms], device=f"cuda:{lr}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = ws * cells * args.steps / (t_ms / 1e3)
+
+    # roofline of the dominant kernel
+    kernels = timing["kernels"]
+    top = max(kernels, key=kernels.get)
+    top_ms = kernels[top]
+    peak, peak_kind = measured_peak()
+    if precision == "mixed":
+        alg = BYTES_PER_CELL_UPDATE * cells
+        alg_note = "80 B x cells per launch (one fused launch advances every cell one stage)"
+    else:
+        alg = BYTES_PER_CELL_UPDATE * cells
+        alg_note = "80 B x cells per step, charged to the dominant kernel of the FP64 path"
+    achieved = alg / (top_ms / 1e3) / 1e9
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": profile_traffic(top), "kernel": top, "kernel_ms": top_ms,
+                "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
+                "algorithmic_bytes": alg, "algorithmic_note": alg_note,
+                "step_kernels_ms": kernels}
+
+    extra = {}
+    # FP64 plain path at the same size (short run) and mixed-vs-FP64 error
+    if precision == "mixed" and not args.skip_fp64:
+        fp = capi.Solver(case, capi.PRECISION_FP64, device=lr)
+        fp.set_state(ic)
+        fp.step(2)
+        _, tfp = fp.step_timed(args.fp64_steps)
+        fp64_rate = cells * args.fp64_steps / (tfp["total_ms"] / 1e3)
+        extra["fp64_value"] = fp64_rate
+        extra["mixed_over_fp64"] = value / ws / fp64_rate
+        # accuracy: same IC, same steps
+        fp.set_state(ic)
+        fp.set_info(iteration=0, time=0.0, dt=0.0)
+        fp.step(args.err_steps)
+        ref = fp.get_state()
+        mx = capi.Solver(case, capi.PRECISION_MIXED, device=lr)
+        mx.set_state(ic)
+        mx.step(args.err_steps)
+        got = mx.get_state()
+        extra["mixed_error_vs_fp64"] = dict(steps=args.err_steps, **rel_errors(got, ref))
+        fp.close()
+        mx.close()
+
+    # end to end through the C ABI with host buffers
+    e2e = None
+    if not args.skip_e2e:
+        host_in = torch.from_numpy(ic.reshape(-1)).pin_memory()
+        host_out = torch.empty(ic.size, dtype=torch.float64).pin_memory()
+        lib = capi.load()
+        import ctypes as C
+        P = C.POINTER(C.c_double)
+        e2e_steps = args.steps
+        times = []
+        for job in range(args.e2e_jobs + 1):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            capi.check(lib.ts_set_state(solver.h, C.cast(host_in.data_ptr(), P), capi.LAYOUT_INTERIOR))
+            solver.set_info(iteration=0, time=0.0, dt=0.0)
+            solver.step(e2e_steps)
+            capi.check(lib.ts_get_state(solver.h, C.cast(host_out.data_ptr(), P), capi.LAYOUT_INTERIOR))
+            t1 = time.perf_counter()
+            if job > 0:
+                times.append(t1 - t0)
+        tj = statistics.median(times)
+        state_bytes = ic.size * 8
+        e2e = {"value": ws * cells * e2e_steps / tj, "unit": "cell-updates/s",
+               "h2d_bytes_per_step": state_bytes / e2e_steps, "d2h_bytes_per_step": state_bytes / e2e_steps,
+               "job": f"H2D of the {n}^3 initial state from pinned host memory, {e2e_steps} steps, D2H of the final state",
+               "h2d_bytes_per_job": state_bytes, "d2h_bytes_per_job": state_bytes, "seconds_per_job": tj}
+    solver.close()
+
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        rate, secs, sample = oracle_sample_rate(args.cpu_steps, 1, threads, nz=args.cpu_nz, n=n)
+        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port", "sample": sample,
+               "seconds": secs}
+
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 flux" if precision == "mixed" else "f64",
+                "data": "synthetic (seeded blast initial state, no dataset)",
+                "config": workload_config(n, precision, args.steps), "e2e": e2e, "roofline": roofline,
+                "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": timing["launches"] * ws,
+                "step_info": {"iteration": info["iteration"], "time": info["time"], "dt": info["dt"],
+                              "health": info["health"]}}
+        line.update(extra)
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
+    p.add_argument("--n", type=int, default=N_DEFAULT)
+    p.add_argument("--fp64-steps", type=int, default=5)
+    p.add_argument("--err-steps", type=int, default=50)
+    p.add_argument("--e2e-jobs", type=int, default=2)
+    p.add_argument("--cpu-steps", type=int, default=2)
+    p.add_argument("--cpu-nz", type=int, default=32)
+    p.add_argument("--skip-fp64", action="store_true")
+    p.add_argument("--skip-e2e", action="store_true")
+    p.add_argument("--skip-cpu", action="store_true")
+    args = p.parse_args()
+    if args.impl == "reference":
+        rank = int(os.environ.get("RANK", "0"))
+        run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))
+        return
+    rank, ws, lr, dist = dist_init()
+    run_ours(args, rank, ws, lr, dist)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,219 @@
+/*
+ * ts_fvm.h -- C ABI of the GB300-native explicit finite-volume step.
+ *
+ * This is the drop-in boundary for TurboStructred's hot path: the explicit
+ * FVM residual and stage update of ExplicitRungeKuttaFVM<R>
+ * (src/Methods/ExplicitRungeKuttaFVM.h:15-1493) together with the Kernel
+ * state, ghost fill, CFL time step and update it drives (src/kernel/kernel.h).
+ * Plain C types only: no CUDA, C++ or torch types cross this boundary.
+ *
+ * Plugin selection keeps the reference's enum values
+ * (src/Methods/MethodConfiguration.h:5-23,
+ *  src/BoundaryConditions/BoundaryConditionConfiguration.h:12-19); values this
+ * project adds (HLLC, stiffened gas, precision modes) are appended after them.
+ *
+ * Errors: every call returns a ts_status; ts_last_error() gives the message
+ * of the most recent failure on the calling thread.  Handles are not
+ * thread-safe: one host thread drives one handle.  Each handle owns one CUDA
+ * stream on its device.
+ */
+#ifndef TS_FVM_H
+#define TS_FVM_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define TS_FVM_ABI_VERSION 1
+
+typedef enum ts_status {
+    TS_OK = 0,
+    TS_ERR_INVALID = 1,      /* bad argument or configuration */
+    TS_ERR_UNSUPPORTED = 2,  /* valid in the reference but not built here */
+    TS_ERR_CUDA = 3,         /* CUDA runtime error (message has details) */
+    TS_ERR_NO_MEMORY = 4,    /* device or host allocation failed / budget */
+    TS_ERR_NUMERIC = 5,      /* NaN, rho <= 0 or p <= 0 detected */
+    TS_ERR_TIMEOUT = 6,      /* a bounded device wait gave up */
+    TS_ERR_BUSY = 7,         /* resource in use (e.g. server full) */
+    TS_ERR_NOT_FOUND = 8     /* unknown request id */
+} ts_status;
+
+/* Reconstruction (MethodConfiguration.h:5-10) */
+enum {
+    TS_RECON_PIECEWISE_CONSTANT = 0,
+    TS_RECON_LINEAR_2POINTS = 1,
+    TS_RECON_ENO2_2POINTS = 2,
+    TS_RECON_LINEAR_2POINTS_LIMITED = 3
+};
+/* RPSolver (MethodConfiguration.h:13-17) + HLLC (new) */
+enum { TS_RS_GODUNOV = 0, TS_RS_ROE_PIKE = 1, TS_RS_NONE = 2, TS_RS_HLLC = 3 };
+/* LimiterType (MethodConfiguration.h:20-23) */
+enum { TS_LIM_BARTH_JESPERSEN = 0, TS_LIM_VENKATAKRISHNAN = 1 };
+/* BoundaryConditionType (BoundaryConditionConfiguration.h:12-19) */
+enum {
+    TS_BC_WALL = 0,
+    TS_BC_SYMMETRY = 1,
+    TS_BC_MOVING_WALL = 2,
+    TS_BC_SUBSONIC_INLET = 3,
+    TS_BC_SUBSONIC_OUTLET = 4,
+    TS_BC_NATURAL = 5
+};
+/* Equation of state: ideal gas (the reference's, RoeSolverPerfectGasEOS.h:23)
+   and stiffened gas p = (gamma-1) rho e - gamma p_inf (new). */
+enum { TS_EOS_IDEAL_GAS = 0, TS_EOS_STIFFENED_GAS = 1 };
+/* Precision: all-FP64 (bit-for-bit with the reference), or FP32
+   reconstruction/EOS/flux with FP64 state, stage accumulation and dt. */
+enum { TS_PRECISION_FP64 = 0, TS_PRECISION_MIXED = 1 };
+/* Host state layouts for ts_set_state / ts_get_state. */
+enum {
+    TS_LAYOUT_INTERIOR = 0,   /* interior cells only, x fastest, 5 doubles per cell */
+    TS_LAYOUT_WITH_GHOSTS = 1 /* the reference's Kernel::values array (kernel.h:88-96) */
+};
+/* Health flags reported in ts_step_info.health */
+enum { TS_HEALTH_NAN = 1u, TS_HEALTH_NEG_DENSITY = 2u, TS_HEALTH_NEG_PRESSURE = 4u };
+
+/* BlockNode (KernelConfiguration.h:10-19): stretched-grid block start. */
+typedef struct ts_block_node {
+    double pos;
+    double q_com;
+    int32_t n_cells;
+    int32_t reserved;
+} ts_block_node;
+
+/* BoundaryConditionConfiguration (BoundaryConditionConfiguration.h:21-35). */
+typedef struct ts_bc_config {
+    int32_t type;
+    int32_t reserved;
+    double density;
+    double velocity[3];
+    double pstatic;
+    double temperature;
+} ts_bc_config;
+
+/* KernelConfiguration (KernelConfiguration.h:21-93) with its
+   MethodConfiguration (MethodConfiguration.h:26-37), reduced to the fields the
+   explicit inviscid step reads.  One BC per domain side, in the order
+   x-, x+, y-, y+, z-, z+ (the reference's trivial-marker DomainBCinfo). */
+typedef struct ts_config {
+    int32_t abi_version;   /* TS_FVM_ABI_VERSION */
+    int32_t n_dims;        /* nDims */
+    int32_t nx, ny, nz;    /* nX, nY, nZ */
+    int32_t periodic[3];   /* isPeriodicX/Y/Z */
+    double length[3];      /* LX, LY, LZ */
+    int32_t n_blocks[3];   /* CompressionX/Y/Z sizes; 0 = uniform */
+    int32_t reserved0;
+    const ts_block_node* blocks[3];
+    double gamma;          /* Gamma */
+    int32_t eos;           /* TS_EOS_* */
+    int32_t reserved1;
+    double p_inf;          /* stiffened-gas constant (0 for ideal gas) */
+    int32_t reconstruction;  /* ReconstructionType */
+    int32_t riemann_solver;  /* RiemannProblemSolver */
+    int32_t limiter;         /* GeneralLimitter */
+    int32_t rk_order;        /* RungeKuttaOrder (the reference always runs 1 stage) */
+    double cfl;              /* CFL */
+    double eps;              /* Eps (Harten entropy fix) */
+    int32_t max_iteration;   /* MaxIteration */
+    int32_t reserved2;
+    double max_time;         /* MaxTime */
+    double save_solution_time; /* SaveSolutionTime: clips dt (ExplicitRungeKuttaFVM.h:1433) */
+    double save_slice_time;    /* SaveSliceTime: clips dt (ExplicitRungeKuttaFVM.h:1434) */
+    ts_bc_config bc[6];
+    int32_t precision;       /* TS_PRECISION_* */
+    int32_t device;          /* CUDA device ordinal */
+} ts_config;
+
+/* StepInfo (kernel.h:31-39) plus a health word. */
+typedef struct ts_step_info {
+    int32_t iteration;
+    uint32_t health;
+    double time;
+    double dt;
+    double next_solution_time;
+    double next_slice_time;
+    double residual[5];  /* volume-weighted L1 residual norms (kernel.h:326) */
+} ts_step_info;
+
+typedef struct ts_handle ts_handle;
+
+/* Replaces `new ExplicitRungeKuttaFVM<R>` + Kernel::Init (kernel.h:178-281)
+   and the factory CreateKernel (ExplicitRungeKuttaFVM.h:1496-1513): grid,
+   boundary conditions and method set-up, device state allocation. */
+ts_status ts_create(const ts_config* cfg, ts_handle** out);
+
+/* Releases device memory and the stream (Kernel::Finalize, kernel.h:1879). */
+void ts_destroy(ts_handle* h);
+
+/* Writes the conserved state, like Kernel::SetInitialConditions
+   (kernel.h:125-146) for a point-sampled field, from a host array. */
+ts_status ts_set_state(ts_handle* h, const double* values, int32_t layout);
+
+/* Same from a device pointer on the handle's device (no host copy). */
+ts_status ts_set_state_device(ts_handle* h, const double* device_values, int32_t layout);
+
+/* Reads Kernel::values back (kernel.h:88). */
+ts_status ts_get_state(ts_handle* h, double* values, int32_t layout);
+
+/* n_steps calls of ExplicitRungeKuttaFVM::IterationStep (:1440-1491). */
+ts_status ts_step(ts_handle* h, int32_t n_steps, ts_step_info* info);
+
+/* Device timing of n steps, for benchmarks: CUDA events recorded on the
+   handle's stream around the whole run and around every kernel launch
+   (launched one by one, not from a graph).  Per-kernel times are averages
+   per launch; names identify the kernels of one step in launch order. */
+#define TS_MAX_KERNELS 12
+typedef struct ts_timing {
+    double total_ms;
+    int32_t n_kernels;        /* kernels per step */
+    int32_t launches;         /* kernel launches in the timed region */
+    double kernel_ms[TS_MAX_KERNELS];
+    char kernel_name[TS_MAX_KERNELS][32];
+} ts_timing;
+ts_status ts_step_timed(ts_handle* h, int32_t n_steps, ts_step_info* info, ts_timing* timing);
+
+/* Kernel::Run (kernel.h:1635-1876): steps until MaxIteration or MaxTime,
+   with the reference's termination order and dt overshoot. */
+ts_status ts_run(ts_handle* h, ts_step_info* info);
+
+/* Current StepInfo; and setting it (resume from a checkpoint,
+   Kernel::LoadSolution kernel.h:1031-1079 restores Time). */
+ts_status ts_get_step_info(ts_handle* h, ts_step_info* info);
+ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info);
+
+/* Waits for all work queued on the handle's stream. */
+ts_status ts_synchronize(ts_handle* h);
+
+/* Cell centres and sizes with one ghost layer per active axis, exactly as
+   Grid::InitLocal accumulates them (grid.h:124-344).  Host-only; any pointer
+   may be NULL.  Array lengths are nx+2, (ny+2 | 1), (nz+2 | 1). */
+ts_status ts_grid_coordinates(const ts_config* cfg, double* x, double* hx, double* y, double* hy,
+                              double* z, double* hz);
+
+/* Number of doubles in a host state array of the given layout. */
+size_t ts_state_doubles(const ts_config* cfg, int32_t layout);
+
+/* Synthetic initial states of the benchmark scenarios (host-only, no GPU),
+   point-sampled at the grid's cell centres with a counter-based hash RNG of
+   (seed, i, j, k), written in TS_LAYOUT_INTERIOR order.  See ts_scenario. */
+enum {
+    TS_SCENARIO_SHOCK_TUBE = 0, /* params: x0, rhoL, uL, pL, rhoR, uR, pR */
+    TS_SCENARIO_SHEAR_LAYER = 1, /* params: rho_in, rho_out, u, p, noise amplitude */
+    TS_SCENARIO_BLAST = 2,       /* params: rho, p_out, p_in, radius, noise amplitude */
+    TS_SCENARIO_QUADRANTS = 3    /* params: 4 x (rho, u, v, p) for quadrants ++,-+,--,+- */
+};
+ts_status ts_fill_scenario(const ts_config* cfg, int32_t scenario, uint64_t seed, const double* params,
+                           int32_t n_params, double* values);
+
+/* The hash RNG the scenarios use: uniform double in [0,1). */
+double ts_hash_uniform(uint64_t seed, int64_t i, int64_t j, int64_t k);
+
+const char* ts_last_error(void);
+const char* ts_status_string(ts_status s);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

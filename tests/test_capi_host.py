@@ -1,0 +1,101 @@
+"""The C-ABI library without a GPU: it loads, exports every entry point that
+include/*.h declares, and its host-side logic (grid accumulation, scenarios,
+configuration checks) is right.  No device work is attempted here."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import numpy as np
+import pytest
+
+from conftest import ROOT, golden_names, load_golden
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if not f.endswith(".h"):
+            continue
+        text = open(os.path.join(inc, f)).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        for m in re.finditer(r"\b(ts_[a-z0-9_]+)\s*\(", text):
+            names.add(m.group(1))
+    return names
+
+
+def test_library_exports_all_declared_symbols(tslib):
+    from turbostructred_gb300 import capi
+    out = subprocess.run(["nm", "-D", "--defined-only", capi.LIB_PATH], capture_output=True, text=True).stdout
+    exported = {line.split()[-1] for line in out.splitlines() if line.split()}
+    missing = declared_symbols() - exported
+    assert not missing, missing
+    for name in declared_symbols():
+        assert hasattr(tslib, name)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_host_grid_matches_reference(name, tslib):
+    from turbostructred_gb300 import capi
+    g = load_golden(name)
+    case = capi.make_case(**g["case"])
+    for mine, ref in zip(capi.grid_coordinates(case), (g["x"], g["hx"], g["y"], g["hy"], g["z"], g["hz"])):
+        assert np.array_equal(mine, ref)
+
+
+def test_scenarios_deterministic_and_shaped(tslib):
+    from turbostructred_gb300 import capi
+    case = capi.make_case(ndims=3, nx=8, ny=6, nz=5)
+    a = capi.fill_scenario(case, capi.SCENARIO_BLAST, 3, [1.0, 0.1, 10.0, 0.2, 0.01])
+    b = capi.fill_scenario(case, capi.SCENARIO_BLAST, 3, [1.0, 0.1, 10.0, 0.2, 0.01])
+    c = capi.fill_scenario(case, capi.SCENARIO_BLAST, 4, [1.0, 0.1, 10.0, 0.2, 0.01])
+    assert a.shape == (5, 6, 8, 5)
+    assert np.array_equal(a, b) and not np.array_equal(a, c)
+    assert np.all(np.abs(a[..., 0] - 1.0) <= 0.01 + 1e-15)
+    p = a[..., 4] * 0.4
+    assert set(np.round(np.unique(p), 12)) <= {0.1 * 1.0, 10.0}
+    # the hash RNG depends on (seed, i, j, k) only
+    u = tslib.ts_hash_uniform(3, 1, 2, 3)
+    assert 0.0 <= u < 1.0 and u == tslib.ts_hash_uniform(3, 1, 2, 3)
+
+
+def test_shear_layer_matches_config(tslib):
+    from turbostructred_gb300 import capi
+    case = capi.make_case(ndims=2, nx=16, ny=16)
+    s = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 1, [2.0, 1.0, 0.5, 2.5, 0.01])[0]
+    y = capi.grid_coordinates(case)[2][1:-1]
+    inner = np.abs(y - 0.5) < 0.25
+    assert np.all(s[inner, :, 0] == 2.0) and np.all(s[~inner, :, 0] == 1.0)
+    assert np.allclose(s[inner, :, 1], 1.0) and np.allclose(s[~inner, :, 1], -0.5)
+    v = s[..., 2] / s[..., 0]
+    assert np.abs(v).max() <= 0.01 and np.abs(v).max() > 0.005
+
+
+@pytest.mark.parametrize("bad", [
+    dict(ndims=4), dict(nx=1), dict(gamma=1.0), dict(cfl=0.0), dict(recon=7), dict(limiter=5),
+    dict(solver=9), dict(solver=2), dict(eps=-1.0), dict(length=(0.0, 1.0, 1.0)),
+    dict(ndims=2, ny=1), dict(blocks={0: [(0.0, 1.0, 3)]}),
+])
+def test_invalid_configurations_rejected(bad, tslib):
+    from turbostructred_gb300 import capi
+    case = capi.make_case(**dict(dict(ndims=1, nx=8), **bad))
+    cfg, keep = capi.to_config(case)
+    h = C.c_void_p()
+    st = tslib.ts_create(C.byref(cfg), C.byref(h))
+    assert st == 1, (st, tslib.ts_last_error())
+    assert tslib.ts_last_error()
+
+
+def test_godunov_reported_unsupported(tslib):
+    from turbostructred_gb300 import capi
+    cfg, keep = capi.to_config(capi.make_case(nx=8, solver=capi.RS_GODUNOV))
+    h = C.c_void_p()
+    assert tslib.ts_create(C.byref(cfg), C.byref(h)) == 2
+
+
+def test_state_sizes(tslib):
+    from turbostructred_gb300 import capi
+    cfg, keep = capi.to_config(capi.make_case(ndims=3, nx=4, ny=5, nz=6))
+    assert tslib.ts_state_doubles(C.byref(cfg), 0) == 4 * 5 * 6 * 5
+    assert tslib.ts_state_doubles(C.byref(cfg), 1) == 6 * 7 * 8 * 5

@@ -1,0 +1,158 @@
+"""Parity of the plain FP64 CUDA path with the reference.
+
+The bar is bit-for-bit: every fixture produced by the reference's own code
+(tests/golden) and every oracle run is matched with ``np.array_equal`` (which
+treats +0.0 and -0.0 as equal: the device drops products with the zero
+components of axis normals, which can only flip the sign of an exact zero).
+The one exception is the Venkatakrishnan limiter, whose eps^2 comes from libm
+``pow`` on the host running the test: fixtures made on another platform are
+checked to 1e-12 relative L-infinity instead.
+"""
+import numpy as np
+import pytest
+
+from conftest import golden_names, load_golden
+
+pytestmark = pytest.mark.gpu
+
+
+def run_gpu(case, initial_full, steps, precision=0):
+    from turbostructred_gb300 import capi
+    with capi.Solver(capi.make_case(**case), precision=precision) as s:
+        s.set_state(initial_full, capi.LAYOUT_WITH_GHOSTS)
+        info = s.run() if steps < 0 else s.step(steps)
+        return s.get_state(capi.LAYOUT_WITH_GHOSTS), info
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_plain_matches_reference_fixture(name, tslib):
+    g = load_golden(name)
+    vals, info = run_gpu(g["case"], g["initial"], g["meta"]["steps"])
+    assert info["iteration"] == g["iteration"]
+    if g["case"]["limiter"] == 1 and g["case"]["recon"] == 3:
+        assert rel_linf(vals, g["values"]) <= 1e-12
+        assert abs(info["time"] - g["time"]) <= 1e-12 * abs(g["time"])
+    else:
+        assert np.array_equal(vals, g["values"])
+        assert info["time"] == g["time"]
+        assert info["dt"] == g["dt"]
+    assert np.allclose(info["residual"], g["residual"], rtol=1e-12, atol=0)
+    assert info["health"] == 0
+
+
+def _scenario_full(case, scenario, seed, params):
+    from turbostructred_gb300 import capi
+    from oracle import oracle as O
+    ic = capi.fill_scenario(capi.make_case(**case), scenario, seed, params)
+    return O.embed(case, ic)
+
+
+SYM = (1, 0.0, (0.0, 0.0, 0.0), 0.0)
+NAT = (5, 0.0, (0.0, 0.0, 0.0), 0.0)
+WALL = (0, 0.0, (0.0, 0.0, 0.0), 0.0)
+BLAST = [1.0, 0.1, 10.0, 0.2, 0.01]
+SHEAR = [2.0, 1.0, 0.5, 2.5, 0.01]
+
+
+def oracle_cases():
+    from oracle import oracle as O
+    cs = []
+    for rec, lim in [(0, 0), (1, 0), (2, 0), (3, 0), (3, 1)]:
+        cs.append((f"blast3d_r{rec}l{lim}", O.make_case(ndims=3, nx=20, ny=18, nz=16, periodic=(0, 0, 0), recon=rec,
+                                                       limiter=lim, cfl=0.4, bc=[SYM] * 6), 2, BLAST, 8))
+    for solver in (1, 3):
+        cs.append((f"shear2d_s{solver}", O.make_case(ndims=2, nx=64, ny=48, periodic=(1, 1, 1), recon=3, solver=solver,
+                                                     cfl=0.4), 1, SHEAR, 15))
+    cs.append(("blast3d_hllc_mixedbc", O.make_case(ndims=3, nx=16, ny=12, nz=10, periodic=(1, 0, 0), recon=3,
+                                                   solver=3, cfl=0.4, bc=[NAT, NAT, WALL, SYM, SYM, NAT]), 2, BLAST, 6))
+    # stiffened gas (gamma 4.4, p_inf 6e8 scaled by 1e8 -> 6; not in the reference)
+    for solver in (1, 3):
+        cs.append((f"tube_stiff_s{solver}", O.make_case(ndims=1, nx=300, periodic=(0, 1, 1), recon=3, solver=solver,
+                                                        gamma=4.4, eos=1, p_inf=6.0, cfl=0.5, bc=[NAT] * 6),
+                   0, [0.5, 1.5, 0.2, 4.0, 0.8, -0.3, 0.5], 120))
+    # edge shapes: minimum axis, thin slabs, odd sizes
+    cs.append(("min_nx2", O.make_case(ndims=1, nx=2, periodic=(0, 1, 1), recon=3, cfl=0.3, bc=[WALL, NAT] + [NAT] * 4),
+               0, [0.5, 1.0, 0.1, 1.0, 0.5, 0.0, 0.4], 5))
+    cs.append(("slab2d_2x64", O.make_case(ndims=2, nx=2, ny=64, periodic=(0, 1, 1), recon=3, cfl=0.4,
+                                          bc=[SYM, SYM, NAT, NAT, NAT, NAT]), 1, SHEAR, 10))
+    cs.append(("odd3d", O.make_case(ndims=3, nx=5, ny=17, nz=3, periodic=(1, 0, 1), recon=2, cfl=0.4,
+                                    bc=[NAT, NAT, WALL, SYM, NAT, NAT]), 2, BLAST, 7))
+    return cs
+
+
+@pytest.mark.parametrize("case_spec", oracle_cases(), ids=lambda c: c[0])
+def test_plain_matches_oracle(case_spec, tslib, oracle_mod):
+    name, case, scen, params, steps = case_spec
+    full = _scenario_full(case, scen, 5, params)
+    ref, rinfo = oracle_mod.advance(case, full, steps)
+    vals, info = run_gpu(case, full, steps)
+    assert info["iteration"] == rinfo["iteration"] == steps
+    assert info["time"] == rinfo["time"] and info["dt"] == rinfo["dt"]
+    assert np.array_equal(vals, ref)
+
+
+def test_c3_full_size_256_matches_oracle(tslib, oracle_mod):
+    """C3 at its full size (3D blast 256^3, Symmetry walls, limited linear +
+    Roe): two steps bit-for-bit against the oracle; mass is conserved."""
+    case = oracle_mod.make_case(ndims=3, nx=256, ny=256, nz=256, periodic=(0, 0, 0), recon=3, limiter=0, solver=1,
+                                cfl=0.4, bc=[SYM] * 6)
+    full = _scenario_full(case, 2, 2024, [1.0, 0.1, 10.0, 0.1, 0.01])
+    ref, rinfo = oracle_mod.advance(case, full, 2)
+    vals, info = run_gpu(case, full, 2)
+    assert info["time"] == rinfo["time"]
+    assert np.array_equal(vals, ref)
+    inner = (slice(1, -1),) * 3
+    m0, m1 = full[inner][..., 0].sum(), vals[inner][..., 0].sum()
+    assert abs(m1 - m0) <= 1e-12 * m0
+
+
+def test_c2_full_size_1024_matches_oracle(tslib, oracle_mod):
+    """C2's grid (2D shear layer 1024^2 periodic, limited linear + Roe twin of
+    the HLLC config): three steps bit-for-bit against the oracle."""
+    case = oracle_mod.make_case(ndims=2, nx=1024, ny=1024, periodic=(1, 1, 1), recon=3, solver=1, cfl=0.4)
+    full = _scenario_full(case, 1, 2025, SHEAR)
+    ref, rinfo = oracle_mod.advance(case, full, 3)
+    vals, info = run_gpu(case, full, 3)
+    assert info["time"] == rinfo["time"]
+    assert np.array_equal(vals, ref)
+
+
+def test_run_matches_step_and_resume(tslib):
+    """Run = steps until MaxTime with overshoot; a run split by a checkpoint
+    (get_state + step info, resumed on a fresh handle) is identical."""
+    from turbostructred_gb300 import capi
+    g = load_golden("sod_eps_snapshots")
+    case = capi.make_case(**g["case"])
+    with capi.Solver(case) as s:
+        s.set_state(g["initial"], capi.LAYOUT_WITH_GHOSTS)
+        s.step(100)
+        mid = s.get_state(capi.LAYOUT_WITH_GHOSTS)
+        info = s.info()
+    with capi.Solver(case) as s2:
+        s2.set_state(mid, capi.LAYOUT_WITH_GHOSTS)
+        s2.set_info(iteration=info["iteration"], time=info["time"], dt=info["dt"],
+                    next_solution_time=info["next_solution_time"], next_slice_time=info["next_slice_time"])
+        fin = s2.run()
+        vals = s2.get_state(capi.LAYOUT_WITH_GHOSTS)
+    assert fin["iteration"] == g["iteration"] and fin["time"] == g["time"]
+    assert np.array_equal(vals, g["values"])
+
+
+def test_health_flags_negative_density(tslib):
+    """A state with a negative density is reported through the health word
+    (the reference has no such check); the handle stays usable."""
+    from turbostructred_gb300 import capi
+    case = capi.make_case(ndims=1, nx=32, periodic=(1, 1, 1), cfl=0.4)
+    ic = capi.fill_scenario(case, capi.SCENARIO_SHOCK_TUBE, 0, [0.5, 1.0, 0.0, 1.0, 0.5, 0.0, 0.5])
+    ic[0, 0, 3, 0] = -1.0
+    with capi.Solver(case) as s:
+        s.set_state(ic)
+        info = s.step(1)
+        assert info["health"] != 0
+        ic[0, 0, 3, 0] = 1.0
+        s.set_state(ic)
+        assert s.step(2)["health"] == 0

@@ -1,0 +1,287 @@
+"""ctypes binding of the C ABI in include/ts_fvm.h.
+
+The library is the in-tree ``libtsfvm.so`` built by :mod:`turbostructred_gb300.build`.
+Loading fails loudly when it is missing: there is no CPU fallback.
+
+Problems are described by the same plain ``dict`` keys the reference's
+KernelConfiguration uses (ndims, nx, ny, nz, periodic, length, blocks, gamma,
+recon, limiter, solver, eps, cfl, max_iter, max_time, bc ...), see
+:func:`make_case`.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libtsfvm.so")
+
+ABI_VERSION = 1
+
+# enum values (include/ts_fvm.h)
+RECON_PWC, RECON_LINEAR2, RECON_ENO2, RECON_LINEAR2_LIM = 0, 1, 2, 3
+RS_GODUNOV, RS_ROE, RS_NONE, RS_HLLC = 0, 1, 2, 3
+LIM_BJ, LIM_VENKAT = 0, 1
+BC_WALL, BC_SYMMETRY, BC_MOVING_WALL, BC_SUBSONIC_INLET, BC_SUBSONIC_OUTLET, BC_NATURAL = range(6)
+EOS_IDEAL, EOS_STIFFENED = 0, 1
+PRECISION_FP64, PRECISION_MIXED = 0, 1
+LAYOUT_INTERIOR, LAYOUT_WITH_GHOSTS = 0, 1
+SCENARIO_SHOCK_TUBE, SCENARIO_SHEAR_LAYER, SCENARIO_BLAST, SCENARIO_QUADRANTS = 0, 1, 2, 3
+HEALTH_NAN, HEALTH_NEG_DENSITY, HEALTH_NEG_PRESSURE = 1, 2, 4
+
+STATUS = {0: "ok", 1: "invalid", 2: "unsupported", 3: "cuda", 4: "no_memory", 5: "numeric",
+          6: "timeout", 7: "busy", 8: "not_found"}
+
+
+class TsError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+class BlockNode(C.Structure):
+    _fields_ = [("pos", C.c_double), ("q_com", C.c_double), ("n_cells", C.c_int32), ("reserved", C.c_int32)]
+
+
+class BcConfig(C.Structure):
+    _fields_ = [("type", C.c_int32), ("reserved", C.c_int32), ("density", C.c_double),
+                ("velocity", C.c_double * 3), ("pstatic", C.c_double), ("temperature", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("abi_version", C.c_int32), ("n_dims", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32),
+        ("nz", C.c_int32), ("periodic", C.c_int32 * 3), ("length", C.c_double * 3),
+        ("n_blocks", C.c_int32 * 3), ("reserved0", C.c_int32), ("blocks", C.POINTER(BlockNode) * 3),
+        ("gamma", C.c_double), ("eos", C.c_int32), ("reserved1", C.c_int32), ("p_inf", C.c_double),
+        ("reconstruction", C.c_int32), ("riemann_solver", C.c_int32), ("limiter", C.c_int32),
+        ("rk_order", C.c_int32), ("cfl", C.c_double), ("eps", C.c_double),
+        ("max_iteration", C.c_int32), ("reserved2", C.c_int32), ("max_time", C.c_double),
+        ("save_solution_time", C.c_double), ("save_slice_time", C.c_double),
+        ("bc", BcConfig * 6), ("precision", C.c_int32), ("device", C.c_int32),
+    ]
+
+
+class StepInfo(C.Structure):
+    _fields_ = [("iteration", C.c_int32), ("health", C.c_uint32), ("time", C.c_double), ("dt", C.c_double),
+                ("next_solution_time", C.c_double), ("next_slice_time", C.c_double),
+                ("residual", C.c_double * 5)]
+
+    def as_dict(self):
+        return dict(iteration=self.iteration, health=self.health, time=self.time, dt=self.dt,
+                    next_solution_time=self.next_solution_time, next_slice_time=self.next_slice_time,
+                    residual=list(self.residual))
+
+
+MAX_KERNELS = 12
+
+
+class Timing(C.Structure):
+    _fields_ = [("total_ms", C.c_double), ("n_kernels", C.c_int32), ("launches", C.c_int32),
+                ("kernel_ms", C.c_double * MAX_KERNELS), ("kernel_name", (C.c_char * 32) * MAX_KERNELS)]
+
+    def as_dict(self):
+        return dict(total_ms=self.total_ms, launches=self.launches,
+                    kernels={self.kernel_name[k].value.decode(): self.kernel_ms[k] for k in range(self.n_kernels)})
+
+
+EXPORTS = [
+    "ts_create", "ts_destroy", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
+    "ts_run",
+    "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates", "ts_state_doubles",
+    "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
+]
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Load the in-tree CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(f"{path} is missing: run turbostructred_gb300.build.build() first")
+    L = C.CDLL(path)
+    P = C.POINTER
+    L.ts_create.argtypes = [P(Config), P(C.c_void_p)]
+    L.ts_destroy.argtypes = [C.c_void_p]
+    L.ts_destroy.restype = None
+    L.ts_set_state.argtypes = [C.c_void_p, P(C.c_double), C.c_int32]
+    L.ts_set_state_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    L.ts_get_state.argtypes = [C.c_void_p, P(C.c_double), C.c_int32]
+    L.ts_step.argtypes = [C.c_void_p, C.c_int32, P(StepInfo)]
+    L.ts_step_timed.argtypes = [C.c_void_p, C.c_int32, P(StepInfo), P(Timing)]
+    L.ts_run.argtypes = [C.c_void_p, P(StepInfo)]
+    L.ts_get_step_info.argtypes = [C.c_void_p, P(StepInfo)]
+    L.ts_set_step_info.argtypes = [C.c_void_p, P(StepInfo)]
+    L.ts_synchronize.argtypes = [C.c_void_p]
+    L.ts_grid_coordinates.argtypes = [P(Config)] + [P(C.c_double)] * 6
+    L.ts_state_doubles.argtypes = [P(Config), C.c_int32]
+    L.ts_state_doubles.restype = C.c_size_t
+    L.ts_fill_scenario.argtypes = [P(Config), C.c_int32, C.c_uint64, P(C.c_double), C.c_int32, P(C.c_double)]
+    L.ts_hash_uniform.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int64]
+    L.ts_hash_uniform.restype = C.c_double
+    L.ts_last_error.restype = C.c_char_p
+    L.ts_status_string.restype = C.c_char_p
+    for name in ("ts_create", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
+                 "ts_run",
+                 "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates",
+                 "ts_fill_scenario"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(status: int):
+    if status != 0:
+        raise TsError(status, load().ts_last_error().decode())
+
+
+def make_case(**kw) -> dict:
+    """Problem description; defaults follow KernelConfiguration.h:21-93."""
+    case = dict(ndims=1, nx=1, ny=1, nz=1, periodic=(1, 1, 1), length=(1.0, 1.0, 1.0), blocks={},
+                gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
+                eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
+                save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6)
+    case.update(kw)
+    return case
+
+
+def to_config(case: dict, precision: int = PRECISION_FP64, device: int = 0):
+    """Returns (Config, keepalive) -- keepalive holds the block arrays."""
+    c = Config()
+    c.abi_version = ABI_VERSION
+    c.n_dims, c.nx, c.ny, c.nz = case["ndims"], case["nx"], case["ny"], case["nz"]
+    keep = []
+    for a in range(3):
+        c.periodic[a] = int(case["periodic"][a])
+        c.length[a] = case["length"][a]
+        blocks = case.get("blocks", {}).get(a, [])
+        if blocks:
+            arr = (BlockNode * len(blocks))()
+            for b, (pos, q, n) in enumerate(blocks):
+                arr[b].pos, arr[b].q_com, arr[b].n_cells = pos, q, n
+            keep.append(arr)
+            c.n_blocks[a] = len(blocks)
+            c.blocks[a] = C.cast(arr, C.POINTER(BlockNode))
+    c.gamma, c.eos, c.p_inf = case["gamma"], case.get("eos", EOS_IDEAL), case.get("p_inf", 0.0)
+    c.reconstruction, c.riemann_solver, c.limiter = case["recon"], case["solver"], case["limiter"]
+    c.rk_order = 1
+    c.cfl, c.eps = case["cfl"], case["eps"]
+    c.max_iteration, c.max_time = case["max_iter"], case["max_time"]
+    c.save_solution_time = case.get("save_solution_time", 0.0)
+    c.save_slice_time = case.get("save_slice_time", 0.0)
+    for s, (t, dens, vel, ps) in enumerate(case["bc"]):
+        c.bc[s].type, c.bc[s].density, c.bc[s].pstatic = t, dens, ps
+        for a in range(3):
+            c.bc[s].velocity[a] = vel[a]
+    c.precision, c.device = precision, device
+    return c, keep
+
+
+def interior_shape(case: dict):
+    nd = case["ndims"]
+    return (case["nz"] if nd > 2 else 1, case["ny"] if nd > 1 else 1, case["nx"], 5)
+
+
+def ghost_shape(case: dict):
+    nd = case["ndims"]
+    return (case["nz"] + 2 if nd > 2 else 1, case["ny"] + 2 if nd > 1 else 1, case["nx"] + 2, 5)
+
+
+def grid_coordinates(case: dict):
+    cfg, keep = to_config(case)
+    nx = case["nx"] + 2
+    ny = case["ny"] + 2 if case["ndims"] > 1 else 1
+    nz = case["nz"] + 2 if case["ndims"] > 2 else 1
+    arrs = [np.zeros(n) for n in (nx, nx, ny, ny, nz, nz)]
+    check(load().ts_grid_coordinates(C.byref(cfg), *[a.ctypes.data_as(C.POINTER(C.c_double)) for a in arrs]))
+    return arrs
+
+
+def fill_scenario(case: dict, scenario: int, seed: int, params) -> np.ndarray:
+    """Synthetic initial state (interior cells, shape (nz, ny, nx, 5))."""
+    cfg, keep = to_config(case)
+    out = np.zeros(interior_shape(case))
+    p = (C.c_double * len(params))(*params)
+    check(load().ts_fill_scenario(C.byref(cfg), scenario, seed, p, len(params),
+                                  out.ctypes.data_as(C.POINTER(C.c_double))))
+    return out
+
+
+class Solver:
+    """One device-resident domain driven through the C ABI."""
+
+    def __init__(self, case: dict, precision: int = PRECISION_FP64, device: int = 0):
+        self.case = case
+        self.lib = load()
+        cfg, self._keep = to_config(case, precision, device)
+        self._cfg = cfg
+        h = C.c_void_p()
+        check(self.lib.ts_create(C.byref(cfg), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.lib.ts_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_state(self, values: np.ndarray, layout: int = LAYOUT_INTERIOR):
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        check(self.lib.ts_set_state(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), layout))
+
+    def set_state_device(self, ptr: int, layout: int = LAYOUT_INTERIOR):
+        check(self.lib.ts_set_state_device(self.h, C.c_void_p(ptr), layout))
+
+    def get_state(self, layout: int = LAYOUT_INTERIOR, out: np.ndarray | None = None) -> np.ndarray:
+        shape = interior_shape(self.case) if layout == LAYOUT_INTERIOR else ghost_shape(self.case)
+        if out is None:
+            out = np.empty(shape)
+        check(self.lib.ts_get_state(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), layout))
+        return out
+
+    def step(self, n: int = 1) -> dict:
+        si = StepInfo()
+        check(self.lib.ts_step(self.h, n, C.byref(si)))
+        return si.as_dict()
+
+    def step_timed(self, n: int):
+        """n steps with CUDA events on the library's stream: (info, timing)."""
+        si, tm = StepInfo(), Timing()
+        check(self.lib.ts_step_timed(self.h, n, C.byref(si), C.byref(tm)))
+        return si.as_dict(), tm.as_dict()
+
+    def run(self) -> dict:
+        si = StepInfo()
+        check(self.lib.ts_run(self.h, C.byref(si)))
+        return si.as_dict()
+
+    def info(self) -> dict:
+        si = StepInfo()
+        check(self.lib.ts_get_step_info(self.h, C.byref(si)))
+        return si.as_dict()
+
+    def set_info(self, **kw):
+        si = StepInfo()
+        check(self.lib.ts_get_step_info(self.h, C.byref(si)))
+        for k, v in kw.items():
+            setattr(si, k, v)
+        check(self.lib.ts_set_step_info(self.h, C.byref(si)))
+
+    def synchronize(self):
+        check(self.lib.ts_synchronize(self.h))

@@ -1,0 +1,96 @@
+// Internal types shared by the host code and the CUDA kernels of the
+// GB300-native explicit FVM step.  Not part of the C ABI.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <string>
+#include <vector>
+
+#include "ts_fvm.h"
+
+#ifdef __CUDACC__
+#define TS_HD __host__ __device__ __forceinline__
+#else
+#define TS_HD inline
+#endif
+
+namespace ts {
+
+constexpr int NV = 5;      // rho, rho*u, rho*v, rho*w, rho*E
+constexpr int GHOST = 2;   // ghost layers per active axis in device arrays
+
+// Device field layout: structure of arrays, one plane per variable, x fastest.
+// Active axes carry GHOST ghost layers each side (the reference uses one;
+// the second serves the fused mixed-precision stencil).  Rows are padded to
+// a multiple of 8 elements so FP64 and FP32 rows start 64/32-byte aligned,
+// and the first interior cell of a row sits at an even x offset, which keeps
+// TMA boxes that start two cells before a tile 16-byte aligned.
+struct Layout {
+    int nd, nx, ny, nz;  // interior cells
+    int gx, gy, gz;      // ghost widths (GHOST on active axes, else 0)
+    int ex, ey, ez;      // extents including ghosts
+    int px;              // row pitch in elements
+    long long plane;     // elements per variable plane
+
+    TS_HD long long at(int i, int j, int k) const {
+        return ((long long)(k + gz) * ey + (j + gy)) * px + (i + gx);
+    }
+    TS_HD int n(int a) const { return a == 0 ? nx : (a == 1 ? ny : nz); }
+    TS_HD long long stride(int a) const {
+        return a == 0 ? 1LL : (a == 1 ? (long long)px : (long long)px * ey);
+    }
+    long long cells() const { return (long long)nx * ny * nz; }
+};
+
+Layout make_layout(const ts_config& c);
+
+// Boundary conditions of the six domain sides (x-, x+, y-, y+, z-, z+).
+struct BcSet {
+    int type[6];
+    double density[6];
+    double vel[6][3];
+    double pstatic[6];
+};
+
+// Physics and method selection passed by value to kernels.
+struct Phys {
+    int nd;
+    int recon, limiter, solver, eos;
+    int periodic[3];
+    double gamma, p_inf, eps, cfl;
+    BcSet bc;
+};
+
+// Per-handle step control word in device memory (StepInfo, kernel.h:31-39).
+struct Ctl {
+    double time;
+    double dt;
+    double next_sol;
+    double next_slice;
+    double res[5];
+    int iteration;
+    unsigned int health;
+    unsigned int blocks_done;  // last-block-done counter of the dt reduction
+    int stop_req;              // sticky: later kernels of a finished Run exit
+    int run_mode;              // 1 under Kernel::Run termination rules
+    int max_iteration;
+    double max_time;
+    double save_sol, save_slice;
+    double dt_min_raw;         // min(V/SR) before CFL and clipping
+};
+
+// Host copy of the grid in the reference's layout (one ghost per active
+// axis), grid.h:124-344.
+struct HostGrid {
+    std::vector<double> x, hx, y, hy, z, hz;
+};
+
+ts_status build_grid(const ts_config& c, HostGrid& g, std::string& err);
+ts_status validate_config(const ts_config& c, std::string& err);
+Phys make_phys(const ts_config& c);
+
+void set_error(const std::string& msg);
+ts_status fail(ts_status s, const std::string& msg);
+
+}  // namespace ts

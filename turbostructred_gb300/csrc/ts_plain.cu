@@ -1,0 +1,625 @@
+// Plain FP64 path: the drop-in for ExplicitRungeKuttaFVM<R>::IterationStep
+// (src/Methods/ExplicitRungeKuttaFVM.h:1440-1491) on one GB300.
+//
+// This translation unit is compiled with --fmad=false and IEEE division and
+// square root, and every expression keeps the reference's operation order, so
+// results match the reference's FP64 CPU path bit for bit (up to the sign of
+// exact zeros: products with the zero components of axis normals, which the
+// reference evaluates, are dropped here).
+//
+// One step is six launches on the handle's stream:
+//   k_ghost<A>   ghost layers per axis: periodic copy or boundary condition
+//                (Kernel::ExchangeValues + ComputeDummyCellValues, kernel.h:334-915)
+//   k_recon      per-cell slopes and limiter (ComputeSolutionReconstruction, :879-925)
+//   k_flux<A>    one kernel per face direction: face states, EOS, Riemann flux
+//                and max eigenvalue (ComputeResidual face loops, :1182-1419)
+//   k_dt         spectral radius per cell, V/SR, warp-shuffle min, last block
+//                finalises dt (ComputeTimeStep, :1427-1437)
+//   k_update     flux divergence fused with the stage update
+//                (residual accumulation :1232 + Kernel::UpdateSolution, kernel.h:319-331)
+//   k_finish     time/iteration and the Kernel::Run termination rules
+// FP64 is scarce on GB300 (about 2 FMA/clk/SM), so this path is compute-bound;
+// the layout and launches are chosen for coalescing, not for bandwidth.
+#include <cuda_runtime.h>
+
+#include "ts_plain.h"
+
+namespace ts {
+
+namespace {
+
+__device__ __forceinline__ long long vidx(const Layout& L, int v) { return (long long)v * L.plane; }
+
+// ---------------------------------------------------------------------------
+// Boundary conditions (BCGeneral.h:186-268) for a normal sgn*e_A.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void bc_values(const Phys& ph, int side, int A, double sgn, const double in[NV],
+                                          double out[NV]) {
+    const int t = ph.bc.type[side];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v] = in[v];
+    if (t == TS_BC_SYMMETRY) {
+        // rVinNormal = (n.rVin) n ; res -= 2 rVinNormal (BCGeneral.h:214-226)
+        const double m = in[1 + A];
+        const double s = sgn * m;
+        const double rn = s * sgn;
+        out[1 + A] = m - 2.0 * rn;
+    } else if (t == TS_BC_WALL) {
+        out[1] = in[1] * (-1.0);
+        out[2] = in[2] * (-1.0);
+        out[3] = in[3] * (-1.0);
+    } else if (t == TS_BC_MOVING_WALL) {
+        const double rho = in[0];
+        const double ux = in[1] / rho, uy = in[2] / rho, uz = in[3] / rho;
+        const double rhoe = in[4] - 0.5 * rho * (ux * ux + uy * uy + uz * uz);
+        const double dx = 2.0 * ph.bc.vel[side][0] - ux;
+        const double dy = 2.0 * ph.bc.vel[side][1] - uy;
+        const double dz = 2.0 * ph.bc.vel[side][2] - uz;
+        out[1] = rho * dx;
+        out[2] = rho * dy;
+        out[3] = rho * dz;
+        out[4] = rhoe + 0.5 * rho * (dx * dx + dy * dy + dz * dz);
+    } else if (t == TS_BC_SUBSONIC_INLET) {
+        const double r = ph.bc.density[side];
+        const double vx = ph.bc.vel[side][0], vy = ph.bc.vel[side][1], vz = ph.bc.vel[side][2];
+        out[0] = r;
+        out[1] = r * vx;
+        out[2] = r * vy;
+        out[3] = r * vz;
+        double eint = ph.bc.pstatic[side] / (ph.gamma - 1);
+        if (ph.eos == TS_EOS_STIFFENED_GAS) eint = eint + ph.gamma * ph.p_inf / (ph.gamma - 1);
+        out[4] = eint + 0.5 * r * (vx * vx + vy * vy + vz * vz);
+    }
+    // Natural and SubsonicOutlet copy the inner state (BCGeneral.h:200-211).
+}
+
+// ---------------------------------------------------------------------------
+// Riemann solvers
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double pressure(const Phys& ph, double ro, double vx, double vy, double vz, double roE) {
+    double p = (ph.gamma - 1.0) * (roE - ro * (vx * vx + vy * vy + vz * vz) / 2.0);
+    if (ph.eos == TS_EOS_STIFFENED_GAS) p = p - ph.gamma * ph.p_inf;
+    return p;
+}
+
+// F(U).e_A (RoeSolverPerfectGasEOS.h:41-58).
+template <int A>
+__device__ __forceinline__ void phys_flux(const Phys& ph, const double U[NV], double res[NV]) {
+    const double ro = U[0];
+    const double vel[3] = {U[1] / ro, U[2] / ro, U[3] / ro};
+    const double roE = U[4];
+    const double p = pressure(ph, ro, vel[0], vel[1], vel[2], roE);
+    const double vn = vel[A];
+    const double rvn = ro * vn;
+    res[0] = rvn;
+#pragma unroll
+    for (int b = 0; b < 3; ++b) res[1 + b] = (b == A) ? rvn * vel[b] + p : rvn * vel[b];
+    res[4] = vn * (roE + p);
+}
+
+__device__ __forceinline__ double harten(double z, double eps) {
+    z = fabs(z);
+    if (z < eps) z = ((z * z) / eps + eps) * 0.5;
+    return z;
+}
+
+// RoeSolverPerfectGasEOS::ComputeFlux (RoeSolverPerfectGasEOS.h:74-160) with
+// fn = e_A; dn = 1 so dn*c = c and 1/(dn*dn) = 1 exactly.
+template <int A>
+__device__ double roe_flux(const Phys& ph, const double UL[NV], const double UR[NV], double flux[NV]) {
+    const double g = ph.gamma;
+    double FL[NV], FR[NV];
+    phys_flux<A>(ph, UL, FL);
+    phys_flux<A>(ph, UR, FR);
+#pragma unroll
+    for (int i = 0; i < NV; ++i) flux[i] = FL[i] + FR[i];
+    const double ro_l = UL[0], ro_r = UR[0];
+    const double vl[3] = {UL[1] / ro_l, UL[2] / ro_l, UL[3] / ro_l};
+    const double vr[3] = {UR[1] / ro_r, UR[2] / ro_r, UR[3] / ro_r};
+    const double e_l = UL[4] / ro_l, e_r = UR[4] / ro_r;
+    double k = 0.5 * (vl[0] * vl[0] + vl[1] * vl[1] + vl[2] * vl[2]);
+    double h_l = (e_l - k) * g + k;
+    k = 0.5 * (vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2]);
+    double h_r = (e_r - k) * g + k;
+    if (ph.eos == TS_EOS_STIFFENED_GAS) {
+        h_l = h_l - g * ph.p_inf / ro_l;
+        h_r = h_r - g * ph.p_inf / ro_r;
+    }
+    const double sl = sqrt(ro_l), sr = sqrt(ro_r);
+    const double ql = sl / (sl + sr);
+    const double qr = sr / (sl + sr);
+    const double vel[3] = {ql * vl[0] + qr * vr[0], ql * vl[1] + qr * vr[1], ql * vl[2] + qr * vr[2]};
+    const double h = ql * h_l + qr * h_r;
+    const double phi2 = 0.5 * (g - 1) * (vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2]);
+    const double c = sqrt((g - 1) * h - phi2);
+    const double uw = vel[A];
+    const double eig_max = fabs(uw) + c;
+    const double he = ph.eps * eig_max;
+    const double AA1 = harten(uw, he);
+    const double AA3 = harten(uw + c, he);
+    const double AA4 = harten(uw - c, he);
+    const double Eig1 = AA1;
+    const double Eiga = (AA3 - AA4) * 0.5 / c;
+    const double Eigb = (AA3 + AA4) * 0.5 - AA1;
+    const double R1 = phi2 * ro_r - (g - 1) * ro_r * ((vel[0] * vr[0] + vel[1] * vr[1] + vel[2] * vr[2]) - e_r);
+    const double D1 = ro_r * (vr[A] - vel[A]);
+    const double R2 = phi2 * ro_l - (g - 1) * ro_l * ((vel[0] * vl[0] + vel[1] * vl[1] + vel[2] * vl[2]) - e_l);
+    const double D2 = ro_l * (vl[A] - vel[A]);
+    const double C2 = 1.0 / (c * c);
+    // Qa = (0, e_A, uw), Qb = (1, vel, h); terms multiplying a zero Qa entry
+    // are exact zeros and are left out.
+    {
+        const double t = Eig1 * UL[0] + Eiga * D2 + Eigb * (R2 * C2) - Eig1 * UR[0] - Eiga * D1 - Eigb * (R1 * C2);
+        flux[0] = (flux[0] + t) * 0.5;
+    }
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        double t;
+        if (b == A)
+            t = Eig1 * UL[1 + b] + Eiga * (R2 + D2 * vel[b]) + Eigb * (R2 * vel[b] * C2 + D2) - Eig1 * UR[1 + b] -
+                Eiga * (R1 + D1 * vel[b]) - Eigb * (R1 * vel[b] * C2 + D1);
+        else
+            t = Eig1 * UL[1 + b] + Eiga * (D2 * vel[b]) + Eigb * (R2 * vel[b] * C2) - Eig1 * UR[1 + b] -
+                Eiga * (D1 * vel[b]) - Eigb * (R1 * vel[b] * C2);
+        flux[1 + b] = (flux[1 + b] + t) * 0.5;
+    }
+    {
+        const double t = Eig1 * UL[4] + Eiga * (R2 * uw + D2 * h) + Eigb * (R2 * h * C2 + D2 * uw) - Eig1 * UR[4] -
+                         Eiga * (R1 * uw + D1 * h) - Eigb * (R1 * h * C2 + D1 * uw);
+        flux[4] = (flux[4] + t) * 0.5;
+    }
+    return eig_max;
+}
+
+// HLLC (Toro ch. 10.4) with Einfeldt-type speeds from Roe averages; same
+// operation order as the oracle's restatement.  Not in the reference.
+template <int A>
+__device__ double hllc_flux(const Phys& ph, const double UL[NV], const double UR[NV], double flux[NV]) {
+    const double g = ph.gamma;
+    const double pinf = ph.eos == TS_EOS_STIFFENED_GAS ? ph.p_inf : 0.0;
+    const int m = 1 + A;
+    const double rl = UL[0], rr = UR[0];
+    const double ul = UL[m] / rl, ur = UR[m] / rr;
+    const double vlx = UL[1] / rl, vly = UL[2] / rl, vlz = UL[3] / rl;
+    const double vrx = UR[1] / rr, vry = UR[2] / rr, vrz = UR[3] / rr;
+    const double pl = pressure(ph, rl, vlx, vly, vlz, UL[4]);
+    const double pr = pressure(ph, rr, vrx, vry, vrz, UR[4]);
+    const double cl = sqrt(g * (pl + pinf) / rl);
+    const double cr = sqrt(g * (pr + pinf) / rr);
+    const double hl = (UL[4] + pl) / rl;
+    const double hr = (UR[4] + pr) / rr;
+    const double sl = sqrt(rl), sr = sqrt(rr);
+    const double wl = sl / (sl + sr), wr = sr / (sl + sr);
+    const double ut = wl * ul + wr * ur;
+    const double vtx = wl * vlx + wr * vrx, vty = wl * vly + wr * vry, vtz = wl * vlz + wr * vrz;
+    const double ht = wl * hl + wr * hr;
+    const double ct = sqrt((g - 1) * (ht - 0.5 * (vtx * vtx + vty * vty + vtz * vtz)));
+    const double SL = fmin(ul - cl, ut - ct);
+    const double SR = fmax(ur + cr, ut + ct);
+    const double lam = fmax(fabs(SL), fabs(SR));
+    const double ml = rl * (SL - ul), mr = rr * (SR - ur);
+    const double sstar = (pr - pl + ul * ml - ur * mr) / (ml - mr);
+    if (SL >= 0.0) {
+        phys_flux<A>(ph, UL, flux);
+    } else if (SR <= 0.0) {
+        phys_flux<A>(ph, UR, flux);
+    } else if (sstar >= 0.0) {
+        double F[NV], us[NV];
+        phys_flux<A>(ph, UL, F);
+        const double coef = ml / (SL - sstar);
+        us[0] = coef;
+        us[1] = coef * vlx; us[2] = coef * vly; us[3] = coef * vlz;
+        us[m] = coef * sstar;
+        us[4] = coef * (UL[4] / rl + (sstar - ul) * (sstar + pl / ml));
+#pragma unroll
+        for (int v = 0; v < NV; ++v) flux[v] = F[v] + SL * (us[v] - UL[v]);
+    } else {
+        double F[NV], us[NV];
+        phys_flux<A>(ph, UR, F);
+        const double coef = mr / (SR - sstar);
+        us[0] = coef;
+        us[1] = coef * vrx; us[2] = coef * vry; us[3] = coef * vrz;
+        us[m] = coef * sstar;
+        us[4] = coef * (UR[4] / rr + (sstar - ur) * (sstar + pr / mr));
+#pragma unroll
+        for (int v = 0; v < NV; ++v) flux[v] = F[v] + SR * (us[v] - UR[v]);
+    }
+    return lam;
+}
+
+// ---------------------------------------------------------------------------
+// Kernels
+// ---------------------------------------------------------------------------
+
+// Transverse (p,q) -> (i,j,k) for a line along axis A.
+template <int A>
+__device__ __forceinline__ void line_cell(int p, int q, int s, int& i, int& j, int& k) {
+    if (A == 0) { i = s; j = p; k = q; }
+    else if (A == 1) { i = p; j = s; k = q; }
+    else { i = p; j = q; k = s; }
+}
+
+template <int A>
+__global__ void k_ghost(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int n1 = (A == 0) ? L.ny : L.nx;
+    const int n2 = (A == 2) ? L.ny : L.nz;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2) return;
+    const int p = t % n1, q = t / n1;
+    int i, j, k;
+    line_cell<A>(p, q, 0, i, j, k);
+    const long long c0 = L.at(i, j, k);
+    const long long st = L.stride(A);
+    const int n = L.n(A);
+    double* U = b.U;
+    if (ph.periodic[A]) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            double* u = U + vidx(L, v) + c0;
+            u[-1 * st] = u[(long long)(n - 1) * st];
+            u[(long long)n * st] = u[0];
+            u[-2 * st] = u[(long long)(n - 2) * st];
+            u[(long long)(n + 1) * st] = u[st];
+        }
+        return;
+    }
+    double in[NV], out[NV];
+    // left side ghosts mirror cells 0 and 1; right side mirror n-1 and n-2
+    // (ComputeDummyCellValues, kernel.h:731-765); faceNormalL on both sides.
+    for (int layer = 1; layer <= GHOST; ++layer) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) in[v] = U[vidx(L, v) + c0 + (long long)(layer - 1) * st];
+        bc_values(ph, 2 * A, A, -1.0, in, out);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) U[vidx(L, v) + c0 - (long long)layer * st] = out[v];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) in[v] = U[vidx(L, v) + c0 + (long long)(n - layer) * st];
+        bc_values(ph, 2 * A + 1, A, -1.0, in, out);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) U[vidx(L, v) + c0 + (long long)(n - 1 + layer) * st] = out[v];
+    }
+}
+
+// Venkatakrishnan l-function (Limiters.h:102-115).
+__device__ __forceinline__ double venkat(double um, double ui, double d2, double umax, double umin, double eps2) {
+    const double un = 0.5 * (umax - umin);
+    um /= un;
+    ui /= un;
+    d2 /= un;
+    const double dm = um - ui;
+    return ((dm * dm + eps2) + 2 * d2 * dm) / (dm * dm + 2 * d2 * d2 + dm * d2 + eps2);
+}
+
+// Per interior cell: slopes (Linear2PointsStencil.h:147-178 or
+// ENO2PointsStencil.h:202-239) and, for Linear2psLim, the limiter
+// (Linear2psLim.h:305-374, Limiters.h:28-119).
+__global__ void k_recon(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= L.nx) return;
+    const int nd = ph.nd;
+    const long long c = L.at(i, j, k);
+    const int ix[3] = {i, j, k};
+    double val[NV], nb[6][NV], g[3][NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) val[v] = b.U[vidx(L, v) + c];
+    for (int a = 0; a < nd; ++a) {
+        const long long st = L.stride(a);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            nb[2 * a][v] = b.U[vidx(L, v) + c - st];
+            nb[2 * a + 1][v] = b.U[vidx(L, v) + c + st];
+        }
+    }
+    for (int a = 0; a < nd; ++a) {
+        const double* X = b.cx[a];
+        const int g0 = (a == 0) ? L.gx : (a == 1 ? L.gy : L.gz);
+        const double xm = X[ix[a] - 1 + g0], xc = X[ix[a] + g0], xp = X[ix[a] + 1 + g0];
+        if (ph.recon == TS_RECON_ENO2_2POINTS) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const double gl = (val[v] - nb[2 * a][v]) / (xc - xm);
+                const double gr = (nb[2 * a + 1][v] - val[v]) / (xp - xc);
+                g[a][v] = (fabs(gl) < fabs(gr)) ? gl : gr;
+            }
+        } else {
+            const double d = xp - xm;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) g[a][v] = (nb[2 * a + 1][v] - nb[2 * a][v]) / d;
+        }
+#pragma unroll
+        for (int v = 0; v < NV; ++v) b.G[vidx(L, a * NV + v) + c] = g[a][v];
+    }
+    if (ph.recon != TS_RECON_LINEAR_2POINTS_LIMITED) return;
+
+    // Projections (SampleSolution(+-h/2) - vals) to the 2*nDim faces.
+    double hcell[3];
+    hcell[0] = b.ch[0][i + L.gx];
+    hcell[1] = b.ch[1][j + L.gy];
+    hcell[2] = b.ch[2][k + L.gz];
+    const double eps2 = b.eps2 ? b.eps2[c] : 0.0;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double umax = val[v], umin = val[v];
+        for (int f = 0; f < 2 * nd; ++f) {
+            const double vn = nb[f][v];
+            if (umax < vn) umax = vn;
+            if (umin > vn) umin = vn;
+        }
+        double lmin = 1.0;
+        if (!(umax - umin < 3.0 * 2.2250738585072014e-308)) {
+            for (int f = 0; f < 2 * nd; ++f) {
+                const int a = f >> 1;
+                const double s = (f & 1) ? 0.5 * hcell[a] : -0.5 * hcell[a];
+                const double d2 = (val[v] + g[a][v] * s) - val[v];
+                double lv = 1.0;
+                if (ph.limiter == TS_LIM_VENKATAKRISHNAN) {
+                    if (d2 > 0) lv = venkat(umax, val[v], d2, umax, umin, eps2);
+                    if (d2 < 0) lv = venkat(umin, val[v], d2, umax, umin, eps2);
+                } else {
+                    if (d2 > 0) { const double r = (umax - val[v]) / d2; lv = (r < 1.0) ? r : 1.0; }
+                    if (d2 < 0) { const double r = (umin - val[v]) / d2; lv = (r < 1.0) ? r : 1.0; }
+                }
+                if (lmin > lv) lmin = lv;
+            }
+        }
+        b.Lim[vidx(L, v) + c] = lmin;
+    }
+}
+
+// Face-centred sample of a cell's reconstruction (SampleSolution).
+__device__ __forceinline__ void sample(const PlainBufs& b, const Phys& ph, long long c, int a, double s,
+                                       double out[NV]) {
+    const Layout& L = b.L;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) out[v] = b.U[vidx(L, v) + c];
+    if (ph.recon == TS_RECON_PIECEWISE_CONSTANT) return;
+    if (ph.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = out[v] + b.Lim[vidx(L, v) + c] * (b.G[vidx(L, a * NV + v) + c] * s);
+    } else {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) out[v] = out[v] + b.G[vidx(L, a * NV + v) + c] * s;
+    }
+}
+
+// One face per thread along axis A; faces are stored at their right cell.
+template <int A>
+__global__ void k_flux(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const int ilim = (A == 0) ? L.nx + 1 : L.nx;
+    if (i >= ilim) return;
+    const int s = (A == 0) ? i : (A == 1 ? j : k);
+    const int n = L.n(A);
+    const long long st = L.stride(A);
+    const long long cf = L.at(i, j, k);  // cell to the right of the face
+    const double* H = b.ch[A];
+    const int g0 = (A == 0) ? L.gx : (A == 1 ? L.gy : L.gz);
+    double UL[NV], UR[NV];
+    if (s == 0 && !ph.periodic[A]) {
+        sample(b, ph, cf, A, -0.5 * H[s + g0], UR);
+        bc_values(ph, 2 * A, A, 1.0, UR, UL);
+    } else if (s == n && !ph.periodic[A]) {
+        sample(b, ph, cf - st, A, 0.5 * H[s - 1 + g0], UL);
+        bc_values(ph, 2 * A + 1, A, 1.0, UL, UR);
+    } else {
+        // A ghost reconstruction on a periodic axis is the opposite interior
+        // cell's object sampled with the ghost's own h (ExchangeReconstructions).
+        const long long cl = (s == 0) ? cf + (long long)(n - 1) * st : cf - st;
+        const long long cr = (s == n) ? cf - (long long)n * st : cf;
+        sample(b, ph, cl, A, 0.5 * H[s - 1 + g0], UL);
+        sample(b, ph, cr, A, -0.5 * H[s + g0], UR);
+    }
+    double F[NV];
+    const double lam = (ph.solver == TS_RS_HLLC) ? hllc_flux<A>(ph, UL, UR, F) : roe_flux<A>(ph, UL, UR, F);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) b.F[A][vidx(L, v) + cf] = F[v];
+    b.Lam[A][cf] = lam;
+}
+
+__device__ __forceinline__ double warp_min(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    return v;
+}
+
+__device__ __forceinline__ double face_area(const PlainBufs& b, int nd, int a, int i, int j, int k) {
+    const Layout& L = b.L;
+    const double hx = b.ch[0][i + L.gx], hy = b.ch[1][j + L.gy], hz = b.ch[2][k + L.gz];
+    if (a == 0) return nd == 1 ? 1.0 : (nd == 2 ? hy : hy * hz);
+    if (a == 1) return nd == 2 ? hx : hx * hz;
+    return hx * hy;
+}
+
+// Spectral radius per cell in the reference's accumulation order (x-left,
+// x-right, y-left, ...), V/SR, block min by warp shuffles; the high-side
+// ghost cells, whose SR is their single face term, join the min.  The last
+// block to finish reduces the block minima and sets dt.
+__global__ void k_dt(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const int nd = ph.nd;
+    double r = __longlong_as_double(0x7ff0000000000000LL);  // +inf
+    if (i < L.nx) {
+        const long long c = L.at(i, j, k);
+        const double hx = b.ch[0][i + L.gx], hy = b.ch[1][j + L.gy], hz = b.ch[2][k + L.gz];
+        const double V = hx * hy * hz;
+        double sr = 0.0;
+        const int ix[3] = {i, j, k};
+        for (int a = 0; a < nd; ++a) {
+            const double fS = face_area(b, nd, a, i, j, k);
+            const long long st = L.stride(a);
+            sr += fS * b.Lam[a][c];
+            sr += fS * b.Lam[a][c + st];
+            if (ix[a] == L.n(a) - 1) {
+                double hg[3] = {hx, hy, hz};
+                hg[a] = b.ch[a][L.n(a) + (a == 0 ? L.gx : (a == 1 ? L.gy : L.gz))];
+                const double Vg = hg[0] * hg[1] * hg[2];
+                r = fmin(r, Vg / (fS * b.Lam[a][c + st]));
+            }
+        }
+        r = fmin(r, V / sr);
+    }
+    __shared__ double wmin[32];
+    r = warp_min(r);
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    if (lane == 0) wmin[wid] = r;
+    __syncthreads();
+    const int nblk = gridDim.x * gridDim.y * gridDim.z;
+    const int bid = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    __shared__ bool last;
+    if (threadIdx.x == 0) {
+        double m = wmin[0];
+        for (int w = 1; w < (int)(blockDim.x + 31) / 32; ++w) m = fmin(m, wmin[w]);
+        b.partial[bid] = m;
+        __threadfence();
+        last = (atomicAdd(&b.ctl->blocks_done, 1u) == (unsigned)(nblk - 1));
+    }
+    __syncthreads();
+    if (!last) return;
+    __threadfence();
+    double m = __longlong_as_double(0x7ff0000000000000LL);
+    for (int t = threadIdx.x; t < nblk; t += blockDim.x) m = fmin(m, ((volatile double*)b.partial)[t]);
+    m = warp_min(m);
+    if (lane == 0) wmin[wid] = m;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        m = wmin[0];
+        for (int w = 1; w < (int)(blockDim.x + 31) / 32; ++w) m = fmin(m, wmin[w]);
+        Ctl* ctl = b.ctl;
+        double dt = m * ph.cfl;
+        if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
+        if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
+        ctl->dt_min_raw = m;
+        ctl->dt = dt;
+        for (int v = 0; v < NV; ++v) ctl->res[v] = 0.0;
+        ctl->blocks_done = 0;
+    }
+}
+
+// Residual R = -sum_a (F_{a,+} - F_{a,-}) fS_a accumulated from zero in the
+// reference's direction order, then U += dt*(R/V); residual norms and health.
+__global__ void k_update(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    const int nd = ph.nd;
+    double nrm[NV] = {0, 0, 0, 0, 0};
+    unsigned int health = 0;
+    if (i < L.nx) {
+        const long long c = L.at(i, j, k);
+        const double hx = b.ch[0][i + L.gx], hy = b.ch[1][j + L.gy], hz = b.ch[2][k + L.gz];
+        const double V = hx * hy * hz;
+        const double dt = b.ctl->dt;
+        double R[NV] = {0.0, 0.0, 0.0, 0.0, 0.0};
+        for (int a = 0; a < nd; ++a) {
+            const double fS = face_area(b, nd, a, i, j, k);
+            const long long st = L.stride(a);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) {
+                const double* F = b.F[a] + vidx(L, v);
+                R[v] -= (F[c + st] - F[c]) * fS;
+            }
+        }
+        double u[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            double* p = b.U + vidx(L, v) + c;
+            u[v] = *p + dt * (R[v] / V);
+            *p = u[v];
+            nrm[v] = V * fabs(R[v]);
+        }
+        const double ke = 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
+        const double p = pressure(ph, u[0], 0.0, 0.0, 0.0, u[4] - ke);
+        if (!(u[0] == u[0]) || !(u[4] == u[4]) || !(p == p)) health |= TS_HEALTH_NAN;
+        if (u[0] <= 0.0) health |= TS_HEALTH_NEG_DENSITY;
+        if (p <= 0.0 && ph.eos == TS_EOS_IDEAL_GAS) health |= TS_HEALTH_NEG_PRESSURE;
+        if (ph.eos == TS_EOS_STIFFENED_GAS && p + ph.p_inf <= 0.0) health |= TS_HEALTH_NEG_PRESSURE;
+    }
+    // block sums of the diagnostic norms (accumulation order differs from the
+    // reference's serial sum; the norms are reported, never fed back)
+    __shared__ double red[NV][32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double s = nrm[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+        if (lane == 0) red[v][wid] = s;
+    }
+    health = __reduce_or_sync(0xffffffffu, health);
+    if (lane == 0 && health) atomicOr(&b.ctl->health, health);
+    __syncthreads();
+    if (threadIdx.x < NV) {
+        double s = 0.0;
+        for (int w = 0; w < (int)(blockDim.x + 31) / 32; ++w) s += red[threadIdx.x][w];
+        atomicAdd(&b.ctl->res[threadIdx.x], s);
+    }
+}
+
+// time += dt, iteration++ (IterationStep :1486-1487); under Run also the
+// snapshot-time bookkeeping and termination test (kernel.h:1763-1846).
+__global__ void k_finish(Ctl* ctl) {
+    if (ctl->stop_req) return;
+    ctl->time += ctl->dt;
+    ctl->iteration += 1;
+    if (!ctl->run_mode) return;
+    if ((ctl->save_sol > 0) && (ctl->next_sol == ctl->time)) ctl->next_sol += ctl->save_sol;
+    if ((ctl->save_slice > 0) && (ctl->next_slice == ctl->time)) ctl->next_slice += ctl->save_slice;
+    if (ctl->iteration == ctl->max_iteration || ctl->time >= ctl->max_time) ctl->stop_req = 1;
+}
+
+}  // namespace
+
+int plain_partial_blocks(const Layout& L) {
+    const int bx = (L.nx + kPlainBlock - 1) / kPlainBlock;
+    return bx * L.ny * L.nz;
+}
+
+cudaError_t plain_step(const PlainBufs& b, const Phys& ph, cudaStream_t st, cudaEvent_t* ev, int* n_launch,
+                       const char** names) {
+    const Layout& L = b.L;
+    const dim3 blk(kPlainBlock);
+    const dim3 cells((L.nx + kPlainBlock - 1) / kPlainBlock, L.ny, L.nz);
+    auto ghost_grid = [&](int a) {
+        const int n1 = (a == 0) ? L.ny : L.nx;
+        const int n2 = (a == 2) ? L.ny : L.nz;
+        return dim3((n1 * n2 + kPlainBlock - 1) / kPlainBlock);
+    };
+    int nl = 0;
+    if (ev) cudaEventRecord(ev[0], st);
+    auto mark = [&](const char* name) {
+        if (names) names[nl] = name;
+        ++nl;
+        if (ev) cudaEventRecord(ev[nl], st);
+    };
+    k_ghost<0><<<ghost_grid(0), blk, 0, st>>>(b, ph);
+    mark("k_ghost_x");
+    if (ph.nd > 1) { k_ghost<1><<<ghost_grid(1), blk, 0, st>>>(b, ph); mark("k_ghost_y"); }
+    if (ph.nd > 2) { k_ghost<2><<<ghost_grid(2), blk, 0, st>>>(b, ph); mark("k_ghost_z"); }
+    if (ph.recon != TS_RECON_PIECEWISE_CONSTANT) { k_recon<<<cells, blk, 0, st>>>(b, ph); mark("k_recon"); }
+    k_flux<0><<<dim3((L.nx + 1 + kPlainBlock - 1) / kPlainBlock, L.ny, L.nz), blk, 0, st>>>(b, ph);
+    mark("k_flux_x");
+    if (ph.nd > 1) { k_flux<1><<<dim3(cells.x, L.ny + 1, L.nz), blk, 0, st>>>(b, ph); mark("k_flux_y"); }
+    if (ph.nd > 2) { k_flux<2><<<dim3(cells.x, L.ny, L.nz + 1), blk, 0, st>>>(b, ph); mark("k_flux_z"); }
+    k_dt<<<cells, blk, 0, st>>>(b, ph);
+    mark("k_dt");
+    k_update<<<cells, blk, 0, st>>>(b, ph);
+    mark("k_update");
+    k_finish<<<1, 1, 0, st>>>(b.ctl);
+    mark("k_finish");
+    if (n_launch) *n_launch = nl;
+    return cudaGetLastError();
+}
+
+}  // namespace ts
