@@ -183,6 +183,12 @@ ts_status ts_run(ts_handle* h, ts_step_info* info);
 ts_status ts_get_step_info(ts_handle* h, ts_step_info* info);
 ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info);
 
+/* Tile shape (cells per CTA along x and y) of the mixed-precision fused
+   kernel; tx*ty must be 32..256 threads in whole warps.  Results do not
+   depend on the tile: every face flux is a function of its two cells only.
+   TS_ERR_UNSUPPORTED for the FP64 path. */
+ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty);
+
 /* Waits for all work queued on the handle's stream. */
 ts_status ts_synchronize(ts_handle* h);
 

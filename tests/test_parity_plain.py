@@ -28,11 +28,25 @@ def rel_linf(a, b):
     return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-300))
 
 
+def host_grid_matches(g):
+    """Stretched grids use libm pow (grid.h:177); on a host whose libm rounds
+    differently from the one that made the fixture, the grid itself differs."""
+    from turbostructred_gb300 import capi
+    mine = capi.grid_coordinates(capi.make_case(**g["case"]))
+    return all(np.array_equal(a, b) for a, b in zip(mine, (g["x"], g["hx"], g["y"], g["hy"], g["z"], g["hz"])))
+
+
 @pytest.mark.parametrize("name", golden_names())
-def test_plain_matches_reference_fixture(name, tslib):
+def test_plain_matches_reference_fixture(name, tslib, oracle_mod):
     g = load_golden(name)
     vals, info = run_gpu(g["case"], g["initial"], g["meta"]["steps"])
     assert info["iteration"] == g["iteration"]
+    if not host_grid_matches(g):
+        # same inputs on this host: bit-for-bit with the oracle; the fixture to 1e-12
+        ref, rinfo = oracle_mod.advance(g["case"], g["initial"], g["meta"]["steps"])
+        assert np.array_equal(vals, ref) and info["time"] == rinfo["time"]
+        assert rel_linf(vals, g["values"]) <= 1e-12
+        return
     if g["case"]["limiter"] == 1 and g["case"]["recon"] == 3:
         assert rel_linf(vals, g["values"]) <= 1e-12
         assert abs(info["time"] - g["time"]) <= 1e-12 * abs(g["time"])

@@ -20,11 +20,16 @@ LIB = os.path.join(PKG, "libtsfvm.so")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-I" + INCLUDE, "-I" + CSRC]
+# Host code never contracts a*b+c into an FMA (g++ does by default on
+# aarch64): the grid accumulation must round exactly like the reference.
+COMMON = ["-O3", "-std=c++20", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off",
+          "-I" + INCLUDE, "-I" + CSRC]
 
 UNITS = {
     "ts_plain.cu": ["--fmad=false"],
-    "ts_mixed.cu": [],
+    # FP32 flux path: flush-to-zero and approximate FP32 division/sqrt; FP64
+    # arithmetic is unaffected by these flags.
+    "ts_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "ts_capi.cu": [],
     "ts_host.cpp": [],
 }

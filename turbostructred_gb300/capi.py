@@ -89,7 +89,7 @@ class Timing(C.Structure):
 
 EXPORTS = [
     "ts_create", "ts_destroy", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
-    "ts_run",
+    "ts_run", "ts_set_tile",
     "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates", "ts_state_doubles",
     "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
 ]
@@ -118,6 +118,8 @@ def load(path: str = LIB_PATH):
     L.ts_get_step_info.argtypes = [C.c_void_p, P(StepInfo)]
     L.ts_set_step_info.argtypes = [C.c_void_p, P(StepInfo)]
     L.ts_synchronize.argtypes = [C.c_void_p]
+    L.ts_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.ts_set_tile.restype = C.c_int
     L.ts_grid_coordinates.argtypes = [P(Config)] + [P(C.c_double)] * 6
     L.ts_state_doubles.argtypes = [P(Config), C.c_int32]
     L.ts_state_doubles.restype = C.c_size_t
@@ -285,3 +287,6 @@ class Solver:
 
     def synchronize(self):
         check(self.lib.ts_synchronize(self.h))
+
+    def set_tile(self, tx: int, ty: int):
+        check(self.lib.ts_set_tile(self.h, tx, ty))

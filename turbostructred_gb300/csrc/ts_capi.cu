@@ -186,7 +186,8 @@ struct ts_handle {
         return TS_OK;
     }
 
-    double* state_planes() { return cfg.precision == TS_PRECISION_MIXED ? mb.U : pb.U; }
+    // Current state planes; for the mixed path the caller has pulled ctl.
+    double* state_planes() { return cfg.precision == TS_PRECISION_MIXED ? mixed_state(mb, ctl_h->parity) : pb.U; }
 
     void enqueue_step() {
         if (cfg.precision == TS_PRECISION_MIXED) mixed_step(mb, ph, stream);
@@ -317,9 +318,16 @@ static ts_status set_state_impl(ts_handle* h, const double* values, int32_t layo
     const size_t nd = ts_state_doubles(&h->cfg, layout);
     const long long ncell = (long long)(nd / NV);
     const double* src = values;
+    ts_status s;
+    if (h->cfg.precision == TS_PRECISION_MIXED) {
+        // a fresh state has no pending residual and lives in buffer 0
+        if ((s = h->pull_ctl()) != TS_OK) return s;
+        h->ctl_h->parity = 0;
+        h->ctl_h->dt_apply = 0.0;
+        if ((s = h->push_ctl()) != TS_OK) return s;
+    }
     if (!device_ptr) {
-        ts_status s = h->ensure_stage(nd);
-        if (s != TS_OK) return s;
+        if ((s = h->ensure_stage(nd)) != TS_OK) return s;
         TS_CUDA(cudaMemcpyAsync(h->stage_d, values, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
         src = h->stage_d;
     }
@@ -349,7 +357,11 @@ ts_status ts_get_state(ts_handle* h, double* values, int32_t layout) {
     const long long ncell = (long long)(nd / NV);
     ts_status s = h->ensure_stage(nd);
     if (s != TS_OK) return s;
-    if (h->cfg.precision == TS_PRECISION_MIXED) mixed_materialize(h->mb, h->ph, h->stream);
+    if (h->cfg.precision == TS_PRECISION_MIXED) {
+        if ((s = h->pull_ctl()) != TS_OK) return s;
+        mixed_materialize(h->mb, h->ph, h->stream);
+        h->ctl_h->dt_apply = 0.0;  // the device copy is cleared by the apply pass
+    }
     const int blk = 256;
     k_gather<<<(unsigned)((ncell + blk - 1) / blk), blk, 0, h->stream>>>(h->stage_d, h->L, h->state_planes(),
                                                                           layout == TS_LAYOUT_WITH_GHOSTS, ncell);
@@ -467,6 +479,19 @@ ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info) {
     h->ctl_h->next_sol = info->next_solution_time;
     h->ctl_h->next_slice = info->next_slice_time;
     return h->push_ctl();
+}
+
+ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty) {
+    if (!h) return fail(TS_ERR_INVALID, "NULL handle");
+    if (h->cfg.precision != TS_PRECISION_MIXED) return fail(TS_ERR_UNSUPPORTED, "tiles apply to the mixed path");
+    DeviceGuard g(h->device);
+    TS_CUDA(cudaStreamSynchronize(h->stream));
+    std::string err;
+    ts_status s = mixed_set_tile(h->mb, tx, ty, err);
+    if (s != TS_OK) return fail(s, err);
+    for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);  // launch shape changed
+    h->graphs.clear();
+    return TS_OK;
 }
 
 ts_status ts_synchronize(ts_handle* h) {

@@ -40,7 +40,7 @@ struct Layout {
     TS_HD long long stride(int a) const {
         return a == 0 ? 1LL : (a == 1 ? (long long)px : (long long)px * ey);
     }
-    long long cells() const { return (long long)nx * ny * nz; }
+    TS_HD long long cells() const { return (long long)nx * ny * nz; }
 };
 
 Layout make_layout(const ts_config& c);
@@ -78,6 +78,10 @@ struct Ctl {
     double max_time;
     double save_sol, save_slice;
     double dt_min_raw;         // min(V/SR) before CFL and clipping
+    // mixed-precision path (deferred stage update)
+    double dt_apply;           // dt of the residual still waiting to be applied
+    int parity;                // which of the two state/residual buffers is current
+    unsigned int srmax_bits;   // running max of SR/V as FP32 bits (positive floats order as uints)
 };
 
 // Host copy of the grid in the reference's layout (one ghost per active
