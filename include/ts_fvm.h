@@ -216,6 +216,30 @@ ts_status ts_fill_scenario(const ts_config* cfg, int32_t scenario, uint64_t seed
 /* The hash RNG the scenarios use: uniform double in [0,1). */
 double ts_hash_uniform(uint64_t seed, int64_t i, int64_t j, int64_t k);
 
+/* Advance a state by n_steps of the mixed-precision fused step without
+   allocating any device memory.  No counterpart in the reference: this is
+   for callers that are not allowed to call cudaMalloc themselves or through
+   us -- code embedded in a host application that owns every byte of device
+   memory through its own pool or budget, or a latency-critical loop where an
+   allocation's implicit synchronisation and unpredictable cost are not
+   acceptable.
+     cfg       problem set-up; precision must be TS_PRECISION_MIXED.
+     state_in  device pointer, TS_LAYOUT_INTERIOR doubles (caller-owned).
+     state_out device pointer, same layout (may equal state_in).
+     stream    a cudaStream_t, or NULL for the legacy default stream.
+     info      optional; its time, iteration and snapshot times are the
+               starting point and it receives the step info at the end.
+   Every call works in one file-scope scratch array of TS_NOALLOC_MAX_PLANE
+   elements per variable plane (about 38 MB, resident on every GPU that has
+   loaded this library, until the process exits): grids whose padded planes
+   exceed it are rejected with TS_ERR_INVALID.  The first call on a device
+   looks up that array's device address, so make it before any stream
+   capture.  All calls share the array and leave their data in it; calls that
+   overlap on the GPU (other streams, other host threads) race on it. */
+#define TS_NOALLOC_MAX_PLANE 262144
+ts_status ts_advance_noalloc(const ts_config* cfg, const double* state_in, double* state_out, int32_t n_steps,
+                             void* stream, ts_step_info* info);
+
 const char* ts_last_error(void);
 const char* ts_status_string(ts_status s);
 

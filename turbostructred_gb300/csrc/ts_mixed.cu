@@ -33,6 +33,9 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "ts_mixed.h"
@@ -861,3 +864,145 @@ void mixed_materialize(MixedBufs& mb, const Phys&, cudaStream_t st) {
 double* mixed_state(MixedBufs& mb, int parity) { return mb.U[parity & 1]; }
 
 }  // namespace ts
+
+// ---------------------------------------------------------------------------
+// ts_advance_noalloc: the fused mixed-precision step for callers that may not
+// allocate device memory.  Everything the kernel needs beyond the caller's
+// input and output -- both state buffers, both residual buffers, the grid
+// geometry and the control word -- lives in one fixed array in device memory
+// that is part of this library's module.
+// ---------------------------------------------------------------------------
+namespace ts {
+namespace noalloc {
+
+constexpr size_t kNaPlane = TS_NOALLOC_MAX_PLANE;
+constexpr size_t kNaGeo = kNaPlane + 16;  // AxisGeo entries of all three axes together
+constexpr size_t kNaBytes = 2 * NV * kNaPlane * sizeof(double) + 2 * NV * kNaPlane * sizeof(float) +
+                            kNaGeo * sizeof(AxisGeo) + sizeof(Ctl) + 16 * 256;
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
+
+constexpr int kNaMaxDevices = 64;
+std::mutex g_noalloc_mutex;
+void* g_noalloc_base[kNaMaxDevices] = {};
+
+__global__ void k_na_scatter(const double* __restrict__ aos, Layout L, double* __restrict__ U) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= L.cells()) return;
+    const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
+    const long long c = L.at(i, j, k);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) U[(long long)v * L.plane + c] = aos[t * NV + v];
+}
+
+__global__ void k_na_gather(double* __restrict__ aos, Layout L, const double* __restrict__ U0,
+                            const double* __restrict__ U1, const Ctl* ctl) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= L.cells()) return;
+    const double* U = ctl->parity ? U1 : U0;
+    const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
+    const long long c = L.at(i, j, k);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) aos[t * NV + v] = U[(long long)v * L.plane + c];
+}
+
+}  // namespace noalloc
+}  // namespace ts
+
+using namespace ts;
+using namespace ts::noalloc;
+
+extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* state_in, double* state_out,
+                                        int32_t n_steps, void* stream, ts_step_info* info) {
+    if (!cfg || !state_in || !state_out) return fail(TS_ERR_INVALID, "NULL argument");
+    if (n_steps < 0) return fail(TS_ERR_INVALID, "n_steps must be >= 0");
+    if (cfg->precision != TS_PRECISION_MIXED)
+        return fail(TS_ERR_UNSUPPORTED, "ts_advance_noalloc runs the mixed-precision step only");
+    HostGrid grid;
+    std::string err;
+    ts_status s = build_grid(*cfg, grid, err);
+    if (s != TS_OK) return fail(s, err);
+    const Layout L = make_layout(*cfg);
+    const size_t geo_entries = (size_t)(L.nx + 2 * L.gx) + (L.ny + 2 * L.gy) + (L.nz + 2 * L.gz);
+    if ((size_t)L.plane > kNaPlane || geo_entries > kNaGeo)
+        return fail(TS_ERR_INVALID, "grid too large for ts_advance_noalloc: a padded variable plane holds " +
+                                        std::to_string(L.plane) + " elements, the limit is " +
+                                        std::to_string(kNaPlane));
+    int dev = cfg->device, ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || dev < 0 || dev >= ndev || dev >= kNaMaxDevices)
+        return fail(TS_ERR_INVALID, "device ordinal out of range");
+    int prev = -1;
+    cudaGetDevice(&prev);
+    if (prev != dev && cudaSetDevice(dev) != cudaSuccess) return fail(TS_ERR_CUDA, "cudaSetDevice failed");
+    struct Restore {
+        int prev, dev;
+        ~Restore() { if (prev >= 0 && prev != dev) cudaSetDevice(prev); }
+    } restore{prev, dev};
+
+    // Once per device, with that device current: the scratch array's device
+    // address (the host-side symbol is not a device pointer).
+    unsigned char* base;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+        if (!g_noalloc_base[dev]) {
+            void* p = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+            if (e != cudaSuccess || !p)
+                return fail(TS_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+            g_noalloc_base[dev] = p;
+        }
+        base = static_cast<unsigned char*>(g_noalloc_base[dev]);
+    }
+    // bump allocation inside the scratch array
+    size_t off = 0;
+    auto carve = [&](size_t bytes, void** out) -> ts_status {
+        off = (off + 255) & ~size_t(255);
+        if (off + bytes > kNaBytes) return fail(TS_ERR_INVALID, "ts_advance_noalloc scratch exhausted");
+        *out = base + off;
+        off += bytes;
+        return TS_OK;
+    };
+    Ctl* ctl = nullptr;
+    if ((s = carve(sizeof(Ctl), (void**)&ctl)) != TS_OK) return s;
+    MixedBufs mb;
+    const Phys ph = make_phys(*cfg);
+    if ((s = mixed_init(*cfg, L, ph, grid, ctl, carve, mb, err)) != TS_OK) return fail(s, err);
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    Ctl c;
+    std::memset(&c, 0, sizeof c);
+    c.time = info ? info->time : 0.0;
+    c.iteration = info ? info->iteration : 0;
+    c.next_sol = info ? info->next_solution_time : cfg->save_solution_time;
+    c.next_slice = info ? info->next_slice_time : cfg->save_slice_time;
+    c.max_iteration = cfg->max_iteration;
+    c.max_time = cfg->max_time;
+    c.save_sol = cfg->save_solution_time;
+    c.save_slice = cfg->save_slice_time;
+#define NA_CUDA(call)                                                                                    \
+    do {                                                                                                 \
+        cudaError_t e_ = (call);                                                                         \
+        if (e_ != cudaSuccess) return fail(TS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+    NA_CUDA(cudaMemcpyAsync(ctl, &c, sizeof c, cudaMemcpyHostToDevice, st));
+    NA_CUDA(cudaMemsetAsync(mb.R[0], 0, sizeof(float) * NV * L.plane, st));
+    const unsigned blocks = (unsigned)((L.cells() + 255) / 256);
+    k_na_scatter<<<blocks, 256, 0, st>>>(state_in, L, mb.U[0]);
+    for (int k = 0; k < n_steps; ++k) mixed_step(mb, ph, st);
+    mixed_materialize(mb, ph, st);
+    k_na_gather<<<blocks, 256, 0, st>>>(state_out, L, mb.U[0], mb.U[1], ctl);
+    NA_CUDA(cudaGetLastError());
+    NA_CUDA(cudaMemcpyAsync(&c, ctl, sizeof c, cudaMemcpyDeviceToHost, st));
+    NA_CUDA(cudaStreamSynchronize(st));
+#undef NA_CUDA
+    if (info) {
+        info->iteration = c.iteration;
+        info->health = c.health;
+        info->time = c.time;
+        info->dt = c.dt;
+        info->next_solution_time = c.next_sol;
+        info->next_slice_time = c.next_slice;
+        for (int v = 0; v < NV; ++v) info->residual[v] = 0.0;
+    }
+    return TS_OK;
+}
