@@ -183,11 +183,13 @@ ts_status ts_run(ts_handle* h, ts_step_info* info);
 ts_status ts_get_step_info(ts_handle* h, ts_step_info* info);
 ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info);
 
-/* Tile shape (cells per CTA along x and y) of the mixed-precision fused
-   kernel; tx*ty must be 32..256 threads in whole warps.  Results do not
-   depend on the tile: every face flux is a function of its two cells only.
-   TS_ERR_UNSUPPORTED for the FP64 path. */
-ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty);
+/* Launch shape of the mixed-precision fused kernel: the tile (cells per CTA
+   along x and y; compiled shapes: 3D 32x8, 16x16, 64x4; 2D 32x8, 16x16;
+   1D 256, 128) and the number of z chunks each tile column is cut into
+   (0 = chosen from the grid and the SM count).  Results do not depend on
+   either: every face flux is a function of its two cells only.
+   TS_ERR_UNSUPPORTED for the FP64 path or an uncompiled tile. */
+ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty, int32_t z_chunks);
 
 /* Waits for all work queued on the handle's stream. */
 ts_status ts_synchronize(ts_handle* h);

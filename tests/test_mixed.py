@@ -112,14 +112,15 @@ def test_mixed_tile_independent_bitwise(nd, tslib):
     if nd == 3:
         case = O.make_case(ndims=3, nx=37, ny=29, nz=21, periodic=(1, 0, 0), recon=3, solver=1, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, SYM, SYM])
-        tiles, scen, params = [(32, 8), (16, 16), (64, 4), (8, 4)], 2, [1.0, 0.1, 10.0, 0.2, 0.01]
+        tiles = [(32, 8, 0), (16, 16, 0), (64, 4, 0), (32, 8, 1), (32, 8, 3), (16, 16, 7)]
+        scen, params = 2, [1.0, 0.1, 10.0, 0.2, 0.01]
     elif nd == 2:
         case = O.make_case(ndims=2, nx=70, ny=45, periodic=(1, 0, 1), recon=3, solver=3, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, NAT, NAT])
-        tiles, scen, params = [(32, 8), (16, 16), (128, 2), (32, 1)], 1, [2.0, 1.0, 0.5, 2.5, 0.01]
+        tiles, scen, params = [(32, 8, 0), (16, 16, 0)], 1, [2.0, 1.0, 0.5, 2.5, 0.01]
     else:
         case = O.make_case(ndims=1, nx=1000, periodic=(0, 1, 1), recon=3, cfl=0.5, bc=[NAT] * 6)
-        tiles, scen, params = [(256, 1), (64, 1), (32, 1), (128, 1)], 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
+        tiles, scen, params = [(256, 1, 0), (128, 1, 0)], 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
     full = _full(case, scen, 3, params)
     outs = [run(case, full, 9, 1, tile=t)[0] for t in tiles]
     for o in outs[1:]:

@@ -118,7 +118,7 @@ def load(path: str = LIB_PATH):
     L.ts_get_step_info.argtypes = [C.c_void_p, P(StepInfo)]
     L.ts_set_step_info.argtypes = [C.c_void_p, P(StepInfo)]
     L.ts_synchronize.argtypes = [C.c_void_p]
-    L.ts_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32]
+    L.ts_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
     L.ts_set_tile.restype = C.c_int
     L.ts_grid_coordinates.argtypes = [P(Config)] + [P(C.c_double)] * 6
     L.ts_state_doubles.argtypes = [P(Config), C.c_int32]
@@ -288,5 +288,5 @@ class Solver:
     def synchronize(self):
         check(self.lib.ts_synchronize(self.h))
 
-    def set_tile(self, tx: int, ty: int):
-        check(self.lib.ts_set_tile(self.h, tx, ty))
+    def set_tile(self, tx: int, ty: int, z_chunks: int = 0):
+        check(self.lib.ts_set_tile(self.h, tx, ty, z_chunks))

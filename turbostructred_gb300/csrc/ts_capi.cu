@@ -481,13 +481,13 @@ ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info) {
     return h->push_ctl();
 }
 
-ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty) {
+ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty, int32_t z_chunks) {
     if (!h) return fail(TS_ERR_INVALID, "NULL handle");
     if (h->cfg.precision != TS_PRECISION_MIXED) return fail(TS_ERR_UNSUPPORTED, "tiles apply to the mixed path");
     DeviceGuard g(h->device);
     TS_CUDA(cudaStreamSynchronize(h->stream));
     std::string err;
-    ts_status s = mixed_set_tile(h->mb, tx, ty, err);
+    ts_status s = mixed_set_tile(h->mb, tx, ty, z_chunks, err);
     if (s != TS_OK) return fail(s, err);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);  // launch shape changed
     h->graphs.clear();

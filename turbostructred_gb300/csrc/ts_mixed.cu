@@ -14,11 +14,20 @@
 // pass per step: 40 B FP64 read + 20 B FP32 read + 40 B + 20 B written per
 // cell-update.  A final apply pass materialises the state for the host.
 //
-// Tiling.  Each CTA owns an x-y tile (TX x TY cells) and marches along z
-// (2.5D blocking), keeping a 3-plane ring of the FP32 working state with a
-// 2-cell halo, a 2-plane ring of limited half-slopes with a 1-cell halo and
-// the face fluxes in shared memory; CTAs get contiguous ranges of
-// (column, plane) work so the persistent grid is balanced to one plane.
+// Tiling.  Each CTA owns an x-y tile of TX x TY cells (compile-time, one
+// thread per tile cell) and marches along z (2.5D blocking), keeping a
+// 3-plane ring of the FP32 working state with a 2-cell halo, a 2-plane ring
+// of limited half-slopes with a 1-cell halo and the face fluxes in shared
+// memory.  Every thread has fixed roles: two working-state positions of the
+// halo box (loads for the next plane are issued into registers as soon as the
+// current plane is stored, so their latency hides behind the plane's
+// compute), up to two reconstruction positions, the x face left of its cell,
+// the y face below and the z face above (the tile's far faces go to the first
+// TX + TY threads), and its cell's residual.
+//
+// Schedule.  Work is (column, z-chunk) pairs indexed z-chunk-major and dealt
+// round-robin to the persistent CTAs, so CTAs running at the same time sweep
+// neighbouring columns at the same z and share halo rows through L2.
 //
 // Ghost cells are virtual: a load outside the domain wraps on periodic axes
 // and mirrors plus applies the boundary condition (BCGeneral.h:186-268)
@@ -53,10 +62,12 @@ struct MixArgs {
     int goff[3];  // index offset into geo per axis (ghost width or 0)
     Ctl* ctl;
     MixPhys mp;
-    int tx, ty, ncx;
-    long long total;  // columns x planes
-    int per_cta;      // planes per CTA
+    int ncx;      // tile columns along x
+    int ncol;     // tile columns
+    int ch;       // planes per z chunk
+    int nq;       // column-chunks = ncol * number of chunks
 };
+
 
 // ---------------------------------------------------------------------------
 // FP64 <-> FP32 on the integer pipe
@@ -230,98 +241,154 @@ __device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], co
     return roe32<A>(p, UL, UR, F);
 }
 
-// ---------------------------------------------------------------------------
-// Shared-memory layout of one CTA
-// ---------------------------------------------------------------------------
-template <int ND>
-struct Smem {
-    float* W;   // [WS][NV][BY][BX]  FP32 working state, 2-cell halo
-    float* D;   // [DS][3][NV][RY][RX] limited half-slopes, 1-cell halo
-    float* Fx;  // [6][TY][TX+1]
-    float* Fy;  // [6][TY+1][TX]
-    float* Fz;  // [2][6][TY][TX]
-    int TX, TY, BX, BY, RX, RY;
-    static constexpr int WS = ND == 3 ? 3 : 1;
-    static constexpr int DS = ND == 3 ? 2 : 1;
 
-    __device__ void setup(float* base, int tx, int ty) {
-        TX = tx; TY = ty;
-        BX = tx + 2 * HB; BY = ND >= 2 ? ty + 2 * HB : 1;
-        RX = tx + 2; RY = ND >= 2 ? ty + 2 : 1;
-        W = base;
-        D = W + WS * NV * BY * BX;
-        Fx = D + DS * 3 * NV * RY * RX;
-        Fy = Fx + 6 * ty * (tx + 1);
-        Fz = Fy + (ND >= 2 ? 6 * (ty + 1) * tx : 0);
+// ---------------------------------------------------------------------------
+// Compile-time tile geometry and shared-memory layout (floats)
+// ---------------------------------------------------------------------------
+template <int ND_, int TX_, int TY_>
+struct Tile {
+    static constexpr int ND = ND_;
+    static constexpr int TX = TX_;
+    static constexpr int TY = ND_ >= 2 ? TY_ : 1;
+    static constexpr int NT = TX * TY;
+    static constexpr int BX = TX + 2 * HB;                 // working-state box
+    static constexpr int BY = ND >= 2 ? TY + 2 * HB : 1;
+    static constexpr int RX = TX + 2;                      // reconstruction ring
+    static constexpr int RY = ND >= 2 ? TY + 2 : 1;
+    static constexpr int NBOX = BX * BY;
+    static constexpr int NRING = RX * RY;
+    static constexpr int NA = (NBOX + NT - 1) / NT;        // box positions per thread
+    static constexpr int NB = (NRING + NT - 1) / NT;       // ring positions per thread
+    static constexpr int WS = ND == 3 ? 3 : 1;             // working-state planes kept
+    static constexpr int DS = ND == 3 ? 2 : 1;             // slope planes kept
+    static constexpr int W_OFF = 0;
+    static constexpr int D_OFF = W_OFF + WS * NV * NBOX;
+    static constexpr int FX_OFF = D_OFF + DS * ND * NV * NRING;
+    static constexpr int FY_OFF = FX_OFF + 6 * TY * (TX + 1);
+    static constexpr int FZ_OFF = FY_OFF + (ND >= 2 ? 6 * (TY + 1) * TX : 0);
+    static constexpr int TOTAL = FZ_OFF + (ND == 3 ? 2 * 6 * TY * TX : 0);
+    static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
+
+    static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
+    static __device__ __forceinline__ int d(int s, int ax, int v, int ring) {
+        return D_OFF + ((s * ND + ax) * NV + v) * NRING + ring;
     }
-    static size_t bytes(int tx, int ty) {
-        const size_t bx = tx + 2 * HB, by = ND >= 2 ? ty + 2 * HB : 1, rx = tx + 2, ry = ND >= 2 ? ty + 2 : 1;
-        size_t f = WS * NV * by * bx + DS * 3 * NV * ry * rx + 6 * ty * (tx + 1);
-        if (ND >= 2) f += 6 * (ty + 1) * tx;
-        if (ND == 3) f += 2 * 6 * ty * tx;
-        return f * sizeof(float);
+    static __device__ __forceinline__ int fx(int v, int y, int x) { return FX_OFF + (v * TY + y) * (TX + 1) + x; }
+    static __device__ __forceinline__ int fy(int v, int y, int x) { return FY_OFF + (v * (TY + 1) + y) * TX + x; }
+    static __device__ __forceinline__ int fz(int s, int v, int y, int x) {
+        return FZ_OFF + ((s * 6 + v) * TY + y) * TX + x;
     }
-    __device__ float& w(int s, int v, int y, int x) { return W[((s * NV + v) * BY + y) * BX + x]; }
-    __device__ float& d(int s, int a, int v, int y, int x) { return D[(((s * 3 + a) * NV + v) * RY + y) * RX + x]; }
-    __device__ float& fx(int v, int y, int x) { return Fx[(v * TY + y) * (TX + 1) + x]; }
-    __device__ float& fy(int v, int y, int x) { return Fy[(v * (TY + 1) + y) * TX + x]; }
-    __device__ float& fz(int s, int v, int y, int x) { return Fz[((s * 6 + v) * TY + y) * TX + x]; }
 };
 
 __device__ __forceinline__ int wslot(int p) { return (p + 3) % 3; }
 __device__ __forceinline__ int dslot(int p) { return (p + 2) & 1; }
 
-// ---------------------------------------------------------------------------
-// Phase A: FP32 working state of plane p (and U^{n+1} of owned cells)
-// ---------------------------------------------------------------------------
-template <int ND>
-__device__ void load_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int p, int z0, int z1, float dtf,
-                           unsigned int& health) {
+// One working-state position of a thread: where its source cell lives in a
+// z-plane and how to turn it into the working copy.
+struct BoxPos {
+    int off;        // element offset of the source cell within a z-plane; -1: not used
+    int box;        // box index in shared memory
+    float cfxy;     // 1 / (hx hy) of the source cell
+    int xs, ys;     // boundary side applied after mirroring, or -1
+    bool own;       // the cell belongs to this tile: write U^{n+1}
+};
+
+struct Prefetch {
+    double u[NV];
+    float r[NV];
+};
+
+template <class T>
+__device__ __forceinline__ void setup_box(const MixArgs& a, int i0, int j0, BoxPos (&bp)[T::NA]) {
     const Layout& L = a.L;
-    const MixPhys& mp = a.mp;
-    const int slot = ND == 3 ? wslot(p) : 0;
-    int sk = 0, zs = -1;
-    if (ND == 3) resolve(p, L.nz, mp.periodic[2], 4, sk, zs);
-    const bool own_plane = p >= z0 && p < z1;
-    const double* __restrict__ Uin = a.U[a.ctl->parity];
-    double* __restrict__ Uout = a.U[a.ctl->parity ^ 1];
-    const float* __restrict__ Rin = a.R[a.ctl->parity];
-    const float hz_ih = a.geo[2][sk + a.goff[2]].ih;
-    const int n = s.BX * s.BY;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int lx = t % s.BX, ly = t / s.BX;
-        const int dx = lx < HB ? HB - lx : (lx >= s.TX + HB ? lx - s.TX - HB + 1 : 0);
-        const int dy = ND >= 2 ? (ly < HB ? HB - ly : (ly >= s.TY + HB ? ly - s.TY - HB + 1 : 0)) : 0;
+#pragma unroll
+    for (int k = 0; k < T::NA; ++k) {
+        const int t = threadIdx.x + k * T::NT;
+        bp[k].off = -1;
+        if (t >= T::NBOX) continue;
+        const int lx = t % T::BX, ly = t / T::BX;
+        const int dx = lx < HB ? HB - lx : (lx >= T::TX + HB ? lx - T::TX - HB + 1 : 0);
+        const int dy = T::ND >= 2 ? (ly < HB ? HB - ly : (ly >= T::TY + HB ? ly - T::TY - HB + 1 : 0)) : 0;
         if (dx + dy > HB) continue;
         const int gi = i0 + lx - HB;
-        const int gj = ND >= 2 ? j0 + ly - HB : 0;
+        const int gj = T::ND >= 2 ? j0 + ly - HB : 0;
         if (gi >= L.nx + HB) continue;
-        if (ND >= 2 && gj >= L.ny + HB) continue;
-        int si, xs, sj = 0, ys = -1;
-        resolve(gi, L.nx, mp.periodic[0], 0, si, xs);
-        if (ND >= 2) resolve(gj, L.ny, mp.periodic[1], 2, sj, ys);
-        const long long c = L.at(si, sj, sk);
-        const float cf = dtf * (a.geo[0][si + a.goff[0]].ih * a.geo[1][sj + a.goff[1]].ih * hz_ih);
-        double u[NV];
+        if (T::ND >= 2 && gj >= L.ny + HB) continue;
+        int si, sj = 0;
+        resolve(gi, L.nx, a.mp.periodic[0], 0, si, bp[k].xs);
+        bp[k].ys = -1;
+        if (T::ND >= 2) resolve(gj, L.ny, a.mp.periodic[1], 2, sj, bp[k].ys);
+        bp[k].off = (sj + L.gy) * L.px + (si + L.gx);
+        bp[k].box = t;
+        bp[k].cfxy = __ldg(&a.geo[0][si + a.goff[0]].ih) * __ldg(&a.geo[1][sj + a.goff[1]].ih);
+        bp[k].own = dx == 0 && dy == 0 && gi < L.nx && gj < L.ny;
+    }
+}
+
+__device__ __forceinline__ int plane_of(const MixArgs& a, int p, int& zs) {
+    int sk = 0;
+    zs = -1;
+    resolve(p, a.L.nz, a.mp.periodic[2], 4, sk, zs);
+    return sk;
+}
+
+// Issue the loads of plane p (FP64 state and FP32 pending residual) into registers.
+template <class T>
+__device__ __forceinline__ void issue(const MixArgs& a, const double* __restrict__ Uin,
+                                      const float* __restrict__ Rin, int p, const BoxPos (&bp)[T::NA],
+                                      Prefetch (&pf)[T::NA]) {
+    const Layout& L = a.L;
+    int zs;
+    const int sk = T::ND == 3 ? plane_of(a, p, zs) : 0;
+    const int zoff = (sk + L.gz) * L.px * L.ey;
+#pragma unroll
+    for (int k = 0; k < T::NA; ++k) {
+        if (bp[k].off < 0) continue;
+        const long long c = zoff + bp[k].off;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) pf[k].u[v] = __ldcg(Uin + v * L.plane + c);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) pf[k].r[v] = __ldcg(Rin + v * L.plane + c);
+    }
+}
+
+// Turn the prefetched plane p into the FP32 working copy in shared memory and
+// write U^{n+1} = U^n + dt R^n / V for the owned cells of planes [z0, z1).
+template <class T>
+__device__ __forceinline__ void store(const MixArgs& a, float* sm, double* __restrict__ Uout, int p, int z0, int z1,
+                                      float dtf, const BoxPos (&bp)[T::NA], const Prefetch (&pf)[T::NA],
+                                      unsigned int& health) {
+    const Layout& L = a.L;
+    const MixPhys& mp = a.mp;
+    int zs = -1;
+    const int sk = T::ND == 3 ? plane_of(a, p, zs) : 0;
+    const int zoff = (sk + L.gz) * L.px * L.ey;
+    const float cfz = dtf * __ldg(&a.geo[2][sk + a.goff[2]].ih);
+    const int slot = T::ND == 3 ? wslot(p) : 0;
+    const bool own_plane = p >= z0 && p < z1;
+#pragma unroll
+    for (int k = 0; k < T::NA; ++k) {
+        if (bp[k].off < 0) continue;
+        const float cf = bp[k].cfxy * cfz;
         float inc[NV], w[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) u[v] = Uin[(long long)v * L.plane + c];
+        for (int v = 0; v < NV; ++v) inc[v] = cf * pf[k].r[v];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) inc[v] = cf * Rin[(long long)v * L.plane + c];
+        for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(pf[k].u[v]) + inc[v];
+        w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf[k].u[4] - mp.einf_d) : f64_to_f32(pf[k].u[4])) +
+               inc[4];
+        if (bp[k].xs >= 0) bc32(mp, bp[k].xs, 0, w);
+        if (T::ND >= 2 && bp[k].ys >= 0) bc32(mp, bp[k].ys, 1, w);
+        if (T::ND == 3 && zs >= 0) bc32(mp, zs, 2, w);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
-        w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4])) + inc[4];
-        if (xs >= 0) bc32(mp, xs, 0, w);
-        if (ND >= 2 && ys >= 0) bc32(mp, ys, 1, w);
-        if (ND == 3 && zs >= 0) bc32(mp, zs, 2, w);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) s.w(slot, v, ly, lx) = w[v];
-        if (own_plane && dx == 0 && dy == 0 && gi < L.nx && gj < L.ny) {
+        for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp[k].box)] = w[v];
+        if (own_plane && bp[k].own) {
+            const long long c = zoff + bp[k].off;
             double un[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                un[v] = u[v] + f32_to_f64(inc[v]);
-                Uout[(long long)v * L.plane + c] = un[v];
+                un[v] = pf[k].u[v] + f32_to_f64(inc[v]);
+                __stcg(Uout + v * L.plane + c, un[v]);
             }
             if (!(un[0] > 0.0)) health |= (un[0] == un[0]) ? TS_HEALTH_NEG_DENSITY : TS_HEALTH_NAN;
             if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
@@ -329,66 +396,73 @@ __device__ void load_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int p,
     }
 }
 
-// ---------------------------------------------------------------------------
-// Phase B: limited half-slopes of plane p on the tile plus a 1-cell ring
-// ---------------------------------------------------------------------------
-template <int ND>
-__device__ void recon_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int p) {
+// Limited half-slopes of plane p on the tile and its 1-cell ring (corners
+// excluded); ring cells outside a non-periodic boundary are not needed.
+template <class T>
+__device__ __forceinline__ void recon(const MixArgs& a, float* sm, int i0, int j0, int p) {
     const Layout& L = a.L;
     const MixPhys& mp = a.mp;
-    const int ws = ND == 3 ? wslot(p) : 0;
-    const int wd = ND == 3 ? wslot(p - 1) : 0, wu = ND == 3 ? wslot(p + 1) : 0;
-    const int ds = ND == 3 ? dslot(p) : 0;
     int sk = 0, zs;
-    if (ND == 3) {
+    if (T::ND == 3) {
         if ((p < 0 || p >= L.nz) && !mp.periodic[2]) return;
-        resolve(p, L.nz, mp.periodic[2], 4, sk, zs);
+        resolve(p, L.nz, 1, 4, sk, zs);
     }
-    const AxisGeo gz = a.geo[2][sk + a.goff[2]];
-    const int n = s.RX * s.RY;
-    for (int t = threadIdx.x; t < n; t += blockDim.x) {
-        const int rx = t % s.RX, ry = t / s.RX;
-        const int ox = (rx < 1 || rx > s.TX) ? 1 : 0;
-        const int oy = ND >= 2 ? ((ry < 1 || ry > s.TY) ? 1 : 0) : 0;
-        if (ox + oy > 1) continue;
-        const int gi = i0 + rx - 1, gj = ND >= 2 ? j0 + ry - 1 : 0;
-        if (gi > L.nx || (ND >= 2 && gj > L.ny)) continue;
+    const int ws = T::ND == 3 ? wslot(p) : 0;
+    const int wd = T::ND == 3 ? wslot(p - 1) : 0, wu = T::ND == 3 ? wslot(p + 1) : 0;
+    const int ds = T::ND == 3 ? dslot(p) : 0;
+    AxisGeo gz;
+    if (T::ND == 3) gz = a.geo[2][sk + a.goff[2]];
+#pragma unroll
+    for (int k = 0; k < T::NB; ++k) {
+        const int t = threadIdx.x + k * T::NT;
+        if (t >= T::NRING) continue;
+        const int rx = t % T::RX, ry = t / T::RX;
+        const bool ox = rx < 1 || rx > T::TX;
+        const bool oy = T::ND >= 2 && (ry < 1 || ry > T::TY);
+        if (ox && oy) continue;
+        const int gi = i0 + rx - 1, gj = T::ND >= 2 ? j0 + ry - 1 : 0;
+        if (gi > L.nx || (T::ND >= 2 && gj > L.ny)) continue;
         if ((gi < 0 || gi >= L.nx) && !mp.periodic[0]) continue;
-        if (ND >= 2 && (gj < 0 || gj >= L.ny) && !mp.periodic[1]) continue;
-        int si, xs, sj = 0, ys;
+        if (T::ND >= 2 && (gj < 0 || gj >= L.ny) && !mp.periodic[1]) continue;
+        int si, sj = 0, xs, ys;
         resolve(gi, L.nx, 1, 0, si, xs);
-        if (ND >= 2) resolve(gj, L.ny, 1, 2, sj, ys);
-        const AxisGeo g[3] = {a.geo[0][si + a.goff[0]], a.geo[1][sj + a.goff[1]], gz};
-        const int lx = rx + 1, ly = ND >= 2 ? ry + 1 : 0;
+        if (T::ND >= 2) resolve(gj, L.ny, 1, 2, sj, ys);
+        AxisGeo g[3];
+        g[0] = a.geo[0][si + a.goff[0]];
+        if (T::ND >= 2) g[1] = a.geo[1][sj + a.goff[1]];
+        if (T::ND == 3) g[2] = gz;
+        const int box = (T::ND >= 2 ? (ry + 1) * T::BX : 0) + rx + 1;
         float eps2 = 0.0f;
         if (mp.limiter == TS_LIM_VENKATAKRISHNAN && mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
             // eps^2 = (K (hx hy hz)^(1/nd))^3 with K = 5 (Limiters.h:93-96, Constants.h:11)
-            const float vol = g[0].h * g[1].h * g[2].h;
-            eps2 = 125.0f * (ND == 3 ? vol : (ND == 2 ? vol * sqrtf(vol) : vol * vol * vol));
+            float vol = g[0].h;
+            if (T::ND >= 2) vol *= g[1].h;
+            if (T::ND == 3) vol *= g[2].h;
+            eps2 = 125.0f * (T::ND == 3 ? vol : (T::ND == 2 ? vol * sqrtf(vol) : vol * vol * vol));
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            const float w0 = s.w(ws, v, ly, lx);
+            const float w0 = sm[T::w(ws, v, box)];
             float nm[3], np[3];
-            nm[0] = s.w(ws, v, ly, lx - 1);
-            np[0] = s.w(ws, v, ly, lx + 1);
-            if (ND >= 2) { nm[1] = s.w(ws, v, ly - 1, lx); np[1] = s.w(ws, v, ly + 1, lx); }
-            if (ND == 3) { nm[2] = s.w(wd, v, ly, lx); np[2] = s.w(wu, v, ly, lx); }
+            nm[0] = sm[T::w(ws, v, box - 1)];
+            np[0] = sm[T::w(ws, v, box + 1)];
+            if (T::ND >= 2) { nm[1] = sm[T::w(ws, v, box - T::BX)]; np[1] = sm[T::w(ws, v, box + T::BX)]; }
+            if (T::ND == 3) { nm[2] = sm[T::w(wd, v, box)]; np[2] = sm[T::w(wu, v, box)]; }
             float dd[3];
             if (mp.recon == TS_RECON_ENO2_2POINTS) {
 #pragma unroll
-                for (int ax = 0; ax < ND; ++ax) {
+                for (int ax = 0; ax < T::ND; ++ax) {
                     const float gl = (w0 - nm[ax]) * g[ax].il, gr = (np[ax] - w0) * g[ax].ir;
                     dd[ax] = (fabsf(gl) < fabsf(gr) ? gl : gr) * g[ax].hh;
                 }
             } else {
 #pragma unroll
-                for (int ax = 0; ax < ND; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
+                for (int ax = 0; ax < T::ND; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
             }
             if (mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
                 float umax = w0, umin = w0;
 #pragma unroll
-                for (int ax = 0; ax < ND; ++ax) {
+                for (int ax = 0; ax < T::ND; ++ax) {
                     umax = fmaxf(umax, fmaxf(nm[ax], np[ax]));
                     umin = fminf(umin, fminf(nm[ax], np[ax]));
                 }
@@ -398,14 +472,15 @@ __device__ void recon_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int p
                         // Limiters.h:86-115, per face projection +-dd
                         const float iun = 2.0f / (umax - umin);
 #pragma unroll
-                        for (int ax = 0; ax < ND; ++ax) {
+                        for (int ax = 0; ax < T::ND; ++ax) {
 #pragma unroll
                             for (int sg = 0; sg < 2; ++sg) {
                                 const float d2 = sg ? -dd[ax] : dd[ax];
                                 if (d2 == 0.0f) continue;
                                 const float dm = ((d2 > 0.0f ? umax : umin) - w0) * iun;
                                 const float q = d2 * iun;
-                                const float r = ((dm * dm + eps2) + 2.0f * q * dm) / (dm * dm + 2.0f * q * q + dm * q + eps2);
+                                const float r =
+                                    ((dm * dm + eps2) + 2.0f * q * dm) / (dm * dm + 2.0f * q * q + dm * q + eps2);
                                 lim = fminf(lim, r);
                             }
                         }
@@ -414,25 +489,22 @@ __device__ void recon_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int p
                         // ratio over the 2*nd face projections +-dd.
                         float dmax = 0.0f;
 #pragma unroll
-                        for (int ax = 0; ax < ND; ++ax) dmax = fmaxf(dmax, fabsf(dd[ax]));
+                        for (int ax = 0; ax < T::ND; ++ax) dmax = fmaxf(dmax, fabsf(dd[ax]));
                         if (dmax > 0.0f) lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
                     }
                 }
 #pragma unroll
-                for (int ax = 0; ax < ND; ++ax) dd[ax] *= lim;
+                for (int ax = 0; ax < T::ND; ++ax) dd[ax] *= lim;
             }
 #pragma unroll
-            for (int ax = 0; ax < ND; ++ax) s.d(ds, ax, v, ry, rx) = dd[ax];
+            for (int ax = 0; ax < T::ND; ++ax) sm[T::d(ds, ax, v, t)] = dd[ax];
         }
     }
 }
 
-// ---------------------------------------------------------------------------
-// Phase C: fluxes of plane z (x and y faces) and of the z face above it
-// ---------------------------------------------------------------------------
-template <int ND, int SOLVER, int A>
-__device__ __forceinline__ void face_flux(const MixPhys& mp, bool bc_lo, bool bc_hi, float UL[NV], float UR[NV],
-                                          float F[NV], float& lam) {
+template <int SOLVER, int A>
+__device__ __forceinline__ float face_flux(const MixPhys& mp, bool bc_lo, bool bc_hi, float UL[NV], float UR[NV],
+                                           float F[NV]) {
     if (bc_lo) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) UL[v] = UR[v];
@@ -442,172 +514,201 @@ __device__ __forceinline__ void face_flux(const MixPhys& mp, bool bc_lo, bool bc
         for (int v = 0; v < NV; ++v) UR[v] = UL[v];
         bc32(mp, 2 * A + 1, A, UR);
     }
-    lam = flux32<SOLVER, A>(mp, UL, UR, F);
+    return flux32<SOLVER, A>(mp, UL, UR, F);
 }
 
-template <int ND, int SOLVER>
-__device__ void flux_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int z, bool do_xy, bool do_z) {
-    const Layout& L = a.L;
-    const MixPhys& mp = a.mp;
-    const bool pwc = mp.recon == TS_RECON_PIECEWISE_CONSTANT;
-    const int ws = ND == 3 ? wslot(z) : 0, ds = ND == 3 ? dslot(z) : 0;
-    float UL[NV], UR[NV], F[NV], lam;
-    if (do_xy) {
-        const int nfx = (s.TX + 1) * s.TY;
-        for (int t = threadIdx.x; t < nfx; t += blockDim.x) {
-            const int fx = t % (s.TX + 1), fy = t / (s.TX + 1);
-            const int gi = i0 + fx, gj = j0 + fy;
-            if (gi > L.nx || gj >= L.ny) continue;
-            const int ly = ND >= 2 ? fy + HB : 0, ry = ND >= 2 ? fy + 1 : 0;
+// x face fx (left of tile column fx) in tile row fy.
+template <class T, int SOLVER>
+__device__ __forceinline__ void xface(const MixArgs& a, float* sm, int i0, int j0, int ws, int ds, bool pwc, int fx,
+                                      int fy) {
+    const int gi = i0 + fx, gj = j0 + fy;
+    if (gi > a.L.nx || gj >= a.L.ny) return;
+    const int bl = (T::ND >= 2 ? (fy + HB) * T::BX : 0) + fx + 1;
+    const int rl = (T::ND >= 2 ? (fy + 1) * T::RX : 0) + fx;
+    float UL[NV], UR[NV], F[NV];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                UL[v] = s.w(ws, v, ly, fx + 1) + (pwc ? 0.0f : s.d(ds, 0, v, ry, fx));
-                UR[v] = s.w(ws, v, ly, fx + 2) - (pwc ? 0.0f : s.d(ds, 0, v, ry, fx + 1));
-            }
-            face_flux<ND, SOLVER, 0>(mp, gi == 0 && !mp.periodic[0], gi == L.nx && !mp.periodic[0], UL, UR, F, lam);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) s.fx(v, fy, fx) = F[v];
-            s.fx(5, fy, fx) = lam;
-        }
-        if (ND >= 2) {
-            const int nfy = s.TX * (s.TY + 1);
-            for (int t = threadIdx.x; t < nfy; t += blockDim.x) {
-                const int fx = t % s.TX, fy = t / s.TX;
-                const int gi = i0 + fx, gj = j0 + fy;
-                if (gi >= L.nx || gj > L.ny) continue;
-#pragma unroll
-                for (int v = 0; v < NV; ++v) {
-                    UL[v] = s.w(ws, v, fy + 1, fx + HB) + (pwc ? 0.0f : s.d(ds, 1, v, fy, fx + 1));
-                    UR[v] = s.w(ws, v, fy + 2, fx + HB) - (pwc ? 0.0f : s.d(ds, 1, v, fy + 1, fx + 1));
-                }
-                face_flux<ND, SOLVER, 1>(mp, gj == 0 && !mp.periodic[1], gj == L.ny && !mp.periodic[1], UL, UR, F,
-                                         lam);
-#pragma unroll
-                for (int v = 0; v < NV; ++v) s.fy(v, fy, fx) = F[v];
-                s.fy(5, fy, fx) = lam;
-            }
-        }
+    for (int v = 0; v < NV; ++v) {
+        UL[v] = sm[T::w(ws, v, bl)] + (pwc ? 0.0f : sm[T::d(ds, 0, v, rl)]);
+        UR[v] = sm[T::w(ws, v, bl + 1)] - (pwc ? 0.0f : sm[T::d(ds, 0, v, rl + 1)]);
     }
-    if (ND == 3 && do_z) {
-        // face between planes z and z+1, stored in slot dslot(z+1)
-        const int wu = wslot(z + 1), du = dslot(z + 1), fs = dslot(z + 1);
-        const int gk = z + 1;
-        const int nf = s.TX * s.TY;
-        for (int t = threadIdx.x; t < nf; t += blockDim.x) {
-            const int fx = t % s.TX, fy = t / s.TX;
-            if (i0 + fx >= L.nx || j0 + fy >= L.ny) continue;
+    const bool per = a.mp.periodic[0];
+    const float lam = face_flux<SOLVER, 0>(a.mp, gi == 0 && !per, gi == a.L.nx && !per, UL, UR, F);
 #pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                UL[v] = s.w(ws, v, fy + HB, fx + HB) + (pwc ? 0.0f : s.d(ds, 2, v, fy + 1, fx + 1));
-                UR[v] = s.w(wu, v, fy + HB, fx + HB) - (pwc ? 0.0f : s.d(du, 2, v, fy + 1, fx + 1));
-            }
-            face_flux<ND, SOLVER, 2>(mp, gk == 0 && !mp.periodic[2], gk == L.nz && !mp.periodic[2], UL, UR, F, lam);
-#pragma unroll
-            for (int v = 0; v < NV; ++v) s.fz(fs, v, fy, fx) = F[v];
-            s.fz(fs, 5, fy, fx) = lam;
-        }
-    }
+    for (int v = 0; v < NV; ++v) sm[T::fx(v, fy, fx)] = F[v];
+    sm[T::fx(5, fy, fx)] = lam;
 }
 
-// ---------------------------------------------------------------------------
-// Phase D: residual and spectral radius of the owned cells of plane z
-// ---------------------------------------------------------------------------
-template <int ND>
-__device__ void residual_plane(const MixArgs& a, Smem<ND>& s, int i0, int j0, int z, float& srmax) {
+template <class T, int SOLVER>
+__device__ __forceinline__ void yface(const MixArgs& a, float* sm, int i0, int j0, int ws, int ds, bool pwc, int fx,
+                                      int fy) {
+    const int gi = i0 + fx, gj = j0 + fy;
+    if (gi >= a.L.nx || gj > a.L.ny) return;
+    const int bl = (fy + 1) * T::BX + fx + HB;
+    const int rl = fy * T::RX + fx + 1;
+    float UL[NV], UR[NV], F[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        UL[v] = sm[T::w(ws, v, bl)] + (pwc ? 0.0f : sm[T::d(ds, 1, v, rl)]);
+        UR[v] = sm[T::w(ws, v, bl + T::BX)] - (pwc ? 0.0f : sm[T::d(ds, 1, v, rl + T::RX)]);
+    }
+    const bool per = a.mp.periodic[1];
+    const float lam = face_flux<SOLVER, 1>(a.mp, gj == 0 && !per, gj == a.L.ny && !per, UL, UR, F);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sm[T::fy(v, fy, fx)] = F[v];
+    sm[T::fy(5, fy, fx)] = lam;
+}
+
+// z face between planes z and z+1 above tile cell (fx, fy).
+template <class T, int SOLVER>
+__device__ __forceinline__ void zface(const MixArgs& a, float* sm, int i0, int j0, int z, bool pwc, int fx, int fy) {
+    if (i0 + fx >= a.L.nx || j0 + fy >= a.L.ny) return;
+    const int ws = wslot(z), wu = wslot(z + 1), ds = dslot(z), du = dslot(z + 1);
+    const int b = (fy + HB) * T::BX + fx + HB;
+    const int r = (fy + 1) * T::RX + fx + 1;
+    float UL[NV], UR[NV], F[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        UL[v] = sm[T::w(ws, v, b)] + (pwc ? 0.0f : sm[T::d(ds, 2, v, r)]);
+        UR[v] = sm[T::w(wu, v, b)] - (pwc ? 0.0f : sm[T::d(du, 2, v, r)]);
+    }
+    const int gk = z + 1;
+    const bool per = a.mp.periodic[2];
+    const float lam = face_flux<SOLVER, 2>(a.mp, gk == 0 && !per, gk == a.L.nz && !per, UL, UR, F);
+    const int fs = dslot(z + 1);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sm[T::fz(fs, v, fy, fx)] = F[v];
+    sm[T::fz(fs, 5, fy, fx)] = lam;
+}
+
+// Residual and spectral radius of the owned cell of this thread in plane z.
+template <class T>
+__device__ __forceinline__ void residual(const MixArgs& a, const float* sm, float* __restrict__ Rout, int i0, int j0,
+                                         int z, float& srmax) {
     const Layout& L = a.L;
-    const int t = threadIdx.x;
-    if (t >= s.TX * s.TY) return;
-    const int tx = t % s.TX, ty = t / s.TX;
+    const int tx = threadIdx.x % T::TX, ty = threadIdx.x / T::TX;
     const int gi = i0 + tx, gj = j0 + ty;
     if (gi >= L.nx || gj >= L.ny) return;
     const AxisGeo gx = a.geo[0][gi + a.goff[0]], gy = a.geo[1][gj + a.goff[1]], gz = a.geo[2][z + a.goff[2]];
     const float fsx = gy.h * gz.h, fsy = gx.h * gz.h, fsz = gx.h * gy.h;
     const float iv = gx.ih * gy.ih * gz.ih;
     float R[NV];
-    const float lxl = s.fx(5, ty, tx), lxr = s.fx(5, ty, tx + 1);
+    const float lxl = sm[T::fx(5, ty, tx)], lxr = sm[T::fx(5, ty, tx + 1)];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) R[v] = -(s.fx(v, ty, tx + 1) - s.fx(v, ty, tx)) * fsx;
+    for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * fsx;
     float sr = fsx * (lxl + lxr);
     if (gi == L.nx - 1) srmax = fmaxf(srmax, fsx * lxr * a.geo[0][L.nx + a.goff[0]].ih * gy.ih * gz.ih);
-    if (ND >= 2) {
+    if (T::ND >= 2) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (s.fy(v, ty + 1, tx) - s.fy(v, ty, tx)) * fsy;
-        const float lyr = s.fy(5, ty + 1, tx);
-        sr += fsy * (s.fy(5, ty, tx) + lyr);
+        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * fsy;
+        const float lyr = sm[T::fy(5, ty + 1, tx)];
+        sr += fsy * (sm[T::fy(5, ty, tx)] + lyr);
         if (gj == L.ny - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * a.geo[1][L.ny + a.goff[1]].ih * gz.ih);
     }
-    if (ND == 3) {
+    if (T::ND == 3) {
         const int dn = dslot(z), up = dslot(z + 1);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (s.fz(up, v, ty, tx) - s.fz(dn, v, ty, tx)) * fsz;
-        const float lzr = s.fz(up, 5, ty, tx);
-        sr += fsz * (s.fz(dn, 5, ty, tx) + lzr);
+        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * fsz;
+        const float lzr = sm[T::fz(up, 5, ty, tx)];
+        sr += fsz * (sm[T::fz(dn, 5, ty, tx)] + lzr);
         if (z == L.nz - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * a.geo[2][L.nz + a.goff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
-    float* __restrict__ Rout = a.R[a.ctl->parity ^ 1];
     const long long c = L.at(gi, gj, z);
 #pragma unroll
-    for (int v = 0; v < NV; ++v) Rout[(long long)v * L.plane + c] = R[v];
+    for (int v = 0; v < NV; ++v) __stcg(Rout + v * L.plane + c, R[v]);
 }
 
 // ---------------------------------------------------------------------------
 // The fused step kernel
 // ---------------------------------------------------------------------------
-template <int ND, int SOLVER>
-__global__ void __launch_bounds__(256) k_mix_step(MixArgs a) {
+template <class T, int SOLVER>
+__global__ void __launch_bounds__(T::NT) k_mix_step(MixArgs a) {
     Ctl* ctl = a.ctl;
     if (ctl->stop_req) return;
-    extern __shared__ float smem[];
-    Smem<ND> s;
-    s.setup(smem, a.tx, a.ty);
+    extern __shared__ float sm[];
     const Layout& L = a.L;
+    const int par = ctl->parity;
+    const double* __restrict__ Uin = a.U[par];
+    double* __restrict__ Uout = a.U[par ^ 1];
+    const float* __restrict__ Rin = a.R[par];
+    float* __restrict__ Rout = a.R[par ^ 1];
     const float dtf = f64_to_f32(ctl->dt_apply);
-    const int nz = ND == 3 ? L.nz : 1;
+    const bool pwc = a.mp.recon == TS_RECON_PIECEWISE_CONSTANT;
+    const int tx = threadIdx.x % T::TX, ty = threadIdx.x / T::TX;
     float srmax = 0.0f;
     unsigned int health = 0;
-    const long long beg = (long long)blockIdx.x * a.per_cta;
-    const long long end = min(beg + a.per_cta, a.total);
-    const bool pwc = a.mp.recon == TS_RECON_PIECEWISE_CONSTANT;
-    for (long long gidx = beg; gidx < end;) {
-        const int col = (int)(gidx / nz);
-        const int z0 = (int)(gidx % nz);
-        const int z1 = (int)min((long long)nz, z0 + (end - gidx));
-        const int i0 = (col % a.ncx) * a.tx;
-        const int j0 = (col / a.ncx) * a.ty;
-        if (ND < 3) {
-            load_plane<ND>(a, s, i0, j0, 0, 0, 1, dtf, health);
+    BoxPos bp[T::NA];
+    Prefetch pf[T::NA];
+
+    auto fluxes = [&](int i0, int j0, int z, bool do_xy, bool do_z) {
+        const int ws = T::ND == 3 ? wslot(z) : 0, ds = T::ND == 3 ? dslot(z) : 0;
+        if (do_xy) {
+            xface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, tx, ty);
+            if (T::ND >= 2) yface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, tx, ty);
+            if ((int)threadIdx.x < T::TY) xface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, T::TX, threadIdx.x);
+            else if (T::ND >= 2 && (int)threadIdx.x < T::TY + T::TX)
+                yface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, threadIdx.x - T::TY, T::TY);
+        }
+        if (T::ND == 3 && do_z) zface<T, SOLVER>(a, sm, i0, j0, z, pwc, tx, ty);
+    };
+
+    if (T::ND < 3) {
+        int q = blockIdx.x;
+        if (q < a.nq) {
+            setup_box<T>(a, (q % a.ncx) * T::TX, (q / a.ncx) * T::TY, bp);
+            issue<T>(a, Uin, Rin, 0, bp, pf);
+        }
+        while (q < a.nq) {
+            const int i0 = (q % a.ncx) * T::TX, j0 = (q / a.ncx) * T::TY;
+            store<T>(a, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
+            const int qn = q + gridDim.x;
+            if (qn < a.nq) {  // prefetch the next column while this one computes
+                setup_box<T>(a, (qn % a.ncx) * T::TX, (qn / a.ncx) * T::TY, bp);
+                issue<T>(a, Uin, Rin, 0, bp, pf);
+            }
             __syncthreads();
-            if (!pwc) { recon_plane<ND>(a, s, i0, j0, 0); __syncthreads(); }
-            flux_plane<ND, SOLVER>(a, s, i0, j0, 0, true, false);
+            if (!pwc) { recon<T>(a, sm, i0, j0, 0); __syncthreads(); }
+            fluxes(i0, j0, 0, true, false);
             __syncthreads();
-            residual_plane<ND>(a, s, i0, j0, 0, srmax);
+            residual<T>(a, sm, Rout, i0, j0, 0, srmax);
             __syncthreads();
-        } else {
-            // prologue: planes z0-2 .. z0+1, slopes of z0-1 and z0, z face z0-1/2
-            load_plane<ND>(a, s, i0, j0, z0 - 2, z0, z1, dtf, health);
-            load_plane<ND>(a, s, i0, j0, z0 - 1, z0, z1, dtf, health);
-            load_plane<ND>(a, s, i0, j0, z0, z0, z1, dtf, health);
+            q = qn;
+        }
+    } else {
+        for (int q = blockIdx.x; q < a.nq; q += gridDim.x) {
+            const int zc = q / a.ncol, col = q % a.ncol;
+            const int i0 = (col % a.ncx) * T::TX, j0 = (col / a.ncx) * T::TY;
+            const int z0 = zc * a.ch, z1 = min(L.nz, z0 + a.ch);
+            setup_box<T>(a, i0, j0, bp);
+            // prologue: planes z0-2 .. z0+1, slopes of z0-1 and z0, the z face z0-1/2
+            for (int p = z0 - 2; p <= z0; ++p) {
+                issue<T>(a, Uin, Rin, p, bp, pf);
+                store<T>(a, sm, Uout, p, z0, z1, dtf, bp, pf, health);
+            }
+            issue<T>(a, Uin, Rin, z0 + 1, bp, pf);
             __syncthreads();
-            if (!pwc) { recon_plane<ND>(a, s, i0, j0, z0 - 1); }
+            if (!pwc) recon<T>(a, sm, i0, j0, z0 - 1);
             __syncthreads();
-            load_plane<ND>(a, s, i0, j0, z0 + 1, z0, z1, dtf, health);
+            store<T>(a, sm, Uout, z0 + 1, z0, z1, dtf, bp, pf, health);
+            issue<T>(a, Uin, Rin, z0 + 2, bp, pf);
             __syncthreads();
-            if (!pwc) { recon_plane<ND>(a, s, i0, j0, z0); __syncthreads(); }
-            flux_plane<ND, SOLVER>(a, s, i0, j0, z0 - 1, false, true);
-            __syncthreads();
+            if (!pwc) { recon<T>(a, sm, i0, j0, z0); __syncthreads(); }
+            fluxes(i0, j0, z0 - 1, false, true);
+            __syncthreads();  // the first store below reuses the slot of plane z0-1
             for (int z = z0; z < z1; ++z) {
-                load_plane<ND>(a, s, i0, j0, z + 2, z0, z1, dtf, health);
+                // plane z+2 was prefetched during the previous plane's compute
+                store<T>(a, sm, Uout, z + 2, z0, z1, dtf, bp, pf, health);
+                if (z + 3 <= z1 + 1) issue<T>(a, Uin, Rin, z + 3, bp, pf);
                 __syncthreads();
-                if (!pwc) { recon_plane<ND>(a, s, i0, j0, z + 1); __syncthreads(); }
-                flux_plane<ND, SOLVER>(a, s, i0, j0, z, true, true);
+                if (!pwc) { recon<T>(a, sm, i0, j0, z + 1); __syncthreads(); }
+                fluxes(i0, j0, z, true, true);
                 __syncthreads();
-                residual_plane<ND>(a, s, i0, j0, z, srmax);
+                residual<T>(a, sm, Rout, i0, j0, z, srmax);
             }
             __syncthreads();
         }
-        gidx += z1 - z0;
     }
+
     // CFL: max over cells of SR/V, block max by warp shuffles, one atomic per
     // CTA; the last CTA to finish turns it into dt (FP64) and closes the step.
 #pragma unroll
@@ -622,7 +723,7 @@ __global__ void __launch_bounds__(256) k_mix_step(MixArgs a) {
     if (threadIdx.x == 0) {
         float m = 0.0f;
         unsigned int hh = 0;
-        for (int k = 0; k < (int)(blockDim.x + 31) / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
+        for (int k = 0; k < T::NT / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
         if (m > 0.0f) atomicMax(&ctl->srmax_bits, __float_as_uint(m));
         if (hh) atomicOr(&ctl->health, hh);
         __threadfence();
@@ -672,21 +773,40 @@ __global__ void k_mix_apply(MixArgs a) {
 
 __global__ void k_mix_clear_pending(Ctl* ctl) { ctl->dt_apply = 0.0; }
 
-template <int ND, int SOLVER>
-void launch_step(const MixedBufs& mb, const MixArgs& a, cudaStream_t st) {
-    k_mix_step<ND, SOLVER><<<mb.grid, mb.tx * mb.ty, mb.smem, st>>>(a);
+
+// Tile shapes compiled per dimension (one thread per tile cell).
+#define TS_MIXED_TILES_3D(X) X(3, 32, 8) X(3, 16, 16) X(3, 64, 4)
+#define TS_MIXED_TILES_2D(X) X(2, 32, 8) X(2, 16, 16)
+#define TS_MIXED_TILES_1D(X) X(1, 256, 1) X(1, 128, 1)
+
+template <class T, int SOLVER>
+cudaError_t prepare_kernel() {
+    return cudaFuncSetAttribute(k_mix_step<T, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::BYTES);
 }
 
-template <int ND, int SOLVER>
-cudaError_t set_smem_attr(size_t bytes) {
-    return cudaFuncSetAttribute(k_mix_step<ND, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
-}
-
-template <int ND, int SOLVER>
-int occupancy(int threads, size_t bytes) {
+template <class T, int SOLVER>
+int occupancy_of() {
     int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mix_step<ND, SOLVER>, threads, bytes);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mix_step<T, SOLVER>, T::NT, T::BYTES);
     return nb;
+}
+
+// Calls f.template operator()<Tile, SOLVER>() for the compiled tile matching
+// (nd, tx, ty); returns false when there is none.
+template <class F>
+bool with_tile(int nd, int tx, int ty, int solver, F&& f) {
+    bool found = false;
+#define TS_TRY(ND_, TX_, TY_)                                                                     \
+    if (!found && nd == ND_ && tx == TX_ && (ND_ == 1 || ty == TY_)) {                           \
+        found = true;                                                                            \
+        if (solver == TS_RS_HLLC) f.template operator()<Tile<ND_, TX_, TY_>, TS_RS_HLLC>();      \
+        else f.template operator()<Tile<ND_, TX_, TY_>, TS_RS_ROE_PIKE>();                       \
+    }
+    TS_MIXED_TILES_3D(TS_TRY)
+    TS_MIXED_TILES_2D(TS_TRY)
+    TS_MIXED_TILES_1D(TS_TRY)
+#undef TS_TRY
+    return found;
 }
 
 MixArgs make_args(const MixedBufs& mb) {
@@ -698,59 +818,67 @@ MixArgs make_args(const MixedBufs& mb) {
     a.goff[0] = mb.L.gx; a.goff[1] = mb.L.gy; a.goff[2] = mb.L.gz;
     a.ctl = mb.ctl;
     a.mp = mb.mp;
-    a.tx = mb.tx; a.ty = mb.ty;
     a.ncx = (mb.L.nx + mb.tx - 1) / mb.tx;
     const int ncy = mb.L.nd >= 2 ? (mb.L.ny + mb.ty - 1) / mb.ty : 1;
-    a.total = (long long)a.ncx * ncy * (mb.L.nd == 3 ? mb.L.nz : 1);
-    a.per_cta = mb.planes_per_cta;
+    a.ncol = a.ncx * ncy;
+    const int nz = mb.L.nd == 3 ? mb.L.nz : 1;
+    a.ch = mb.L.nd == 3 ? (nz + mb.zchunks - 1) / mb.zchunks : 1;
+    const int nchunks = (nz + a.ch - 1) / a.ch;
+    a.nq = a.ncol * nchunks;
     return a;
-}
-
-size_t smem_bytes(int nd, int tx, int ty) {
-    if (nd == 3) return Smem<3>::bytes(tx, ty);
-    if (nd == 2) return Smem<2>::bytes(tx, ty);
-    return Smem<1>::bytes(tx, ty);
-}
-
-template <class F>
-auto dispatch(int nd, int solver, F&& f) {
-    if (nd == 3) return solver == TS_RS_HLLC ? f.template operator()<3, TS_RS_HLLC>() : f.template operator()<3, TS_RS_ROE_PIKE>();
-    if (nd == 2) return solver == TS_RS_HLLC ? f.template operator()<2, TS_RS_HLLC>() : f.template operator()<2, TS_RS_ROE_PIKE>();
-    return solver == TS_RS_HLLC ? f.template operator()<1, TS_RS_HLLC>() : f.template operator()<1, TS_RS_ROE_PIKE>();
 }
 
 }  // namespace
 
-ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, std::string& err) {
+ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err) {
     const int nd = mb.L.nd;
     if (nd == 1) ty = 1;
-    if (tx < 4 || ty < 1 || tx * ty > 256 || (tx * ty) % 32 != 0) {
-        err = "tile must have 32..256 threads in whole warps";
-        return TS_ERR_INVALID;
+    size_t bytes = 0;
+    int per_sm = 0;
+    cudaError_t e = cudaSuccess;
+    const bool ok = with_tile(nd, tx, ty, mb.mp.solver, [&]<class T, int S>() {
+        bytes = T::BYTES;
+        e = prepare_kernel<T, S>();
+        if (e == cudaSuccess) per_sm = occupancy_of<T, S>();
+    });
+    if (!ok) {
+        err = "no compiled tile " + std::to_string(tx) + "x" + std::to_string(ty) + " for " + std::to_string(nd) + "D";
+        return TS_ERR_UNSUPPORTED;
     }
-    const size_t bytes = smem_bytes(nd, tx, ty);
-    if (bytes > 227 * 1024) { err = "tile needs too much shared memory"; return TS_ERR_INVALID; }
-    const int solver = mb.mp.solver;
-    cudaError_t e = dispatch(nd, solver, [&]<int ND, int S>() { return set_smem_attr<ND, S>(bytes); });
     if (e != cudaSuccess) { err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e); return TS_ERR_CUDA; }
-    const int per_sm = dispatch(nd, solver, [&]<int ND, int S>() { return occupancy<ND, S>(tx * ty, bytes); });
     if (per_sm < 1) { err = "mixed kernel does not fit on an SM with this tile"; return TS_ERR_UNSUPPORTED; }
     mb.tx = tx;
     mb.ty = ty;
     mb.smem = bytes;
     const int ncx = (mb.L.nx + tx - 1) / tx;
     const int ncy = nd >= 2 ? (mb.L.ny + ty - 1) / ty : 1;
-    const long long total = (long long)ncx * ncy * (nd == 3 ? mb.L.nz : 1);
+    const long long ncol = (long long)ncx * ncy;
     const long long slots = (long long)mb.sms * per_sm;
-    long long per = (total + slots - 1) / slots;
-    if (per < 1) per = 1;
-    mb.planes_per_cta = (int)per;
-    mb.grid = (int)((total + per - 1) / per);
+    const int nz = nd == 3 ? mb.L.nz : 1;
+    if (nd == 3 && zchunks <= 0) {
+        // Chunks of >= 16 planes; pick the count that best fills the
+        // persistent grid, charging ~3 planes of prologue per chunk.
+        double best = -1.0;
+        for (int c = 1; c <= std::max(1, nz / 16); ++c) {
+            const int ch = (nz + c - 1) / c;
+            const int nch = (nz + ch - 1) / ch;
+            const long long q = ncol * nch;
+            const double waves = std::ceil((double)q / (double)slots);
+            const double score = (double)q / (waves * (double)slots) / (1.0 + 3.0 / ch);
+            if (score > best + 1e-9) { best = score; zchunks = c; }
+        }
+    }
+    mb.zchunks = nd == 3 ? std::max(1, std::min(zchunks, nz)) : 1;
+    const int ch = (nz + mb.zchunks - 1) / mb.zchunks;
+    const long long q = ncol * ((nz + ch - 1) / ch);
+    mb.grid = (int)std::min<long long>(q, slots);
     return TS_OK;
 }
 
+
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                      const DeviceAlloc& alloc, MixedBufs& mb, std::string& err) {
+    if (L.plane > (1LL << 31) - 1) { err = "grid too large for the mixed path"; return TS_ERR_INVALID; }
     mb.L = L;
     mb.ctl = ctl;
     ts_status s;
@@ -837,13 +965,15 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
     cudaDeviceGetAttribute(&mb.sms, cudaDevAttrMultiProcessorCount, dev);
     const int tx = L.nd == 1 ? 256 : 32;
     const int ty = L.nd == 1 ? 1 : 8;
-    return mixed_set_tile(mb, tx, ty, err);
+    return mixed_set_tile(mb, tx, ty, 0, err);
 }
+
 
 void mixed_step(MixedBufs& mb, const Phys&, cudaStream_t st, cudaEvent_t* ev, int* n_launch, const char** names) {
     const MixArgs a = make_args(mb);
     if (ev) cudaEventRecord(ev[0], st);
-    dispatch(mb.L.nd, mb.mp.solver, [&]<int ND, int S>() { launch_step<ND, S>(mb, a, st); return 0; });
+    with_tile(mb.L.nd, mb.tx, mb.ty, mb.mp.solver,
+              [&]<class T, int S>() { k_mix_step<T, S><<<mb.grid, T::NT, T::BYTES, st>>>(a); });
     if (ev) cudaEventRecord(ev[1], st);
     if (names) names[0] = "k_mix_step";
     if (n_launch) *n_launch = 1;

@@ -41,9 +41,9 @@ struct MixedBufs {
     const AxisGeo* geo[3] = {nullptr, nullptr, nullptr};
     Ctl* ctl = nullptr;
     MixPhys mp;
-    int tx = 32, ty = 8;   // tile
+    int tx = 32, ty = 8;   // tile (one of the compiled shapes)
+    int zchunks = 1;       // z chunks per column (3D)
     int grid = 0;          // persistent CTAs
-    int planes_per_cta = 0;
     size_t smem = 0;
     int sms = 0;
 };
@@ -52,8 +52,9 @@ using DeviceAlloc = std::function<ts_status(size_t bytes, void** out)>;
 
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                      const DeviceAlloc& alloc, MixedBufs& mb, std::string& err);
-// Choose the tile shape (tx, ty) and recompute the persistent grid.
-ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, std::string& err);
+// Choose the tile shape (tx, ty) and the z chunking (0 = automatic), and
+// recompute the persistent grid.
+ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err);
 
 constexpr int kMixedMaxLaunches = 4;
 void mixed_step(MixedBufs& mb, const Phys& ph, cudaStream_t st, cudaEvent_t* ev = nullptr, int* n_launch = nullptr,
