@@ -218,6 +218,62 @@ ts_status ts_fill_scenario(const ts_config* cfg, int32_t scenario, uint64_t seed
 /* The hash RNG the scenarios use: uniform double in [0,1). */
 double ts_hash_uniform(uint64_t seed, int64_t i, int64_t j, int64_t k);
 
+/* ---------------------------------------------------------------------------
+   Batches: many independent problems of different sizes advanced together.
+   No counterpart in the reference (one Kernel per process there); each
+   problem follows Kernel::Run semantics with its own dt (CFL minimum over its
+   own cells) and its own MaxTime / MaxIteration.  All problems of a batch are
+   1D or 2D, mixed precision; solvers and equations of state may differ.
+   One stage of every unfinished problem is one launch of the fused kernel per
+   (dimension, Riemann solver) present, over a work list of (problem, tile)
+   items, largest problems first; stage
+   chunks are replayed from CUDA graphs while the membership is unchanged.
+   --------------------------------------------------------------------------- */
+typedef struct ts_batch ts_batch;
+
+/* memory_budget: bytes of device memory for all problem states (one arena). */
+ts_status ts_batch_create(int32_t device, size_t memory_budget, ts_batch** out);
+void ts_batch_destroy(ts_batch* b);
+
+/* Adds a problem with its initial state (host, TS_LAYOUT_INTERIOR); cfg must
+   be 1D/2D with TS_PRECISION_MIXED.  TS_ERR_NO_MEMORY when the arena cannot
+   hold it (nothing is changed then).  *id identifies it until removed. */
+ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, int32_t* id);
+
+/* Device bytes a problem would take in a batch arena (0: not batchable). */
+size_t ts_batch_problem_bytes(const ts_config* cfg);
+
+/* n_stages stages of every unfinished problem (finished ones are skipped). */
+ts_status ts_batch_step(ts_batch* b, int32_t n_stages);
+
+/* Stages until every problem has finished (MaxTime or MaxIteration), at most
+   max_stages (<= 0: no limit).  *active receives the problems still running.
+   A problem whose state turns non-physical (NaN, density <= 0) is stopped
+   and reported finished; ts_batch_get returns its health flags. */
+ts_status ts_batch_run(ts_batch* b, int32_t max_stages, int32_t* active);
+
+/* Ids of finished problems not yet collected (up to cap); *n receives the count. */
+ts_status ts_batch_finished(ts_batch* b, int32_t* ids, int32_t cap, int32_t* n);
+
+/* State (TS_LAYOUT_INTERIOR, may be NULL) and step info of a problem. */
+ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* info);
+
+/* Frees a problem's slot and memory. */
+ts_status ts_batch_remove(ts_batch* b, int32_t id);
+
+/* Launch shape for the problems of dimension nd (tile along x, y; see
+   ts_set_tile) and CTAs per SM of the persistent grid (0 = as many as fit). */
+ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int32_t ctas_per_sm);
+
+/* Autotuner: times `stages` stages of the current batch for every compiled
+   tile and CTA count, restoring the problems' states after each trial, and
+   keeps the fastest; *tx, *ty, *ctas_per_sm receive the choice for the
+   batch's dominant dimension. */
+ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx, int32_t* ty, int32_t* ctas_per_sm);
+
+/* Totals since creation: cell-updates done, stages launched, kernel launches. */
+ts_status ts_batch_stats(ts_batch* b, double* cell_updates, int64_t* stages, int64_t* launches);
+
 /* Advance a state by n_steps of the mixed-precision fused step without
    allocating any device memory.  No counterpart in the reference: this is
    for callers that are not allowed to call cudaMalloc themselves or through

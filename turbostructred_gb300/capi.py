@@ -92,6 +92,9 @@ EXPORTS = [
     "ts_run", "ts_set_tile",
     "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates", "ts_state_doubles",
     "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
+    "ts_batch_create", "ts_batch_destroy", "ts_batch_add", "ts_batch_problem_bytes", "ts_batch_step",
+    "ts_batch_run", "ts_batch_finished", "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile",
+    "ts_batch_autotune", "ts_batch_stats",
 ]
 
 _lib = None
@@ -126,6 +129,23 @@ def load(path: str = LIB_PATH):
     L.ts_fill_scenario.argtypes = [P(Config), C.c_int32, C.c_uint64, P(C.c_double), C.c_int32, P(C.c_double)]
     L.ts_hash_uniform.argtypes = [C.c_uint64, C.c_int64, C.c_int64, C.c_int64]
     L.ts_hash_uniform.restype = C.c_double
+    L.ts_batch_create.argtypes = [C.c_int32, C.c_size_t, P(C.c_void_p)]
+    L.ts_batch_destroy.argtypes = [C.c_void_p]
+    L.ts_batch_destroy.restype = None
+    L.ts_batch_add.argtypes = [C.c_void_p, P(Config), P(C.c_double), P(C.c_int32)]
+    L.ts_batch_problem_bytes.argtypes = [P(Config)]
+    L.ts_batch_problem_bytes.restype = C.c_size_t
+    L.ts_batch_step.argtypes = [C.c_void_p, C.c_int32]
+    L.ts_batch_run.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32)]
+    L.ts_batch_finished.argtypes = [C.c_void_p, P(C.c_int32), C.c_int32, P(C.c_int32)]
+    L.ts_batch_get.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(StepInfo)]
+    L.ts_batch_remove.argtypes = [C.c_void_p, C.c_int32]
+    L.ts_batch_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.ts_batch_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
+    L.ts_batch_stats.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), P(C.c_int64)]
+    for name in ("ts_batch_create", "ts_batch_add", "ts_batch_step", "ts_batch_run", "ts_batch_finished",
+                 "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile", "ts_batch_autotune", "ts_batch_stats"):
+        getattr(L, name).restype = C.c_int
     L.ts_last_error.restype = C.c_char_p
     L.ts_status_string.restype = C.c_char_p
     for name in ("ts_create", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
@@ -290,3 +310,85 @@ class Solver:
 
     def set_tile(self, tx: int, ty: int, z_chunks: int = 0):
         check(self.lib.ts_set_tile(self.h, tx, ty, z_chunks))
+
+
+def batch_problem_bytes(case: dict) -> int:
+    cfg, keep = to_config(case, PRECISION_MIXED)
+    return int(load().ts_batch_problem_bytes(C.byref(cfg)))
+
+
+class Batch:
+    """Independent 1D/2D problems advanced together (mixed precision), each
+    under Kernel::Run termination rules with its own dt."""
+
+    def __init__(self, memory_budget: int, device: int = 0):
+        self.lib = load()
+        b = C.c_void_p()
+        check(self.lib.ts_batch_create(device, memory_budget, C.byref(b)))
+        self.b = b
+        self.cases = {}
+
+    def close(self):
+        if self.b:
+            self.lib.ts_batch_destroy(self.b)
+            self.b = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def add(self, case: dict, values: np.ndarray) -> int:
+        cfg, keep = to_config(case, PRECISION_MIXED)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        assert v.size == int(np.prod(interior_shape(case)))
+        pid = C.c_int32()
+        check(self.lib.ts_batch_add(self.b, C.byref(cfg), v.ctypes.data_as(C.POINTER(C.c_double)), C.byref(pid)))
+        self.cases[pid.value] = case
+        return pid.value
+
+    def step(self, n: int = 1):
+        check(self.lib.ts_batch_step(self.b, n))
+
+    def run(self, max_stages: int = 0) -> int:
+        a = C.c_int32()
+        check(self.lib.ts_batch_run(self.b, max_stages, C.byref(a)))
+        return a.value
+
+    def finished(self, cap: int = 1 << 16) -> list:
+        ids = (C.c_int32 * cap)()
+        n = C.c_int32()
+        check(self.lib.ts_batch_finished(self.b, ids, cap, C.byref(n)))
+        return list(ids[:n.value])
+
+    def get(self, pid: int, want_state: bool = True):
+        si = StepInfo()
+        case = self.cases.get(pid)
+        out = np.empty(interior_shape(case)) if want_state and case is not None else None
+        ptr = out.ctypes.data_as(C.POINTER(C.c_double)) if out is not None else None
+        check(self.lib.ts_batch_get(self.b, pid, ptr, C.byref(si)))
+        return out, si.as_dict()
+
+    def remove(self, pid: int):
+        check(self.lib.ts_batch_remove(self.b, pid))
+        self.cases.pop(pid, None)
+
+    def set_tile(self, nd: int, tx: int, ty: int = 1, ctas_per_sm: int = 0):
+        check(self.lib.ts_batch_set_tile(self.b, nd, tx, ty, ctas_per_sm))
+
+    def autotune(self, stages: int = 8):
+        tx, ty, ct = C.c_int32(), C.c_int32(), C.c_int32()
+        check(self.lib.ts_batch_autotune(self.b, stages, C.byref(tx), C.byref(ty), C.byref(ct)))
+        return tx.value, ty.value, ct.value
+
+    def stats(self) -> dict:
+        cu, st, la = C.c_double(), C.c_int64(), C.c_int64()
+        check(self.lib.ts_batch_stats(self.b, C.byref(cu), C.byref(st), C.byref(la)))
+        return dict(cell_updates=cu.value, stages=st.value, launches=la.value)

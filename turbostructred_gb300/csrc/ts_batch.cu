@@ -1,0 +1,656 @@
+// Batches of independent 1D/2D problems advanced by the fused mixed-precision
+// kernel (include/ts_fvm.h, ts_batch_*).
+//
+// Memory: one device arena (the batch's budget) with a first-fit free list
+// kept on the host; each problem takes its two FP64 state buffers, two FP32
+// residual buffers and its per-axis geometry from it.  A slot table holds
+// every problem's descriptor and control word in device memory.
+//
+// A stage is one launch of the batched kernel per Riemann solver present,
+// over a work list of (slot, tile item) pairs sorted by problem size,
+// largest first.  Finished problems' items skip themselves on the device;
+// the list is rebuilt when membership changes or when most of it is idle.
+// Chunks of stages are captured once into a CUDA graph and replayed while the
+// list is unchanged (the list and descriptors live in device buffers, so
+// replays see updated control words).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "ts_mixed.h"
+
+namespace ts {
+namespace {
+
+#define TB_CUDA(call)                                                                                   \
+    do {                                                                                                \
+        cudaError_t e_ = (call);                                                                        \
+        if (e_ != cudaSuccess)                                                                          \
+            return fail(e_ == cudaErrorMemoryAllocation ? TS_ERR_NO_MEMORY : TS_ERR_CUDA,               \
+                        std::string(#call) + ": " + cudaGetErrorString(e_));                            \
+    } while (0)
+
+constexpr size_t kAlign = 256;
+
+// First-fit allocator over one device allocation; bookkeeping on the host.
+class Arena {
+public:
+    char* base = nullptr;
+    size_t size = 0, used = 0, high = 0;
+    std::map<size_t, size_t> free_;  // offset -> bytes
+    std::map<size_t, size_t> taken_;
+
+    cudaError_t init(size_t bytes) {
+        size = (bytes + kAlign - 1) & ~(kAlign - 1);
+        cudaError_t e = cudaMalloc(&base, size);
+        if (e == cudaSuccess) free_[0] = size;
+        return e;
+    }
+    ~Arena() { if (base) cudaFree(base); }
+    void* take(size_t bytes) {
+        bytes = (bytes + kAlign - 1) & ~(kAlign - 1);
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second < bytes) continue;
+            const size_t off = it->first, len = it->second;
+            free_.erase(it);
+            if (len > bytes) free_[off + bytes] = len - bytes;
+            taken_[off] = bytes;
+            used += bytes;
+            high = std::max(high, off + bytes);
+            return base + off;
+        }
+        return nullptr;
+    }
+    void give(void* p) {
+        const size_t off = (size_t)((char*)p - base);
+        auto t = taken_.find(off);
+        if (t == taken_.end()) return;
+        size_t o = off, len = t->second;
+        used -= len;
+        taken_.erase(t);
+        auto nx = free_.lower_bound(o);
+        if (nx != free_.end() && nx->first == o + len) { len += nx->second; free_.erase(nx); }
+        auto pv = free_.lower_bound(o);
+        if (pv != free_.begin()) {
+            --pv;
+            if (pv->first + pv->second == o) { o = pv->first; len += pv->second; free_.erase(pv); }
+        }
+        free_[o] = len;
+    }
+};
+
+__global__ void k_b_scatter(const double* __restrict__ aos, Layout L, double* __restrict__ U) {
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= L.cells()) return;
+    const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
+    const long long c = L.at(i, j, k);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) U[(long long)v * L.plane + c] = aos[t * NV + v];
+}
+
+// Interior cells of problem p's current state to AoS order.
+__global__ void k_b_gather(double* __restrict__ aos, const ProbDesc* __restrict__ probs, int p) {
+    const ProbDesc& d = probs[p];
+    const Layout& L = d.L;
+    const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (t >= L.cells()) return;
+    const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
+    const double* U = d.U[d.ctl->parity];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) aos[t * NV + v] = U[(long long)v * L.plane + L.at(i, j, k)];
+}
+
+struct Slot {
+    bool used = false;
+    int id = -1;
+    bool collected = false;   // reported by ts_batch_finished
+    long long cells = 0;
+    std::vector<void*> mem;
+    ts_config cfg;
+};
+
+struct Group {
+    int nd = 0, solver = 0;
+    int2* d_items = nullptr;
+    int cap = 0, n = 0;
+    int grid = 0;
+};
+
+struct Tune {
+    int tx, ty, ctas;  // ctas 0: as many as fit
+};
+
+}  // namespace
+}  // namespace ts
+
+using namespace ts;
+
+struct ts_batch {
+    int device = 0, sms = 0;
+    cudaStream_t stream = nullptr;
+    Arena arena;
+    std::vector<Slot> slots;
+    std::vector<ProbDesc> desc;
+    ProbDesc* d_desc = nullptr;
+    Ctl* d_ctl = nullptr;
+    Ctl* h_ctl = nullptr;  // pinned mirror
+    int capacity = 0;
+    std::map<int, int> id2slot;
+    int next_id = 0;
+    std::vector<Group> groups;
+    bool dirty = true;
+    std::map<int, cudaGraphExec_t> graphs;
+    Tune tune[4] = {{0, 0, 0}, {256, 1, 0}, {32, 8, 0}, {32, 8, 0}};
+    double* stage_buf = nullptr;
+    size_t stage_doubles = 0;
+    double done_cell_updates = 0.0;  // of removed problems
+    long long stages = 0, launches = 0;
+
+    ~ts_batch() {
+        int prev = -1;
+        cudaGetDevice(&prev);
+        cudaSetDevice(device);
+        drop_graphs();
+        for (auto& g : groups) cudaFree(g.d_items);
+        cudaFree(d_desc);
+        cudaFree(d_ctl);
+        cudaFreeHost(h_ctl);
+        cudaFree(stage_buf);
+        if (stream) cudaStreamDestroy(stream);
+        if (prev >= 0) cudaSetDevice(prev);
+    }
+
+    void drop_graphs() {
+        for (auto& kv : graphs) cudaGraphExecDestroy(kv.second);
+        graphs.clear();
+    }
+
+    ts_status grow(int need) {
+        if (need <= capacity) return TS_OK;
+        int cap = std::max(64, capacity);
+        while (cap < need) cap *= 2;
+        ProbDesc* nd_ = nullptr;
+        Ctl* nc = nullptr;
+        Ctl* nh = nullptr;
+        TB_CUDA(cudaMalloc(&nd_, sizeof(ProbDesc) * cap));
+        TB_CUDA(cudaMalloc(&nc, sizeof(Ctl) * cap));
+        TB_CUDA(cudaMallocHost(&nh, sizeof(Ctl) * cap));
+        std::memset(nh, 0, sizeof(Ctl) * cap);
+        TB_CUDA(cudaStreamSynchronize(stream));
+        if (capacity) {
+            TB_CUDA(cudaMemcpy(nc, d_ctl, sizeof(Ctl) * capacity, cudaMemcpyDeviceToDevice));
+            std::memcpy(nh, h_ctl, sizeof(Ctl) * capacity);
+        }
+        cudaFree(d_desc);
+        cudaFree(d_ctl);
+        cudaFreeHost(h_ctl);
+        d_desc = nd_;
+        d_ctl = nc;
+        h_ctl = nh;
+        capacity = cap;
+        slots.resize(cap);
+        desc.resize(cap);
+        // control-word pointers moved: re-point every descriptor
+        for (int s = 0; s < cap; ++s) {
+            if (!slots[s].used) continue;
+            desc[s].ctl = d_ctl + s;
+        }
+        TB_CUDA(cudaMemcpy(d_desc, desc.data(), sizeof(ProbDesc) * cap, cudaMemcpyHostToDevice));
+        dirty = true;
+        return TS_OK;
+    }
+
+    int per_sm(int nd, int solver) const {
+        size_t b;
+        int n = 0;
+        mixed_tile_info(nd, tune[nd].tx, tune[nd].ty, solver, &b, &n, true);
+        if (tune[nd].ctas > 0) n = std::min(n, tune[nd].ctas);
+        return std::max(n, 0);
+    }
+
+    // Work items of unfinished problems, grouped by (nd, solver), each group
+    // sorted by problem size, largest first.
+    ts_status rebuild() {
+        std::map<std::pair<int, int>, std::vector<int>> bykey;
+        for (int s = 0; s < capacity; ++s) {
+            if (!slots[s].used || h_ctl[s].stop_req) continue;
+            bykey[{desc[s].L.nd, desc[s].mp.solver}].push_back(s);
+        }
+        std::vector<Group> ng;
+        for (auto& kv : bykey) {
+            Group g;
+            g.nd = kv.first.first;
+            g.solver = kv.first.second;
+            auto& v = kv.second;
+            std::stable_sort(v.begin(), v.end(), [&](int a, int b2) { return slots[a].cells > slots[b2].cells; });
+            std::vector<int2> items;
+            for (int s : v)
+                for (int q = 0; q < desc[s].nq; ++q) items.push_back(make_int2(s, q));
+            g.n = (int)items.size();
+            // reuse an old buffer of the same key when large enough
+            for (auto& og : groups)
+                if (og.d_items && og.nd == g.nd && og.solver == g.solver && og.cap >= g.n) {
+                    g.d_items = og.d_items; g.cap = og.cap; og.d_items = nullptr;
+                    break;
+                }
+            if (!g.d_items) {
+                g.cap = std::max(1024, g.n);
+                TB_CUDA(cudaMalloc(&g.d_items, sizeof(int2) * g.cap));
+            }
+            TB_CUDA(cudaMemcpyAsync(g.d_items, items.data(), sizeof(int2) * g.n, cudaMemcpyHostToDevice, stream));
+            g.grid = std::min(g.n, std::max(1, per_sm(g.nd, g.solver)) * sms);
+            ng.push_back(g);
+        }
+        for (auto& og : groups) cudaFree(og.d_items);
+        groups.swap(ng);
+        drop_graphs();
+        dirty = false;
+        return TS_OK;
+    }
+
+    void enqueue_stage() {
+        for (auto& g : groups) {
+            const Tune& t = tune[g.nd];
+            mixed_launch_batch(g.nd, t.tx, t.ty, g.solver, g.grid, d_desc, g.d_items, g.n, stream);
+            ++launches;
+        }
+        ++stages;
+    }
+
+    ts_status launch(int n) {
+        if (dirty) { ts_status s = rebuild(); if (s != TS_OK) return s; }
+        if (groups.empty()) return TS_OK;
+        static const int chunks[3] = {32, 4, 1};
+        for (int c : chunks) {
+            while (n >= c) {
+                auto it = graphs.find(c);
+                cudaGraphExec_t ex;
+                if (it == graphs.end()) {
+                    cudaGraph_t gph;
+                    const long long s0 = stages, l0 = launches;
+                    TB_CUDA(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+                    for (int k = 0; k < c; ++k) enqueue_stage();
+                    cudaError_t le = cudaGetLastError();
+                    TB_CUDA(cudaStreamEndCapture(stream, &gph));
+                    if (le != cudaSuccess) return fail(TS_ERR_CUDA, std::string("capture: ") + cudaGetErrorString(le));
+                    stages = s0; launches = l0;
+                    cudaError_t ie = cudaGraphInstantiate(&ex, gph, 0);
+                    cudaGraphDestroy(gph);
+                    if (ie != cudaSuccess) return fail(TS_ERR_CUDA, std::string("instantiate: ") + cudaGetErrorString(ie));
+                    graphs[c] = ex;
+                } else {
+                    ex = it->second;
+                }
+                TB_CUDA(cudaGraphLaunch(ex, stream));
+                stages += c;
+                launches += (long long)c * (long long)groups.size();
+                n -= c;
+            }
+        }
+        return TS_OK;
+    }
+
+    // Control words to the host.  A problem whose state turned non-physical
+    // (health flags) will not reach its end time: it is stopped here and
+    // reported finished with its flags.
+    ts_status pull() {
+        TB_CUDA(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl) * capacity, cudaMemcpyDeviceToHost, stream));
+        TB_CUDA(cudaStreamSynchronize(stream));
+        for (int s = 0; s < capacity; ++s) {
+            if (!slots[s].used || h_ctl[s].stop_req || !h_ctl[s].health) continue;
+            h_ctl[s].stop_req = 1;
+            TB_CUDA(cudaMemcpyAsync(&d_ctl[s].stop_req, &h_ctl[s].stop_req, sizeof(int), cudaMemcpyHostToDevice,
+                                    stream));
+            dirty = true;
+        }
+        TB_CUDA(cudaStreamSynchronize(stream));
+        return TS_OK;
+    }
+
+    int active(long long* items_active, long long* items_listed) const {
+        int a = 0;
+        long long ia = 0;
+        for (int s = 0; s < capacity; ++s)
+            if (slots[s].used && !h_ctl[s].stop_req) { ++a; ia += desc[s].nq; }
+        long long il = 0;
+        for (auto& g : groups) il += g.n;
+        if (items_active) *items_active = ia;
+        if (items_listed) *items_listed = il;
+        return a;
+    }
+
+    double cell_updates() const {
+        double c = done_cell_updates;
+        for (int s = 0; s < capacity; ++s)
+            if (slots[s].used) c += (double)slots[s].cells * (double)h_ctl[s].iteration;
+        return c;
+    }
+};
+
+namespace {
+
+struct DevGuard {
+    int prev = -1;
+    explicit DevGuard(int d) { cudaGetDevice(&prev); if (prev != d) cudaSetDevice(d); }
+    ~DevGuard() { int c = -1; cudaGetDevice(&c); if (prev >= 0 && c != prev) cudaSetDevice(prev); }
+};
+
+size_t problem_bytes(const Layout& L) {
+    auto al = [](size_t b) { return (b + kAlign - 1) & ~(kAlign - 1); };
+    size_t b = 2 * al(sizeof(double) * NV * L.plane) + 2 * al(sizeof(float) * NV * L.plane);
+    b += al(sizeof(AxisGeo) * (L.nx + 2 * L.gx)) + al(sizeof(AxisGeo) * (L.ny + 2 * L.gy)) +
+         al(sizeof(AxisGeo) * (L.nz + 2 * L.gz));
+    return b;
+}
+
+}  // namespace
+
+extern "C" {
+
+ts_status ts_batch_create(int32_t device, size_t budget, ts_batch** out) {
+    if (!out) return fail(TS_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(TS_ERR_CUDA, "no CUDA device available");
+    if (device < 0 || device >= ndev) return fail(TS_ERR_INVALID, "device ordinal out of range");
+    if (budget < (1u << 20)) return fail(TS_ERR_INVALID, "memory budget below 1 MiB");
+    std::unique_ptr<ts_batch> b(new ts_batch());
+    b->device = device;
+    DevGuard g(device);
+    cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
+    TB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    TB_CUDA(b->arena.init(budget));
+    ts_status s = b->grow(64);
+    if (s != TS_OK) return s;
+    *out = b.release();
+    return TS_OK;
+}
+
+void ts_batch_destroy(ts_batch* b) { delete b; }
+
+size_t ts_batch_problem_bytes(const ts_config* cfg) {
+    if (!cfg) return 0;
+    std::string err;
+    if (validate_config(*cfg, err) != TS_OK) return 0;
+    if (cfg->n_dims > 2 || cfg->precision != TS_PRECISION_MIXED) return 0;
+    return problem_bytes(make_layout(*cfg));
+}
+
+ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, int32_t* id) {
+    if (!b || !cfg || !values || !id) return fail(TS_ERR_INVALID, "NULL argument");
+    if (cfg->precision != TS_PRECISION_MIXED) return fail(TS_ERR_UNSUPPORTED, "batches run the mixed-precision step");
+    if (cfg->n_dims > 2) return fail(TS_ERR_UNSUPPORTED, "batches hold 1D and 2D problems");
+    HostGrid grid;
+    std::string err;
+    ts_status s = build_grid(*cfg, grid, err);
+    if (s != TS_OK) return fail(s, err);
+    DevGuard g(b->device);
+    const Layout L = make_layout(*cfg);
+    const Phys ph = make_phys(*cfg);
+    if (b->arena.size - b->arena.used < problem_bytes(L))
+        return fail(TS_ERR_NO_MEMORY, "batch memory budget exhausted");
+    int slot = -1;
+    for (int k = 0; k < b->capacity; ++k)
+        if (!b->slots[k].used) { slot = k; break; }
+    if (slot < 0) {
+        slot = b->capacity;
+        if ((s = b->grow(b->capacity + 1)) != TS_OK) return s;
+    }
+    Slot& sl = b->slots[slot];
+    sl = Slot();
+    auto take = [&](size_t bytes, void** p) -> ts_status {
+        *p = b->arena.take(bytes);
+        if (!*p) return fail(TS_ERR_NO_MEMORY, "batch memory budget exhausted");
+        sl.mem.push_back(*p);
+        return TS_OK;
+    };
+    auto undo = [&]() { for (void* p : sl.mem) b->arena.give(p); sl = Slot(); };
+    ProbDesc& d = b->desc[slot];
+    std::memset(&d, 0, sizeof d);
+    if ((s = mixed_problem(*cfg, L, ph, grid, b->d_ctl + slot, take, d, err)) != TS_OK) {
+        undo();
+        return err.empty() ? s : fail(s, err);
+    }
+    for (int k = 0; k < 2; ++k) {
+        if ((s = take(sizeof(double) * NV * L.plane, (void**)&d.U[k])) != TS_OK) { undo(); return s; }
+        if ((s = take(sizeof(float) * NV * L.plane, (void**)&d.R[k])) != TS_OK) { undo(); return s; }
+    }
+    const Tune& t = b->tune[L.nd];
+    mixed_items(d, t.tx, L.nd == 1 ? 1 : t.ty, 0, (long long)b->sms);
+    // initial state: host -> staging -> U[0]; no pending residual
+    const size_t nvals = (size_t)L.cells() * NV;
+    if (b->stage_doubles < nvals) {
+        cudaFree(b->stage_buf);
+        b->stage_buf = nullptr;
+        b->stage_doubles = 0;
+        if (cudaMalloc(&b->stage_buf, nvals * sizeof(double)) != cudaSuccess) { undo(); return fail(TS_ERR_NO_MEMORY, "staging buffer"); }
+        b->stage_doubles = nvals;
+    }
+    TB_CUDA(cudaMemcpyAsync(b->stage_buf, values, nvals * sizeof(double), cudaMemcpyHostToDevice, b->stream));
+    k_b_scatter<<<(unsigned)((L.cells() + 255) / 256), 256, 0, b->stream>>>(b->stage_buf, L, d.U[0]);
+    TB_CUDA(cudaMemsetAsync(d.R[0], 0, sizeof(float) * NV * L.plane, b->stream));
+    Ctl& c = b->h_ctl[slot];
+    std::memset(&c, 0, sizeof c);
+    c.next_sol = cfg->save_solution_time;
+    c.next_slice = cfg->save_slice_time;
+    c.save_sol = cfg->save_solution_time;
+    c.save_slice = cfg->save_slice_time;
+    c.max_iteration = cfg->max_iteration;
+    c.max_time = cfg->max_time;
+    c.run_mode = 1;
+    TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &c, sizeof(Ctl), cudaMemcpyHostToDevice, b->stream));
+    TB_CUDA(cudaMemcpyAsync(b->d_desc + slot, &d, sizeof(ProbDesc), cudaMemcpyHostToDevice, b->stream));
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    sl.used = true;
+    sl.id = b->next_id++;
+    sl.cells = L.cells();
+    sl.cfg = *cfg;
+    b->id2slot[sl.id] = slot;
+    b->dirty = true;
+    *id = sl.id;
+    return TS_OK;
+}
+
+ts_status ts_batch_step(ts_batch* b, int32_t n) {
+    if (!b || n < 0) return fail(TS_ERR_INVALID, "bad argument");
+    DevGuard g(b->device);
+    ts_status s = b->launch(n);
+    if (s != TS_OK) return s;
+    return b->pull();
+}
+
+ts_status ts_batch_run(ts_batch* b, int32_t max_stages, int32_t* active) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    DevGuard g(b->device);
+    ts_status s = b->pull();
+    if (s != TS_OK) return s;
+    long long done = 0;
+    int chunk = 32;
+    for (;;) {
+        long long ia, il;
+        const int a = b->active(&ia, &il);
+        if (a == 0) break;
+        if (max_stages > 0 && done >= max_stages) break;
+        if (2 * ia < il) b->dirty = true;  // most listed items belong to finished problems
+        int n = chunk;
+        if (max_stages > 0) n = (int)std::min<long long>(n, max_stages - done);
+        if ((s = b->launch(n)) != TS_OK) return s;
+        if ((s = b->pull()) != TS_OK) return s;
+        done += n;
+        chunk = std::min(chunk * 2, 256);
+    }
+    if (active) *active = b->active(nullptr, nullptr);
+    return TS_OK;
+}
+
+ts_status ts_batch_finished(ts_batch* b, int32_t* ids, int32_t cap, int32_t* n) {
+    if (!b || !n) return fail(TS_ERR_INVALID, "NULL argument");
+    int k = 0;
+    for (int s = 0; s < b->capacity; ++s) {
+        Slot& sl = b->slots[s];
+        if (!sl.used || sl.collected || !b->h_ctl[s].stop_req) continue;
+        if (k < cap && ids) { ids[k] = sl.id; sl.collected = true; }
+        ++k;
+    }
+    *n = std::min(k, cap);
+    return TS_OK;
+}
+
+ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* info) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    auto it = b->id2slot.find(id);
+    if (it == b->id2slot.end()) return fail(TS_ERR_NOT_FOUND, "unknown problem id");
+    const int slot = it->second;
+    DevGuard g(b->device);
+    const Layout& L = b->desc[slot].L;
+    const unsigned blocks = (unsigned)((L.cells() + 255) / 256);
+    mixed_apply(b->d_desc, slot, L.cells(), b->stream);
+    if (values) {
+        const size_t nvals = (size_t)L.cells() * NV;
+        if (b->stage_doubles < nvals) {
+            cudaFree(b->stage_buf);
+            b->stage_buf = nullptr;
+            b->stage_doubles = 0;
+            TB_CUDA(cudaMalloc(&b->stage_buf, nvals * sizeof(double)));
+            b->stage_doubles = nvals;
+        }
+        k_b_gather<<<blocks, 256, 0, b->stream>>>(b->stage_buf, b->d_desc, slot);
+        TB_CUDA(cudaGetLastError());
+        TB_CUDA(cudaMemcpyAsync(values, b->stage_buf, nvals * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+    }
+    ts_status s = b->pull();
+    if (s != TS_OK) return s;
+    if (info) {
+        const Ctl& c = b->h_ctl[slot];
+        info->iteration = c.iteration;
+        info->health = c.health;
+        info->time = c.time;
+        info->dt = c.dt;
+        info->next_solution_time = c.next_sol;
+        info->next_slice_time = c.next_slice;
+        for (int v = 0; v < NV; ++v) info->residual[v] = 0.0;
+    }
+    return TS_OK;
+}
+
+ts_status ts_batch_remove(ts_batch* b, int32_t id) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    auto it = b->id2slot.find(id);
+    if (it == b->id2slot.end()) return fail(TS_ERR_NOT_FOUND, "unknown problem id");
+    DevGuard g(b->device);
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    const int slot = it->second;
+    Slot& sl = b->slots[slot];
+    b->done_cell_updates += (double)sl.cells * (double)b->h_ctl[slot].iteration;
+    for (void* p : sl.mem) b->arena.give(p);
+    sl = Slot();
+    std::memset(&b->h_ctl[slot], 0, sizeof(Ctl));
+    b->h_ctl[slot].stop_req = 1;
+    TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &b->h_ctl[slot], sizeof(Ctl), cudaMemcpyHostToDevice, b->stream));
+    b->id2slot.erase(it);
+    b->dirty = true;
+    return TS_OK;
+}
+
+ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int32_t ctas) {
+    if (!b || nd < 1 || nd > 2) return fail(TS_ERR_INVALID, "bad argument");
+    if (nd == 1) ty = 1;
+    size_t bytes;
+    int per;
+    if (!mixed_tile_info(nd, tx, ty, TS_RS_ROE_PIKE, &bytes, &per, true) || per < 1)
+        return fail(TS_ERR_UNSUPPORTED, "no compiled tile of that shape");
+    DevGuard g(b->device);
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    b->tune[nd] = Tune{tx, ty, ctas};
+    for (int s = 0; s < b->capacity; ++s) {
+        if (!b->slots[s].used || b->desc[s].L.nd != nd) continue;
+        mixed_items(b->desc[s], tx, ty, 0, (long long)b->sms);
+        TB_CUDA(cudaMemcpyAsync(b->d_desc + s, &b->desc[s], sizeof(ProbDesc), cudaMemcpyHostToDevice, b->stream));
+    }
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    b->dirty = true;
+    return TS_OK;
+}
+
+ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx_out, int32_t* ty_out, int32_t* ctas_out) {
+    if (!b || stages < 1) return fail(TS_ERR_INVALID, "bad argument");
+    DevGuard g(b->device);
+    ts_status s = b->pull();
+    if (s != TS_OK) return s;
+    // dominant dimension by cells
+    long long cells[3] = {0, 0, 0};
+    for (int k = 0; k < b->capacity; ++k)
+        if (b->slots[k].used) cells[b->desc[k].L.nd] += b->slots[k].cells;
+    const int nd = cells[2] > cells[1] ? 2 : 1;
+    if (cells[nd] == 0) return fail(TS_ERR_INVALID, "empty batch");
+    // snapshot: the arena up to its high-water mark and the control words
+    char* snap = nullptr;
+    Ctl* snap_ctl = nullptr;
+    const size_t hb = b->arena.high;
+    TB_CUDA(cudaMalloc(&snap, std::max<size_t>(hb, 1)));
+    TB_CUDA(cudaMalloc(&snap_ctl, sizeof(Ctl) * b->capacity));
+    auto restore = [&]() -> ts_status {
+        TB_CUDA(cudaMemcpyAsync(b->arena.base, snap, hb, cudaMemcpyDeviceToDevice, b->stream));
+        TB_CUDA(cudaMemcpyAsync(b->d_ctl, snap_ctl, sizeof(Ctl) * b->capacity, cudaMemcpyDeviceToDevice, b->stream));
+        TB_CUDA(cudaStreamSynchronize(b->stream));
+        return b->pull();
+    };
+    TB_CUDA(cudaMemcpyAsync(snap, b->arena.base, hb, cudaMemcpyDeviceToDevice, b->stream));
+    TB_CUDA(cudaMemcpyAsync(snap_ctl, b->d_ctl, sizeof(Ctl) * b->capacity, cudaMemcpyDeviceToDevice, b->stream));
+    const std::vector<std::pair<int, int>> tiles =
+        nd == 1 ? std::vector<std::pair<int, int>>{{256, 1}, {128, 1}} : std::vector<std::pair<int, int>>{{32, 8}, {16, 16}};
+    const Tune saved = b->tune[nd];
+    const long long st0 = b->stages, la0 = b->launches;
+    Tune best = saved;
+    float best_ms = 1e30f;
+    cudaEvent_t e0, e1;
+    cudaEventCreate(&e0);
+    cudaEventCreate(&e1);
+    for (auto tl : tiles) {
+        size_t bytes;
+        int per;
+        if (!mixed_tile_info(nd, tl.first, tl.second, TS_RS_ROE_PIKE, &bytes, &per, true) || per < 1) continue;
+        for (int ctas = per; ctas >= 1; ctas = (ctas > 1 ? ctas / 2 : 0)) {
+            if ((s = ts_batch_set_tile(b, nd, tl.first, tl.second, ctas)) != TS_OK) break;
+            if ((s = b->launch(1)) != TS_OK) break;  // rebuild + warm-up
+            if ((s = restore()) != TS_OK) break;
+            cudaEventRecord(e0, b->stream);
+            if ((s = b->launch(stages)) != TS_OK) break;
+            cudaEventRecord(e1, b->stream);
+            cudaEventSynchronize(e1);
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, e0, e1);
+            if (ms < best_ms) { best_ms = ms; best = Tune{tl.first, tl.second, ctas}; }
+            if ((s = restore()) != TS_OK) break;
+            if (ctas == 1) break;
+        }
+        if (s != TS_OK) break;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    cudaFree(snap);
+    cudaFree(snap_ctl);
+    b->stages = st0;
+    b->launches = la0;
+    if (s != TS_OK) return s;
+    if ((s = ts_batch_set_tile(b, nd, best.tx, best.ty, best.ctas)) != TS_OK) return s;
+    if (tx_out) *tx_out = best.tx;
+    if (ty_out) *ty_out = best.ty;
+    if (ctas_out) *ctas_out = best.ctas;
+    return TS_OK;
+}
+
+ts_status ts_batch_stats(ts_batch* b, double* cell_updates, int64_t* stages, int64_t* launches) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    if (cell_updates) *cell_updates = b->cell_updates();
+    if (stages) *stages = b->stages;
+    if (launches) *launches = b->launches;
+    return TS_OK;
+}
+
+}  // extern "C"

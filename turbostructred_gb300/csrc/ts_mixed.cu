@@ -1,5 +1,5 @@
 // Mixed-precision explicit FVM step on GB300: one fused, persistent kernel
-// per RK stage.
+// per RK stage, over a work list of one or many problems.
 //
 // Precision split: reconstruction, EOS and Riemann flux in FP32; the
 // conserved state, the stage accumulation U += dt R / V and the dt reduction
@@ -14,20 +14,23 @@
 // pass per step: 40 B FP64 read + 20 B FP32 read + 40 B + 20 B written per
 // cell-update.  A final apply pass materialises the state for the host.
 //
-// Tiling.  Each CTA owns an x-y tile of TX x TY cells (compile-time, one
-// thread per tile cell) and marches along z (2.5D blocking), keeping a
-// 3-plane ring of the FP32 working state with a 2-cell halo, a 2-plane ring
-// of limited half-slopes with a 1-cell halo and the face fluxes in shared
-// memory.  Every thread has fixed roles: two working-state positions of the
-// halo box (loads for the next plane are issued into registers as soon as the
-// current plane is stored, so their latency hides behind the plane's
-// compute), up to two reconstruction positions, the x face left of its cell,
-// the y face below and the z face above (the tile's far faces go to the first
-// TX + TY threads), and its cell's residual.
-//
-// Schedule.  Work is (column, z-chunk) pairs indexed z-chunk-major and dealt
-// round-robin to the persistent CTAs, so CTAs running at the same time sweep
-// neighbouring columns at the same z and share halo rows through L2.
+// Work items.  A problem is cut into tile columns of TX x TY cells (x-y,
+// compile-time, one thread per tile cell) and, in 3D, z chunks; one item is
+// one (problem, column, chunk).  A CTA marches z through its item (2.5D
+// blocking), keeping a 3-plane ring of the FP32 working state with a 2-cell
+// halo, a 2-plane ring of limited half-slopes with a 1-cell halo and the
+// face fluxes in shared memory.  Every thread has fixed roles: up to two
+// working-state positions of the halo box (the next plane's loads are issued
+// into registers as soon as the current plane is stored, so their latency
+// hides behind the plane's compute), up to two reconstruction positions, the
+// x face left of its cell, the y face below, the z face above (the tile's far
+// faces go to the first TX + TY threads), and its cell's residual.  Items are
+// indexed z-chunk-major and dealt round-robin to the persistent CTAs, so CTAs
+// running at the same time sweep neighbouring columns at the same z and share
+// halo rows through L2.  Each problem has its own control word: the CTA that
+// completes a problem's last item turns its CFL maximum into that problem's
+// dt, so many problems of different sizes advance with their own time steps
+// in one launch.
 //
 // Ghost cells are virtual: a load outside the domain wraps on periodic axes
 // and mirrors plus applies the boundary condition (BCGeneral.h:186-268)
@@ -53,21 +56,6 @@ namespace ts {
 namespace {
 
 constexpr int HB = 2;  // halo of the working-state box
-
-struct MixArgs {
-    Layout L;
-    double* U[2];
-    float* R[2];
-    const AxisGeo* geo[3];
-    int goff[3];  // index offset into geo per axis (ghost width or 0)
-    Ctl* ctl;
-    MixPhys mp;
-    int ncx;      // tile columns along x
-    int ncol;     // tile columns
-    int ch;       // planes per z chunk
-    int nq;       // column-chunks = ncol * number of chunks
-};
-
 
 // ---------------------------------------------------------------------------
 // FP64 <-> FP32 on the integer pipe
@@ -124,21 +112,25 @@ __device__ __forceinline__ void bc32(const MixPhys& p, int side, int A, float w[
     }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 Riemann solvers along axis A.  States carry the shifted energy
-// E' = E - einf, so p = (g-1)(E' - rho |u|^2 / 2) for both equations of state
-// without cancellation; E = E' + einf where the total energy enters.
-// ---------------------------------------------------------------------------
+
 __device__ __forceinline__ float harten32(float z, float e) {
     z = fabsf(z);
     return (z < e) ? ((z * z) / e + e) * 0.5f : z;
 }
 
+__device__ __forceinline__ float pick3(int a, float x, float y, float z) { return a == 0 ? x : (a == 1 ? y : z); }
+
+// ---------------------------------------------------------------------------
+// FP32 Riemann solvers along axis A (a runtime argument: one copy of the
+// solver serves all three face directions).  States carry the shifted energy
+// E' = E - einf, so p = (g-1)(E' - rho |u|^2 / 2) for both equations of state
+// without cancellation; E = E' + einf where the total energy enters.
+// ---------------------------------------------------------------------------
+
 // Roe-Pike flux (RoeSolverPerfectGasEOS.h:74-160) in the equivalent form
 // 1/2 [F(UL) + F(UR) + |A|(UL - UR)], |A| dU = a1 dU + Ac Qa + Bc Qb with
 // Qa = (0, e_A, un), Qb = (1, u, H), Ac = Ea dR + Eb dD, Bc = Ea dD + Eb dR / c^2.
-template <int A>
-__device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
+__device__ __forceinline__ float roe32(const MixPhys& p, int A, const float UL[NV], const float UR[NV], float F[NV]) {
     const float gm1 = p.gm1;
     const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
     const float ulx = UL[1] * rl, uly = UL[2] * rl, ulz = UL[3] * rl;
@@ -155,7 +147,7 @@ __device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], con
     const float c2 = gm1 * (h - 0.5f * q2);
     const float ic = rsqrtf(c2);
     const float c = c2 * ic;
-    const float un = A == 0 ? ux : (A == 1 ? uy : uz);
+    const float un = pick3(A, ux, uy, uz);
     const float lam = fabsf(un) + c;
     float a1 = fabsf(un), a3 = fabsf(un + c), a4 = fabsf(un - c);
     if (p.eps > 0.0f) {
@@ -166,38 +158,37 @@ __device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], con
     const float Eb = (a3 + a4) * 0.5f - a1;
     const float dr = UL[0] - UR[0], dmx = UL[1] - UR[1], dmy = UL[2] - UR[2], dmz = UL[3] - UR[3];
     const float de = UL[4] - UR[4];
-    const float dm_n = A == 0 ? dmx : (A == 1 ? dmy : dmz);
     const float dR = 0.5f * gm1 * q2 * dr - gm1 * (ux * dmx + uy * dmy + uz * dmz - de);
-    const float dD = dm_n - dr * un;
+    const float dD = pick3(A, dmx, dmy, dmz) - dr * un;
     const float Ac = Ea * dR + Eb * dD;
     const float Bc = Ea * dD + Eb * dR * (ic * ic);
-    const float unl = A == 0 ? ulx : (A == 1 ? uly : ulz);
-    const float unr = A == 0 ? urx : (A == 1 ? ury : urz);
+    const float unl = pick3(A, ulx, uly, ulz), unr = pick3(A, urx, ury, urz);
+    const float pn = pl + pr + Ac;
     F[0] = 0.5f * (UL[0] * unl + UR[0] * unr + a1 * dr + Bc);
-    F[1] = 0.5f * (UL[1] * unl + UR[1] * unr + (A == 0 ? pl + pr + Ac : 0.0f) + a1 * dmx + Bc * ux);
-    F[2] = 0.5f * (UL[2] * unl + UR[2] * unr + (A == 1 ? pl + pr + Ac : 0.0f) + a1 * dmy + Bc * uy);
-    F[3] = 0.5f * (UL[3] * unl + UR[3] * unr + (A == 2 ? pl + pr + Ac : 0.0f) + a1 * dmz + Bc * uz);
+    F[1] = 0.5f * (UL[1] * unl + UR[1] * unr + (A == 0 ? pn : 0.0f) + a1 * dmx + Bc * ux);
+    F[2] = 0.5f * (UL[2] * unl + UR[2] * unr + (A == 1 ? pn : 0.0f) + a1 * dmy + Bc * uy);
+    F[3] = 0.5f * (UL[3] * unl + UR[3] * unr + (A == 2 ? pn : 0.0f) + a1 * dmz + Bc * uz);
     F[4] = 0.5f * (el * unl + er * unr + a1 * de + Ac * un + Bc * h);
     return lam;
 }
 
 // HLLC (Toro ch. 10.4), Einfeldt-type speeds from Roe averages.
-template <int A>
-__device__ __forceinline__ float hllc32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
+__device__ __forceinline__ float hllc32(const MixPhys& p, int A, const float UL[NV], const float UR[NV],
+                                        float F[NV]) {
     const float g = p.gamma, gm1 = p.gm1;
     const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
-    const float vl[3] = {UL[1] * rl, UL[2] * rl, UL[3] * rl};
-    const float vr[3] = {UR[1] * rr, UR[2] * rr, UR[3] * rr};
-    const float pl = gm1 * (UL[4] - 0.5f * UL[0] * (vl[0] * vl[0] + vl[1] * vl[1] + vl[2] * vl[2]));
-    const float pr = gm1 * (UR[4] - 0.5f * UR[0] * (vr[0] * vr[0] + vr[1] * vr[1] + vr[2] * vr[2]));
+    const float vlx = UL[1] * rl, vly = UL[2] * rl, vlz = UL[3] * rl;
+    const float vrx = UR[1] * rr, vry = UR[2] * rr, vrz = UR[3] * rr;
+    const float pl = gm1 * (UL[4] - 0.5f * UL[0] * (vlx * vlx + vly * vly + vlz * vlz));
+    const float pr = gm1 * (UR[4] - 0.5f * UR[0] * (vrx * vrx + vry * vry + vrz * vrz));
     const float El = UL[4] + p.einf, Er = UR[4] + p.einf;
     const float cl = sqrtf(g * (pl + p.pinf) * rl), cr = sqrtf(g * (pr + p.pinf) * rr);
     const float sl = UL[0] * rsqrtf(UL[0]), sr = UR[0] * rsqrtf(UR[0]);
     const float inv = 1.0f / (sl + sr);
     const float wl = sl * inv, wr = sr * inv;
-    const float ul = vl[A], ur = vr[A];
+    const float ul = pick3(A, vlx, vly, vlz), ur = pick3(A, vrx, vry, vrz);
     const float ut = wl * ul + wr * ur;
-    const float vtx = wl * vl[0] + wr * vr[0], vty = wl * vl[1] + wr * vr[1], vtz = wl * vl[2] + wr * vr[2];
+    const float vtx = wl * vlx + wr * vrx, vty = wl * vly + wr * vry, vtz = wl * vlz + wr * vrz;
     const float ht = wl * ((El + pl) * rl) + wr * ((Er + pr) * rr);
     const float ct = sqrtf(gm1 * (ht - 0.5f * (vtx * vtx + vty * vty + vtz * vtz)));
     const float SL = fminf(ul - cl, ut - ct);
@@ -208,39 +199,30 @@ __device__ __forceinline__ float hllc32(const MixPhys& p, const float UL[NV], co
     const bool supl = SL >= 0.0f, supr = SR <= 0.0f;
     const bool left = supl || (!supr && ss >= 0.0f);
     const float* U = left ? UL : UR;
-    const float* v = left ? vl : vr;
+    const float vx = left ? vlx : vrx, vy = left ? vly : vry, vz = left ? vlz : vrz;
     const float uk = left ? ul : ur, pk = left ? pl : pr, Ek = left ? El : Er, rk = left ? rl : rr;
     const float Sk = left ? SL : SR, mk = left ? ml : mr;
-    // physical flux of the upwind side
     F[0] = U[0] * uk;
     F[1] = U[1] * uk + (A == 0 ? pk : 0.0f);
     F[2] = U[2] * uk + (A == 1 ? pk : 0.0f);
     F[3] = U[3] * uk + (A == 2 ? pk : 0.0f);
     F[4] = (Ek + pk) * uk;
-    const bool star = !supl && !supr;
-    if (star) {
+    if (!supl && !supr) {
         const float coef = mk / (Sk - ss);
-        float us[NV];
-        us[0] = coef;
-        us[1] = coef * (A == 0 ? ss : v[0]);
-        us[2] = coef * (A == 1 ? ss : v[1]);
-        us[3] = coef * (A == 2 ? ss : v[2]);
-        us[4] = coef * (Ek * rk + (ss - uk) * (ss + pk / mk));
-        F[0] += Sk * (us[0] - U[0]);
-        F[1] += Sk * (us[1] - U[1]);
-        F[2] += Sk * (us[2] - U[2]);
-        F[3] += Sk * (us[3] - U[3]);
-        F[4] += Sk * (us[4] - Ek);
+        F[0] += Sk * (coef - U[0]);
+        F[1] += Sk * (coef * (A == 0 ? ss : vx) - U[1]);
+        F[2] += Sk * (coef * (A == 1 ? ss : vy) - U[2]);
+        F[3] += Sk * (coef * (A == 2 ? ss : vz) - U[3]);
+        F[4] += Sk * (coef * (Ek * rk + (ss - uk) * (ss + pk / mk)) - Ek);
     }
     return fmaxf(fabsf(SL), fabsf(SR));
 }
 
-template <int SOLVER, int A>
-__device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
-    if (SOLVER == TS_RS_HLLC) return hllc32<A>(p, UL, UR, F);
-    return roe32<A>(p, UL, UR, F);
+template <int SOLVER>
+__device__ __forceinline__ float flux32(const MixPhys& p, int A, const float UL[NV], const float UR[NV], float F[NV]) {
+    if (SOLVER == TS_RS_HLLC) return hllc32(p, A, UL, UR, F);
+    return roe32(p, A, UL, UR, F);
 }
-
 
 // ---------------------------------------------------------------------------
 // Compile-time tile geometry and shared-memory layout (floats)
@@ -299,8 +281,8 @@ struct Prefetch {
 };
 
 template <class T>
-__device__ __forceinline__ void setup_box(const MixArgs& a, int i0, int j0, BoxPos (&bp)[T::NA]) {
-    const Layout& L = a.L;
+__device__ __forceinline__ void setup_box(const ProbDesc& d, int i0, int j0, BoxPos (&bp)[T::NA]) {
+    const Layout& L = d.L;
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
         const int t = threadIdx.x + k * T::NT;
@@ -315,31 +297,31 @@ __device__ __forceinline__ void setup_box(const MixArgs& a, int i0, int j0, BoxP
         if (gi >= L.nx + HB) continue;
         if (T::ND >= 2 && gj >= L.ny + HB) continue;
         int si, sj = 0;
-        resolve(gi, L.nx, a.mp.periodic[0], 0, si, bp[k].xs);
+        resolve(gi, L.nx, d.mp.periodic[0], 0, si, bp[k].xs);
         bp[k].ys = -1;
-        if (T::ND >= 2) resolve(gj, L.ny, a.mp.periodic[1], 2, sj, bp[k].ys);
+        if (T::ND >= 2) resolve(gj, L.ny, d.mp.periodic[1], 2, sj, bp[k].ys);
         bp[k].off = (sj + L.gy) * L.px + (si + L.gx);
         bp[k].box = t;
-        bp[k].cfxy = __ldg(&a.geo[0][si + a.goff[0]].ih) * __ldg(&a.geo[1][sj + a.goff[1]].ih);
+        bp[k].cfxy = __ldg(&d.geo[0][si + d.goff[0]].ih) * __ldg(&d.geo[1][sj + d.goff[1]].ih);
         bp[k].own = dx == 0 && dy == 0 && gi < L.nx && gj < L.ny;
     }
 }
 
-__device__ __forceinline__ int plane_of(const MixArgs& a, int p, int& zs) {
+__device__ __forceinline__ int plane_of(const ProbDesc& d, int p, int& zs) {
     int sk = 0;
     zs = -1;
-    resolve(p, a.L.nz, a.mp.periodic[2], 4, sk, zs);
+    resolve(p, d.L.nz, d.mp.periodic[2], 4, sk, zs);
     return sk;
 }
 
 // Issue the loads of plane p (FP64 state and FP32 pending residual) into registers.
 template <class T>
-__device__ __forceinline__ void issue(const MixArgs& a, const double* __restrict__ Uin,
+__device__ __forceinline__ void issue(const ProbDesc& d, const double* __restrict__ Uin,
                                       const float* __restrict__ Rin, int p, const BoxPos (&bp)[T::NA],
                                       Prefetch (&pf)[T::NA]) {
-    const Layout& L = a.L;
+    const Layout& L = d.L;
     int zs;
-    const int sk = T::ND == 3 ? plane_of(a, p, zs) : 0;
+    const int sk = T::ND == 3 ? plane_of(d, p, zs) : 0;
     const int zoff = (sk + L.gz) * L.px * L.ey;
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
@@ -355,15 +337,15 @@ __device__ __forceinline__ void issue(const MixArgs& a, const double* __restrict
 // Turn the prefetched plane p into the FP32 working copy in shared memory and
 // write U^{n+1} = U^n + dt R^n / V for the owned cells of planes [z0, z1).
 template <class T>
-__device__ __forceinline__ void store(const MixArgs& a, float* sm, double* __restrict__ Uout, int p, int z0, int z1,
+__device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __restrict__ Uout, int p, int z0, int z1,
                                       float dtf, const BoxPos (&bp)[T::NA], const Prefetch (&pf)[T::NA],
                                       unsigned int& health) {
-    const Layout& L = a.L;
-    const MixPhys& mp = a.mp;
+    const Layout& L = d.L;
+    const MixPhys& mp = d.mp;
     int zs = -1;
-    const int sk = T::ND == 3 ? plane_of(a, p, zs) : 0;
+    const int sk = T::ND == 3 ? plane_of(d, p, zs) : 0;
     const int zoff = (sk + L.gz) * L.px * L.ey;
-    const float cfz = dtf * __ldg(&a.geo[2][sk + a.goff[2]].ih);
+    const float cfz = dtf * __ldg(&d.geo[2][sk + d.goff[2]].ih);
     const int slot = T::ND == 3 ? wslot(p) : 0;
     const bool own_plane = p >= z0 && p < z1;
 #pragma unroll
@@ -399,9 +381,9 @@ __device__ __forceinline__ void store(const MixArgs& a, float* sm, double* __res
 // Limited half-slopes of plane p on the tile and its 1-cell ring (corners
 // excluded); ring cells outside a non-periodic boundary are not needed.
 template <class T>
-__device__ __forceinline__ void recon(const MixArgs& a, float* sm, int i0, int j0, int p) {
-    const Layout& L = a.L;
-    const MixPhys& mp = a.mp;
+__device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int j0, int p) {
+    const Layout& L = d.L;
+    const MixPhys& mp = d.mp;
     int sk = 0, zs;
     if (T::ND == 3) {
         if ((p < 0 || p >= L.nz) && !mp.periodic[2]) return;
@@ -411,7 +393,7 @@ __device__ __forceinline__ void recon(const MixArgs& a, float* sm, int i0, int j
     const int wd = T::ND == 3 ? wslot(p - 1) : 0, wu = T::ND == 3 ? wslot(p + 1) : 0;
     const int ds = T::ND == 3 ? dslot(p) : 0;
     AxisGeo gz;
-    if (T::ND == 3) gz = a.geo[2][sk + a.goff[2]];
+    if (T::ND == 3) gz = d.geo[2][sk + d.goff[2]];
 #pragma unroll
     for (int k = 0; k < T::NB; ++k) {
         const int t = threadIdx.x + k * T::NT;
@@ -428,8 +410,8 @@ __device__ __forceinline__ void recon(const MixArgs& a, float* sm, int i0, int j
         resolve(gi, L.nx, 1, 0, si, xs);
         if (T::ND >= 2) resolve(gj, L.ny, 1, 2, sj, ys);
         AxisGeo g[3];
-        g[0] = a.geo[0][si + a.goff[0]];
-        if (T::ND >= 2) g[1] = a.geo[1][sj + a.goff[1]];
+        g[0] = d.geo[0][si + d.goff[0]];
+        if (T::ND >= 2) g[1] = d.geo[1][sj + d.goff[1]];
         if (T::ND == 3) g[2] = gz;
         const int box = (T::ND >= 2 ? (ry + 1) * T::BX : 0) + rx + 1;
         float eps2 = 0.0f;
@@ -502,93 +484,83 @@ __device__ __forceinline__ void recon(const MixArgs& a, float* sm, int i0, int j
     }
 }
 
-template <int SOLVER, int A>
-__device__ __forceinline__ float face_flux(const MixPhys& mp, bool bc_lo, bool bc_hi, float UL[NV], float UR[NV],
-                                           float F[NV]) {
-    if (bc_lo) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) UL[v] = UR[v];
-        bc32(mp, 2 * A, A, UL);
-    } else if (bc_hi) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) UR[v] = UL[v];
-        bc32(mp, 2 * A + 1, A, UR);
-    }
-    return flux32<SOLVER, A>(mp, UL, UR, F);
-}
-
-// x face fx (left of tile column fx) in tile row fy.
+// The faces of plane z this thread computes: k = 0 x face left of its cell,
+// 1 y face below, 2 z face above (between z and z+1), 3 one far face of the
+// tile (x face TX for threads < TY, y face TY for the next TX threads).
 template <class T, int SOLVER>
-__device__ __forceinline__ void xface(const MixArgs& a, float* sm, int i0, int j0, int ws, int ds, bool pwc, int fx,
-                                      int fy) {
-    const int gi = i0 + fx, gj = j0 + fy;
-    if (gi > a.L.nx || gj >= a.L.ny) return;
-    const int bl = (T::ND >= 2 ? (fy + HB) * T::BX : 0) + fx + 1;
-    const int rl = (T::ND >= 2 ? (fy + 1) * T::RX : 0) + fx;
-    float UL[NV], UR[NV], F[NV];
+__device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int j0, int z, bool pwc, bool do_xy,
+                                       bool do_z) {
+    const Layout& L = d.L;
+    const int tid = threadIdx.x;
+    const int tx = tid % T::TX, ty = tid / T::TX;
+    const int ws = T::ND == 3 ? wslot(z) : 0, ds = T::ND == 3 ? dslot(z) : 0;
+#pragma unroll 1
+    for (int k = 0; k < 4; ++k) {
+        int axis, fx, fy;
+        if (k == 0) { if (!do_xy) continue; axis = 0; fx = tx; fy = ty; }
+        else if (k == 1) { if (!do_xy || T::ND < 2) continue; axis = 1; fx = tx; fy = ty; }
+        else if (k == 2) { if (!do_z || T::ND < 3) continue; axis = 2; fx = tx; fy = ty; }
+        else {
+            if (!do_xy) continue;
+            if (tid < T::TY) { axis = 0; fx = T::TX; fy = tid; }
+            else if (T::ND >= 2 && tid < T::TY + T::TX) { axis = 1; fx = tid - T::TY; fy = T::TY; }
+            else continue;
+        }
+        const int gi = i0 + fx, gj = j0 + fy;
+        int bl, br, rl, rr, wl = ws, wr = ws, dl = ds, dr = ds, g, n, per, out;
+        if (axis == 0) {
+            if (gi > L.nx || gj >= L.ny) continue;
+            bl = (T::ND >= 2 ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
+            rl = (T::ND >= 2 ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
+            g = gi; n = L.nx; per = d.mp.periodic[0];
+            out = T::fx(0, fy, fx);
+        } else if (axis == 1) {
+            if (gi >= L.nx || gj > L.ny) continue;
+            bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
+            rl = fy * T::RX + fx + 1; rr = rl + T::RX;
+            g = gj; n = L.ny; per = d.mp.periodic[1];
+            out = T::fy(0, fy, fx);
+        } else {
+            if (gi >= L.nx || gj >= L.ny) continue;
+            bl = br = (fy + HB) * T::BX + fx + HB;
+            rl = rr = (fy + 1) * T::RX + fx + 1;
+            wr = wslot(z + 1); dr = dslot(z + 1);
+            g = z + 1; n = L.nz; per = d.mp.periodic[2];
+            out = T::fz(dslot(z + 1), 0, fy, fx);
+        }
+        float UL[NV], UR[NV], F[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        UL[v] = sm[T::w(ws, v, bl)] + (pwc ? 0.0f : sm[T::d(ds, 0, v, rl)]);
-        UR[v] = sm[T::w(ws, v, bl + 1)] - (pwc ? 0.0f : sm[T::d(ds, 0, v, rl + 1)]);
+        for (int v = 0; v < NV; ++v) {
+            UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, axis, v, rl)]);
+            UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, axis, v, rr)]);
+        }
+        if (g == 0 && !per) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) UL[v] = UR[v];
+            bc32(d.mp, 2 * axis, axis, UL);
+        } else if (g == n && !per) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) UR[v] = UL[v];
+            bc32(d.mp, 2 * axis + 1, axis, UR);
+        }
+        const float lam = flux32<SOLVER>(d.mp, axis, UL, UR, F);
+        // the v-stride of each flux array is its plane of faces
+        const int vs = axis == 0 ? T::TY * (T::TX + 1) : (axis == 1 ? (T::TY + 1) * T::TX : T::TY * T::TX);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sm[out + v * vs] = F[v];
+        sm[out + NV * vs] = lam;
     }
-    const bool per = a.mp.periodic[0];
-    const float lam = face_flux<SOLVER, 0>(a.mp, gi == 0 && !per, gi == a.L.nx && !per, UL, UR, F);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) sm[T::fx(v, fy, fx)] = F[v];
-    sm[T::fx(5, fy, fx)] = lam;
-}
-
-template <class T, int SOLVER>
-__device__ __forceinline__ void yface(const MixArgs& a, float* sm, int i0, int j0, int ws, int ds, bool pwc, int fx,
-                                      int fy) {
-    const int gi = i0 + fx, gj = j0 + fy;
-    if (gi >= a.L.nx || gj > a.L.ny) return;
-    const int bl = (fy + 1) * T::BX + fx + HB;
-    const int rl = fy * T::RX + fx + 1;
-    float UL[NV], UR[NV], F[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        UL[v] = sm[T::w(ws, v, bl)] + (pwc ? 0.0f : sm[T::d(ds, 1, v, rl)]);
-        UR[v] = sm[T::w(ws, v, bl + T::BX)] - (pwc ? 0.0f : sm[T::d(ds, 1, v, rl + T::RX)]);
-    }
-    const bool per = a.mp.periodic[1];
-    const float lam = face_flux<SOLVER, 1>(a.mp, gj == 0 && !per, gj == a.L.ny && !per, UL, UR, F);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) sm[T::fy(v, fy, fx)] = F[v];
-    sm[T::fy(5, fy, fx)] = lam;
-}
-
-// z face between planes z and z+1 above tile cell (fx, fy).
-template <class T, int SOLVER>
-__device__ __forceinline__ void zface(const MixArgs& a, float* sm, int i0, int j0, int z, bool pwc, int fx, int fy) {
-    if (i0 + fx >= a.L.nx || j0 + fy >= a.L.ny) return;
-    const int ws = wslot(z), wu = wslot(z + 1), ds = dslot(z), du = dslot(z + 1);
-    const int b = (fy + HB) * T::BX + fx + HB;
-    const int r = (fy + 1) * T::RX + fx + 1;
-    float UL[NV], UR[NV], F[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        UL[v] = sm[T::w(ws, v, b)] + (pwc ? 0.0f : sm[T::d(ds, 2, v, r)]);
-        UR[v] = sm[T::w(wu, v, b)] - (pwc ? 0.0f : sm[T::d(du, 2, v, r)]);
-    }
-    const int gk = z + 1;
-    const bool per = a.mp.periodic[2];
-    const float lam = face_flux<SOLVER, 2>(a.mp, gk == 0 && !per, gk == a.L.nz && !per, UL, UR, F);
-    const int fs = dslot(z + 1);
-#pragma unroll
-    for (int v = 0; v < NV; ++v) sm[T::fz(fs, v, fy, fx)] = F[v];
-    sm[T::fz(fs, 5, fy, fx)] = lam;
 }
 
 // Residual and spectral radius of the owned cell of this thread in plane z.
 template <class T>
-__device__ __forceinline__ void residual(const MixArgs& a, const float* sm, float* __restrict__ Rout, int i0, int j0,
+__device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
                                          int z, float& srmax) {
-    const Layout& L = a.L;
+    const Layout& L = d.L;
     const int tx = threadIdx.x % T::TX, ty = threadIdx.x / T::TX;
     const int gi = i0 + tx, gj = j0 + ty;
     if (gi >= L.nx || gj >= L.ny) return;
-    const AxisGeo gx = a.geo[0][gi + a.goff[0]], gy = a.geo[1][gj + a.goff[1]], gz = a.geo[2][z + a.goff[2]];
+    const AxisGeo gx = d.geo[0][gi + d.goff[0]], gy = d.geo[1][gj + d.goff[1]], gz = d.geo[2][z + d.goff[2]];
     const float fsx = gy.h * gz.h, fsy = gx.h * gz.h, fsz = gx.h * gy.h;
     const float iv = gx.ih * gy.ih * gz.ih;
     float R[NV];
@@ -596,13 +568,13 @@ __device__ __forceinline__ void residual(const MixArgs& a, const float* sm, floa
 #pragma unroll
     for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * fsx;
     float sr = fsx * (lxl + lxr);
-    if (gi == L.nx - 1) srmax = fmaxf(srmax, fsx * lxr * a.geo[0][L.nx + a.goff[0]].ih * gy.ih * gz.ih);
+    if (gi == L.nx - 1) srmax = fmaxf(srmax, fsx * lxr * d.geo[0][L.nx + d.goff[0]].ih * gy.ih * gz.ih);
     if (T::ND >= 2) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * fsy;
         const float lyr = sm[T::fy(5, ty + 1, tx)];
         sr += fsy * (sm[T::fy(5, ty, tx)] + lyr);
-        if (gj == L.ny - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * a.geo[1][L.ny + a.goff[1]].ih * gz.ih);
+        if (gj == L.ny - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * d.geo[1][L.ny + d.goff[1]].ih * gz.ih);
     }
     if (T::ND == 3) {
         const int dn = dslot(z), up = dslot(z + 1);
@@ -610,7 +582,7 @@ __device__ __forceinline__ void residual(const MixArgs& a, const float* sm, floa
         for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * fsz;
         const float lzr = sm[T::fz(up, 5, ty, tx)];
         sr += fsz * (sm[T::fz(dn, 5, ty, tx)] + lzr);
-        if (z == L.nz - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * a.geo[2][L.nz + a.goff[2]].ih);
+        if (z == L.nz - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * d.geo[2][L.nz + d.goff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
     const long long c = L.at(gi, gj, z);
@@ -618,122 +590,12 @@ __device__ __forceinline__ void residual(const MixArgs& a, const float* sm, floa
     for (int v = 0; v < NV; ++v) __stcg(Rout + v * L.plane + c, R[v]);
 }
 
-// ---------------------------------------------------------------------------
-// The fused step kernel
-// ---------------------------------------------------------------------------
-template <class T, int SOLVER>
-__global__ void __launch_bounds__(T::NT) k_mix_step(MixArgs a) {
-    Ctl* ctl = a.ctl;
-    if (ctl->stop_req) return;
-    extern __shared__ float sm[];
-    const Layout& L = a.L;
-    const int par = ctl->parity;
-    const double* __restrict__ Uin = a.U[par];
-    double* __restrict__ Uout = a.U[par ^ 1];
-    const float* __restrict__ Rin = a.R[par];
-    float* __restrict__ Rout = a.R[par ^ 1];
-    const float dtf = f64_to_f32(ctl->dt_apply);
-    const bool pwc = a.mp.recon == TS_RECON_PIECEWISE_CONSTANT;
-    const int tx = threadIdx.x % T::TX, ty = threadIdx.x / T::TX;
-    float srmax = 0.0f;
-    unsigned int health = 0;
-    BoxPos bp[T::NA];
-    Prefetch pf[T::NA];
-
-    auto fluxes = [&](int i0, int j0, int z, bool do_xy, bool do_z) {
-        const int ws = T::ND == 3 ? wslot(z) : 0, ds = T::ND == 3 ? dslot(z) : 0;
-        if (do_xy) {
-            xface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, tx, ty);
-            if (T::ND >= 2) yface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, tx, ty);
-            if ((int)threadIdx.x < T::TY) xface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, T::TX, threadIdx.x);
-            else if (T::ND >= 2 && (int)threadIdx.x < T::TY + T::TX)
-                yface<T, SOLVER>(a, sm, i0, j0, ws, ds, pwc, threadIdx.x - T::TY, T::TY);
-        }
-        if (T::ND == 3 && do_z) zface<T, SOLVER>(a, sm, i0, j0, z, pwc, tx, ty);
-    };
-
-    if (T::ND < 3) {
-        int q = blockIdx.x;
-        if (q < a.nq) {
-            setup_box<T>(a, (q % a.ncx) * T::TX, (q / a.ncx) * T::TY, bp);
-            issue<T>(a, Uin, Rin, 0, bp, pf);
-        }
-        while (q < a.nq) {
-            const int i0 = (q % a.ncx) * T::TX, j0 = (q / a.ncx) * T::TY;
-            store<T>(a, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
-            const int qn = q + gridDim.x;
-            if (qn < a.nq) {  // prefetch the next column while this one computes
-                setup_box<T>(a, (qn % a.ncx) * T::TX, (qn / a.ncx) * T::TY, bp);
-                issue<T>(a, Uin, Rin, 0, bp, pf);
-            }
-            __syncthreads();
-            if (!pwc) { recon<T>(a, sm, i0, j0, 0); __syncthreads(); }
-            fluxes(i0, j0, 0, true, false);
-            __syncthreads();
-            residual<T>(a, sm, Rout, i0, j0, 0, srmax);
-            __syncthreads();
-            q = qn;
-        }
-    } else {
-        for (int q = blockIdx.x; q < a.nq; q += gridDim.x) {
-            const int zc = q / a.ncol, col = q % a.ncol;
-            const int i0 = (col % a.ncx) * T::TX, j0 = (col / a.ncx) * T::TY;
-            const int z0 = zc * a.ch, z1 = min(L.nz, z0 + a.ch);
-            setup_box<T>(a, i0, j0, bp);
-            // prologue: planes z0-2 .. z0+1, slopes of z0-1 and z0, the z face z0-1/2
-            for (int p = z0 - 2; p <= z0; ++p) {
-                issue<T>(a, Uin, Rin, p, bp, pf);
-                store<T>(a, sm, Uout, p, z0, z1, dtf, bp, pf, health);
-            }
-            issue<T>(a, Uin, Rin, z0 + 1, bp, pf);
-            __syncthreads();
-            if (!pwc) recon<T>(a, sm, i0, j0, z0 - 1);
-            __syncthreads();
-            store<T>(a, sm, Uout, z0 + 1, z0, z1, dtf, bp, pf, health);
-            issue<T>(a, Uin, Rin, z0 + 2, bp, pf);
-            __syncthreads();
-            if (!pwc) { recon<T>(a, sm, i0, j0, z0); __syncthreads(); }
-            fluxes(i0, j0, z0 - 1, false, true);
-            __syncthreads();  // the first store below reuses the slot of plane z0-1
-            for (int z = z0; z < z1; ++z) {
-                // plane z+2 was prefetched during the previous plane's compute
-                store<T>(a, sm, Uout, z + 2, z0, z1, dtf, bp, pf, health);
-                if (z + 3 <= z1 + 1) issue<T>(a, Uin, Rin, z + 3, bp, pf);
-                __syncthreads();
-                if (!pwc) { recon<T>(a, sm, i0, j0, z + 1); __syncthreads(); }
-                fluxes(i0, j0, z, true, true);
-                __syncthreads();
-                residual<T>(a, sm, Rout, i0, j0, z, srmax);
-            }
-            __syncthreads();
-        }
-    }
-
-    // CFL: max over cells of SR/V, block max by warp shuffles, one atomic per
-    // CTA; the last CTA to finish turns it into dt (FP64) and closes the step.
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) srmax = fmaxf(srmax, __shfl_xor_sync(0xffffffffu, srmax, o));
-    health = __reduce_or_sync(0xffffffffu, health);
-    __shared__ float wmax[32];
-    __shared__ unsigned int whealth[32];
-    __shared__ bool last;
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    if (lane == 0) { wmax[wid] = srmax; whealth[wid] = health; }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        float m = 0.0f;
-        unsigned int hh = 0;
-        for (int k = 0; k < T::NT / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
-        if (m > 0.0f) atomicMax(&ctl->srmax_bits, __float_as_uint(m));
-        if (hh) atomicOr(&ctl->health, hh);
-        __threadfence();
-        last = atomicAdd(&ctl->blocks_done, 1u) == gridDim.x - 1;
-    }
-    __syncthreads();
-    if (!last || threadIdx.x != 0) return;
-    __threadfence();
+// dt of one problem from its CFL maximum, and the step's bookkeeping
+// (ComputeTimeStep :1427-1437, time += dt and iteration++ :1486-1487, and the
+// Kernel::Run snapshot/termination rules kernel.h:1763-1846).
+__device__ void finish_problem(Ctl* ctl, double cfl) {
     const float m = __uint_as_float(*(volatile unsigned int*)&ctl->srmax_bits);
-    double dt = a.mp.cfl / (double)m;
+    double dt = cfl / (double)m;
     if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
     if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
     ctl->dt_min_raw = 1.0 / (double)m;
@@ -751,19 +613,138 @@ __global__ void __launch_bounds__(T::NT) k_mix_step(MixArgs a) {
     }
 }
 
-// U[parity] += dt R[parity] / V, R[parity] = 0 (materialise the pending update).
-__global__ void k_mix_apply(MixArgs a) {
-    const Layout& L = a.L;
+// ---------------------------------------------------------------------------
+// The fused step kernel
+// ---------------------------------------------------------------------------
+
+// One work item (tile column and z chunk q of problem d).
+template <class T, int SOLVER>
+__device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm, BoxPos (&bp)[T::NA],
+                                             Prefetch (&pf)[T::NA], float& srmax, unsigned int& health) {
+    const Layout& L = d.L;
+    const int par = d.ctl->parity;
+    const double* __restrict__ Uin = d.U[par];
+    double* __restrict__ Uout = d.U[par ^ 1];
+    const float* __restrict__ Rin = d.R[par];
+    float* __restrict__ Rout = d.R[par ^ 1];
+    const float dtf = f64_to_f32(d.ctl->dt_apply);
+    const bool pwc = d.mp.recon == TS_RECON_PIECEWISE_CONSTANT;
+    const int col = q % d.ncol;
+    const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
+    setup_box<T>(d, i0, j0, bp);
+    if (T::ND < 3) {
+        issue<T>(d, Uin, Rin, 0, bp, pf);
+        store<T>(d, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
+        __syncthreads();
+        if (!pwc) { recon<T>(d, sm, i0, j0, 0); __syncthreads(); }
+        fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false);
+        __syncthreads();
+        residual<T>(d, sm, Rout, i0, j0, 0, srmax);
+    } else {
+        const int z0 = (q / d.ncol) * d.ch, z1 = min(L.nz, z0 + d.ch);
+        // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
+        // build the slopes of planes z0-1, z0 and the z face z0-1/2.
+        issue<T>(d, Uin, Rin, z0 - 2, bp, pf);
+        store<T>(d, sm, Uout, z0 - 2, z0, z1, dtf, bp, pf, health);
+        issue<T>(d, Uin, Rin, z0 - 1, bp, pf);
+        store<T>(d, sm, Uout, z0 - 1, z0, z1, dtf, bp, pf, health);
+        issue<T>(d, Uin, Rin, z0, bp, pf);
+#pragma unroll 1
+        for (int z = z0 - 2; z < z1; ++z) {
+            // plane z+2 was prefetched during the previous pass
+            store<T>(d, sm, Uout, z + 2, z0, z1, dtf, bp, pf, health);
+            if (z + 3 <= z1 + 1) issue<T>(d, Uin, Rin, z + 3, bp, pf);
+            __syncthreads();
+            if (!pwc) { recon<T>(d, sm, i0, j0, z + 1); __syncthreads(); }
+            if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true);
+            __syncthreads();
+            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, srmax);
+        }
+    }
+}
+
+// The item's CFL maximum and health into the problem's control word; the CTA
+// that completes the problem's last item closes the problem's step.
+template <class T>
+__device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsigned int health, float* wmax,
+                                           unsigned int* whealth) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) srmax = fmaxf(srmax, __shfl_xor_sync(0xffffffffu, srmax, o));
+    health = __reduce_or_sync(0xffffffffu, health);
+    if (lane == 0) { wmax[wid] = srmax; whealth[wid] = health; }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        float m = 0.0f;
+        unsigned int hh = 0;
+        for (int k = 0; k < T::NT / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
+        Ctl* ctl = d.ctl;
+        if (m > 0.0f) atomicMax(&ctl->srmax_bits, __float_as_uint(m));
+        if (hh) atomicOr(&ctl->health, hh);
+        __threadfence();
+        if (atomicAdd(&ctl->blocks_done, 1u) == (unsigned)(d.nq - 1)) {
+            __threadfence();
+            finish_problem(ctl, d.mp.cfl);
+        }
+    }
+}
+
+// BATCH = false: one problem whose descriptor is a kernel parameter (constant
+// bank: every field is a free operand).  BATCH = true: a list of (problem,
+// item) pairs; each item's descriptor is staged in shared memory.
+template <class T, int SOLVER, bool BATCH>
+__global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ ProbDesc one,
+                                                    const ProbDesc* __restrict__ probs,
+                                                    const int2* __restrict__ items, int n_items) {
+    extern __shared__ float sm[];
+    __shared__ float wmax[32];
+    __shared__ unsigned int whealth[32];
+    BoxPos bp[T::NA];
+    Prefetch pf[T::NA];
+    if constexpr (!BATCH) {
+        if (one.ctl->stop_req) return;
+        for (int q = blockIdx.x; q < n_items; q += gridDim.x) {
+            __syncthreads();  // the previous item is finished with shared memory
+            float srmax = 0.0f;
+            unsigned int health = 0;
+            process_item<T, SOLVER>(one, q, sm, bp, pf, srmax, health);
+            close_item<T>(one, srmax, health, wmax, whealth);
+        }
+    } else {
+        __shared__ ProbDesc sd;
+        __shared__ int s_skip;
+        const int nwords = (int)(sizeof(ProbDesc) / sizeof(int));
+        for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
+            const int2 pq = items[it];
+            __syncthreads();  // the previous item is finished with shared memory
+            for (int k = threadIdx.x; k < nwords; k += T::NT) ((int*)&sd)[k] = ((const int*)(probs + pq.x))[k];
+            __syncthreads();
+            if (threadIdx.x == 0) s_skip = *(volatile int*)&sd.ctl->stop_req;
+            __syncthreads();
+            if (s_skip) continue;
+            float srmax = 0.0f;
+            unsigned int health = 0;
+            process_item<T, SOLVER>(sd, pq.y, sm, bp, pf, srmax, health);
+            close_item<T>(sd, srmax, health, wmax, whealth);
+        }
+    }
+}
+
+// U[parity] += dt R[parity] / V, R[parity] = 0 for problem p (materialise the
+// pending update with the fused kernel's own rounding: (1/hx hy) (dt / hz)).
+__global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
+    const ProbDesc& d = probs[p];
+    const Layout& L = d.L;
     const long long n = L.cells();
     const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (t >= n) return;
     const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
     const long long c = L.at(i, j, k);
-    const int par = a.ctl->parity;
-    const float dtf = f64_to_f32(a.ctl->dt_apply);
-    const float cf = dtf * (a.geo[0][i + a.goff[0]].ih * a.geo[1][j + a.goff[1]].ih * a.geo[2][k + a.goff[2]].ih);
-    double* U = a.U[par];
-    float* R = a.R[par];
+    const int par = d.ctl->parity;
+    const float dtf = f64_to_f32(d.ctl->dt_apply);
+    const float cf = (d.geo[0][i + d.goff[0]].ih * d.geo[1][j + d.goff[1]].ih) * (dtf * d.geo[2][k + d.goff[2]].ih);
+    double* U = d.U[par];
+    float* R = d.R[par];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         U[(long long)v * L.plane + c] += f32_to_f64(cf * R[(long long)v * L.plane + c]);
@@ -771,25 +752,12 @@ __global__ void k_mix_apply(MixArgs a) {
     }
 }
 
-__global__ void k_mix_clear_pending(Ctl* ctl) { ctl->dt_apply = 0.0; }
-
+__global__ void k_mix_clear_pending(const ProbDesc* __restrict__ probs, int p) { probs[p].ctl->dt_apply = 0.0; }
 
 // Tile shapes compiled per dimension (one thread per tile cell).
 #define TS_MIXED_TILES_3D(X) X(3, 32, 8) X(3, 16, 16) X(3, 64, 4)
 #define TS_MIXED_TILES_2D(X) X(2, 32, 8) X(2, 16, 16)
 #define TS_MIXED_TILES_1D(X) X(1, 256, 1) X(1, 128, 1)
-
-template <class T, int SOLVER>
-cudaError_t prepare_kernel() {
-    return cudaFuncSetAttribute(k_mix_step<T, SOLVER>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)T::BYTES);
-}
-
-template <class T, int SOLVER>
-int occupancy_of() {
-    int nb = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_mix_step<T, SOLVER>, T::NT, T::BYTES);
-    return nb;
-}
 
 // Calls f.template operator()<Tile, SOLVER>() for the compiled tile matching
 // (nd, tx, ty); returns false when there is none.
@@ -809,90 +777,104 @@ bool with_tile(int nd, int tx, int ty, int solver, F&& f) {
     return found;
 }
 
-MixArgs make_args(const MixedBufs& mb) {
-    MixArgs a;
-    a.L = mb.L;
-    a.U[0] = mb.U[0]; a.U[1] = mb.U[1];
-    a.R[0] = mb.R[0]; a.R[1] = mb.R[1];
-    for (int ax = 0; ax < 3; ++ax) a.geo[ax] = mb.geo[ax];
-    a.goff[0] = mb.L.gx; a.goff[1] = mb.L.gy; a.goff[2] = mb.L.gz;
-    a.ctl = mb.ctl;
-    a.mp = mb.mp;
-    a.ncx = (mb.L.nx + mb.tx - 1) / mb.tx;
-    const int ncy = mb.L.nd >= 2 ? (mb.L.ny + mb.ty - 1) / mb.ty : 1;
-    a.ncol = a.ncx * ncy;
-    const int nz = mb.L.nd == 3 ? mb.L.nz : 1;
-    a.ch = mb.L.nd == 3 ? (nz + mb.zchunks - 1) / mb.zchunks : 1;
-    const int nchunks = (nz + a.ch - 1) / a.ch;
-    a.nq = a.ncol * nchunks;
-    return a;
-}
-
 }  // namespace
 
-ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err) {
-    const int nd = mb.L.nd;
-    if (nd == 1) ty = 1;
-    size_t bytes = 0;
-    int per_sm = 0;
-    cudaError_t e = cudaSuccess;
-    const bool ok = with_tile(nd, tx, ty, mb.mp.solver, [&]<class T, int S>() {
-        bytes = T::BYTES;
-        e = prepare_kernel<T, S>();
-        if (e == cudaSuccess) per_sm = occupancy_of<T, S>();
+bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_sm, bool batch) {
+    return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
+        *smem = T::BYTES;
+        *per_sm = 0;
+        const int b = (int)T::BYTES;
+        bool ok = cudaFuncSetAttribute(k_mix_step<T, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                  cudaSuccess;
+        if constexpr (T::ND < 3)
+            ok = ok && cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                           cudaSuccess;
+        if (!ok) return;
+        if constexpr (T::ND < 3) {
+            if (batch) {
+                cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, true>, T::NT, T::BYTES);
+                return;
+            }
+        }
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, false>, T::NT, T::BYTES);
     });
-    if (!ok) {
-        err = "no compiled tile " + std::to_string(tx) + "x" + std::to_string(ty) + " for " + std::to_string(nd) + "D";
-        return TS_ERR_UNSUPPORTED;
-    }
-    if (e != cudaSuccess) { err = std::string("cudaFuncSetAttribute: ") + cudaGetErrorString(e); return TS_ERR_CUDA; }
-    if (per_sm < 1) { err = "mixed kernel does not fit on an SM with this tile"; return TS_ERR_UNSUPPORTED; }
-    mb.tx = tx;
-    mb.ty = ty;
-    mb.smem = bytes;
-    const int ncx = (mb.L.nx + tx - 1) / tx;
-    const int ncy = nd >= 2 ? (mb.L.ny + ty - 1) / ty : 1;
-    const long long ncol = (long long)ncx * ncy;
-    const long long slots = (long long)mb.sms * per_sm;
-    const int nz = nd == 3 ? mb.L.nz : 1;
+}
+
+void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const ProbDesc& h_desc, cudaStream_t st) {
+    if (grid <= 0 || h_desc.nq <= 0) return;
+    with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
+        k_mix_step<T, S, false><<<grid, T::NT, T::BYTES, st>>>(h_desc, nullptr, nullptr, h_desc.nq);
+    });
+}
+
+bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const int2* d_items,
+                        int n_items, cudaStream_t st) {
+    if (nd == 3) return false;
+    if (grid <= 0 || n_items <= 0) return true;
+    ProbDesc none;
+    std::memset(&none, 0, sizeof none);
+    return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
+        if constexpr (T::ND < 3)
+            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_items, n_items);
+    });
+}
+
+void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots) {
+    const int nd = d.L.nd;
+    d.ncx = (d.L.nx + tx - 1) / tx;
+    const int ncy = nd >= 2 ? (d.L.ny + ty - 1) / ty : 1;
+    d.ncol = d.ncx * ncy;
+    const int nz = nd == 3 ? d.L.nz : 1;
     if (nd == 3 && zchunks <= 0) {
         // Chunks of >= 16 planes; pick the count that best fills the
-        // persistent grid, charging ~3 planes of prologue per chunk.
+        // persistent grid, charging ~2 planes of start-up per chunk.
         double best = -1.0;
         for (int c = 1; c <= std::max(1, nz / 16); ++c) {
             const int ch = (nz + c - 1) / c;
             const int nch = (nz + ch - 1) / ch;
-            const long long q = ncol * nch;
-            const double waves = std::ceil((double)q / (double)slots);
-            const double score = (double)q / (waves * (double)slots) / (1.0 + 3.0 / ch);
+            const long long q = (long long)d.ncol * nch;
+            const double waves = std::ceil((double)q / (double)std::max(1LL, slots));
+            const double score = (double)q / (waves * (double)std::max(1LL, slots)) / (1.0 + 2.0 / ch);
             if (score > best + 1e-9) { best = score; zchunks = c; }
         }
     }
-    mb.zchunks = nd == 3 ? std::max(1, std::min(zchunks, nz)) : 1;
-    const int ch = (nz + mb.zchunks - 1) / mb.zchunks;
-    const long long q = ncol * ((nz + ch - 1) / ch);
-    mb.grid = (int)std::min<long long>(q, slots);
+    zchunks = nd == 3 ? std::max(1, std::min(zchunks, nz)) : 1;
+    d.ch = nd == 3 ? (nz + zchunks - 1) / zchunks : 1;
+    d.nq = d.ncol * ((nz + d.ch - 1) / d.ch);
+}
+
+ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err) {
+    const int nd = mb.desc.L.nd;
+    if (nd == 1) ty = 1;
+    size_t bytes = 0;
+    int per_sm = 0;
+    if (!mixed_tile_info(nd, tx, ty, mb.desc.mp.solver, &bytes, &per_sm)) {
+        err = "no compiled tile " + std::to_string(tx) + "x" + std::to_string(ty) + " for " + std::to_string(nd) + "D";
+        return TS_ERR_UNSUPPORTED;
+    }
+    if (per_sm < 1) { err = "mixed kernel does not fit on an SM with this tile"; return TS_ERR_UNSUPPORTED; }
+    mb.tx = tx;
+    mb.ty = ty;
+    mb.smem = bytes;
+    const long long slots = (long long)mb.sms * per_sm;
+    mixed_items(mb.desc, tx, ty, zchunks, slots);
+    mb.zchunks = nd == 3 ? (mb.desc.L.nz + mb.desc.ch - 1) / mb.desc.ch : 1;
+    mb.grid = (int)std::min<long long>(mb.desc.nq, slots);
+    if (cudaMemcpy(mb.d_desc, &mb.desc, sizeof(ProbDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
+        err = "descriptor upload failed";
+        return TS_ERR_CUDA;
+    }
     return TS_OK;
 }
 
-
-ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
-                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err) {
+ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
+                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err) {
     if (L.plane > (1LL << 31) - 1) { err = "grid too large for the mixed path"; return TS_ERR_INVALID; }
-    mb.L = L;
-    mb.ctl = ctl;
+    d.L = L;
+    d.ctl = ctl;
+    d.goff[0] = L.gx; d.goff[1] = L.gy; d.goff[2] = L.gz;
     ts_status s;
-    for (int b = 0; b < 2; ++b) {
-        if ((s = alloc(sizeof(double) * NV * L.plane, (void**)&mb.U[b])) != TS_OK) return s;
-        if ((s = alloc(sizeof(float) * NV * L.plane, (void**)&mb.R[b])) != TS_OK) return s;
-        if (cudaMemset(mb.U[b], 0, sizeof(double) * NV * L.plane) != cudaSuccess ||
-            cudaMemset(mb.R[b], 0, sizeof(float) * NV * L.plane) != cudaSuccess) {
-            err = "cudaMemset failed";
-            return TS_ERR_CUDA;
-        }
-    }
-    // per-axis geometry with GHOST ghost entries on active axes
-    bool uniform = true;
+    // per-axis geometry with ghost entries on active axes
     for (int a = 0; a < 3; ++a) {
         const std::vector<double>& X = a == 0 ? g.x : (a == 1 ? g.y : g.z);
         const std::vector<double>& Hh = a == 0 ? g.hx : (a == 1 ? g.hy : g.hz);
@@ -922,25 +904,24 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
                 e.ir = (float)(1.0 / (xp - x0));
                 e.ih = (float)(1.0 / (i >= n || i < 0 ? hc(i) : h));
                 geo[i + gw] = e;
-                if (i >= 0 && i < n && Hh[i + 1] != Hh[1]) uniform = false;
             }
         }
-        void* d;
-        if ((s = alloc(sizeof(AxisGeo) * geo.size(), &d)) != TS_OK) return s;
-        if (cudaMemcpy(d, geo.data(), sizeof(AxisGeo) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        void* p;
+        if ((s = alloc(sizeof(AxisGeo) * geo.size(), &p)) != TS_OK) return s;
+        if (cudaMemcpy(p, geo.data(), sizeof(AxisGeo) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
             err = "geometry upload failed";
             return TS_ERR_CUDA;
         }
-        mb.geo[a] = (const AxisGeo*)d;
+        d.geo[a] = (const AxisGeo*)p;
     }
-    MixPhys& m = mb.mp;
+    MixPhys& m = d.mp;
+    std::memset(&m, 0, sizeof m);
     m.nd = L.nd;
     m.recon = c.reconstruction;
     m.limiter = c.limiter;
     m.solver = c.riemann_solver;
     m.eos = c.eos;
     for (int a = 0; a < 3; ++a) m.periodic[a] = ph.periodic[a];
-    m.uniform = uniform;
     m.gamma = (float)ph.gamma;
     m.gm1 = (float)(ph.gamma - 1.0);
     m.pinf = (float)ph.p_inf;
@@ -960,6 +941,25 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
         m.bc_state[sd][4] = (float)(ph.bc.pstatic[sd] / (ph.gamma - 1) + 0.5 * r * (vx * vx + vy * vy + vz * vz));
         for (int a = 0; a < 3; ++a) m.bc_vel[sd][a] = (float)ph.bc.vel[sd][a];
     }
+    return TS_OK;
+}
+
+ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
+                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err) {
+    ts_status s;
+    ProbDesc& d = mb.desc;
+    std::memset(&d, 0, sizeof d);
+    if ((s = mixed_problem(c, L, ph, g, ctl, alloc, d, err)) != TS_OK) return s;
+    for (int b = 0; b < 2; ++b) {
+        if ((s = alloc(sizeof(double) * NV * L.plane, (void**)&d.U[b])) != TS_OK) return s;
+        if ((s = alloc(sizeof(float) * NV * L.plane, (void**)&d.R[b])) != TS_OK) return s;
+        if (cudaMemset(d.U[b], 0, sizeof(double) * NV * L.plane) != cudaSuccess ||
+            cudaMemset(d.R[b], 0, sizeof(float) * NV * L.plane) != cudaSuccess) {
+            err = "cudaMemset failed";
+            return TS_ERR_CUDA;
+        }
+    }
+    if ((s = alloc(sizeof(ProbDesc), (void**)&mb.d_desc)) != TS_OK) return s;
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&mb.sms, cudaDevAttrMultiProcessorCount, dev);
@@ -968,12 +968,9 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
     return mixed_set_tile(mb, tx, ty, 0, err);
 }
 
-
 void mixed_step(MixedBufs& mb, const Phys&, cudaStream_t st, cudaEvent_t* ev, int* n_launch, const char** names) {
-    const MixArgs a = make_args(mb);
     if (ev) cudaEventRecord(ev[0], st);
-    with_tile(mb.L.nd, mb.tx, mb.ty, mb.mp.solver,
-              [&]<class T, int S>() { k_mix_step<T, S><<<mb.grid, T::NT, T::BYTES, st>>>(a); });
+    mixed_launch_single(mb.desc.L.nd, mb.tx, mb.ty, mb.desc.mp.solver, mb.grid, mb.desc, st);
     if (ev) cudaEventRecord(ev[1], st);
     if (names) names[0] = "k_mix_step";
     if (n_launch) *n_launch = 1;
@@ -981,17 +978,17 @@ void mixed_step(MixedBufs& mb, const Phys&, cudaStream_t st, cudaEvent_t* ev, in
 
 void mixed_reset(MixedBufs& mb, cudaStream_t st) {
     // caller has set parity 0 and dt_apply 0 in the control word
-    cudaMemsetAsync(mb.R[0], 0, sizeof(float) * NV * mb.L.plane, st);
+    cudaMemsetAsync(mb.desc.R[0], 0, sizeof(float) * NV * mb.desc.L.plane, st);
 }
 
-void mixed_materialize(MixedBufs& mb, const Phys&, cudaStream_t st) {
-    const MixArgs a = make_args(mb);
-    const long long n = mb.L.cells();
-    k_mix_apply<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(a);
-    k_mix_clear_pending<<<1, 1, 0, st>>>(mb.ctl);
+void mixed_apply(const ProbDesc* d_probs, int p, long long cells, cudaStream_t st) {
+    k_mix_apply<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(d_probs, p);
+    k_mix_clear_pending<<<1, 1, 0, st>>>(d_probs, p);
 }
 
-double* mixed_state(MixedBufs& mb, int parity) { return mb.U[parity & 1]; }
+void mixed_materialize(MixedBufs& mb, const Phys&, cudaStream_t st) { mixed_apply(mb.d_desc, 0, mb.desc.L.cells(), st); }
+
+double* mixed_state(MixedBufs& mb, int parity) { return mb.desc.U[parity & 1]; }
 
 }  // namespace ts
 
@@ -999,8 +996,8 @@ double* mixed_state(MixedBufs& mb, int parity) { return mb.U[parity & 1]; }
 // ts_advance_noalloc: the fused mixed-precision step for callers that may not
 // allocate device memory.  Everything the kernel needs beyond the caller's
 // input and output -- both state buffers, both residual buffers, the grid
-// geometry and the control word -- lives in one fixed array in device memory
-// that is part of this library's module.
+// geometry, the problem descriptor and the control word -- lives in one fixed
+// array in device memory that is part of this library's module.
 // ---------------------------------------------------------------------------
 namespace ts {
 namespace noalloc {
@@ -1008,7 +1005,7 @@ namespace noalloc {
 constexpr size_t kNaPlane = TS_NOALLOC_MAX_PLANE;
 constexpr size_t kNaGeo = kNaPlane + 16;  // AxisGeo entries of all three axes together
 constexpr size_t kNaBytes = 2 * NV * kNaPlane * sizeof(double) + 2 * NV * kNaPlane * sizeof(float) +
-                            kNaGeo * sizeof(AxisGeo) + sizeof(Ctl) + 16 * 256;
+                            kNaGeo * sizeof(AxisGeo) + sizeof(Ctl) + sizeof(ProbDesc) + 16 * 256;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNaBytes];
 
@@ -1115,12 +1112,12 @@ extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* stat
         if (e_ != cudaSuccess) return fail(TS_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
     } while (0)
     NA_CUDA(cudaMemcpyAsync(ctl, &c, sizeof c, cudaMemcpyHostToDevice, st));
-    NA_CUDA(cudaMemsetAsync(mb.R[0], 0, sizeof(float) * NV * L.plane, st));
+    NA_CUDA(cudaMemsetAsync(mb.desc.R[0], 0, sizeof(float) * NV * L.plane, st));
     const unsigned blocks = (unsigned)((L.cells() + 255) / 256);
-    k_na_scatter<<<blocks, 256, 0, st>>>(state_in, L, mb.U[0]);
+    k_na_scatter<<<blocks, 256, 0, st>>>(state_in, L, mb.desc.U[0]);
     for (int k = 0; k < n_steps; ++k) mixed_step(mb, ph, st);
     mixed_materialize(mb, ph, st);
-    k_na_gather<<<blocks, 256, 0, st>>>(state_out, L, mb.U[0], mb.U[1], ctl);
+    k_na_gather<<<blocks, 256, 0, st>>>(state_out, L, mb.desc.U[0], mb.desc.U[1], ctl);
     NA_CUDA(cudaGetLastError());
     NA_CUDA(cudaMemcpyAsync(&c, ctl, sizeof c, cudaMemcpyDeviceToHost, st));
     NA_CUDA(cudaStreamSynchronize(st));

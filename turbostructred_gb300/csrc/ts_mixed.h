@@ -1,5 +1,7 @@
 // Mixed-precision path: FP32 reconstruction, EOS and Riemann flux with FP64
-// state, FP64 stage accumulation and FP64 dt.  See ts_mixed.cu.
+// state, FP64 stage accumulation and FP64 dt.  One fused kernel advances a
+// work list of (problem, tile column, z chunk) items of one or many problems
+// by one stage.  See ts_mixed.cu.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -11,7 +13,7 @@
 
 namespace ts {
 
-// Per-axis geometry of one cell index (device, indexed i + GHOST).
+// Per-axis geometry of one cell index (device, indexed i + ghost width).
 struct AxisGeo {
     float h;      // cell size
     float hh;     // h / 2
@@ -21,11 +23,10 @@ struct AxisGeo {
     float ih;     // 1 / h
 };
 
-// Physics constants for the FP32 flux path, passed by value.
+// Physics constants of one problem for the FP32 flux path.
 struct MixPhys {
     int nd, recon, limiter, solver, eos;
     int periodic[3];
-    int uniform;          // every axis uniform: one volume for all cells
     float gamma, gm1, pinf, einf, eps;
     double einf_d;        // gamma p_inf / (gamma - 1): energy shift, applied in FP64
     double cfl;
@@ -34,21 +35,46 @@ struct MixPhys {
     float bc_vel[6][3];    // MovingWall velocity
 };
 
-struct MixedBufs {
+// Everything the fused kernel needs about one problem (lives in device memory).
+struct ProbDesc {
     Layout L;
-    double* U[2] = {nullptr, nullptr};  // NV FP64 planes each: U^n and U^{n+1}
-    float* R[2] = {nullptr, nullptr};   // NV FP32 planes each: pending residual
-    const AxisGeo* geo[3] = {nullptr, nullptr, nullptr};
-    Ctl* ctl = nullptr;
+    double* U[2];          // NV FP64 planes each: U^n and U^{n+1}
+    float* R[2];           // NV FP32 planes each: pending residual
+    const AxisGeo* geo[3];
+    int goff[3];           // ghost offset into geo per axis
+    Ctl* ctl;              // per-problem step control word
     MixPhys mp;
-    int tx = 32, ty = 8;   // tile (one of the compiled shapes)
-    int zchunks = 1;       // z chunks per column (3D)
-    int grid = 0;          // persistent CTAs
+    int ncx, ncol;         // tile columns along x, in total
+    int ch, nq;            // planes per z chunk, work items (columns x chunks)
+};
+
+struct MixedBufs {
+    ProbDesc desc;                 // host copy
+    ProbDesc* d_desc = nullptr;    // device copy
+    int tx = 32, ty = 8;           // tile (one of the compiled shapes)
+    int zchunks = 1;               // z chunks per column (3D)
+    int grid = 0;                  // persistent CTAs
     size_t smem = 0;
     int sms = 0;
 };
 
 using DeviceAlloc = std::function<ts_status(size_t bytes, void** out)>;
+
+// Geometry and physics of one problem (host work + uploads through `alloc`).
+ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
+                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err);
+// Work items of a problem for a tile and z chunking (0 = automatic, given
+// the persistent grid size `slots`).
+void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots);
+// Compiled tile lookup: smem bytes and resident CTAs per SM (of the batched
+// kernel when `batch`), or false.
+bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_sm, bool batch = false);
+// One stage of one problem (descriptor passed by value).
+void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const ProbDesc& h_desc, cudaStream_t st);
+// One stage of a list of (problem, item) pairs of 1D or 2D problems sharing
+// the solver; false when no batched kernel exists for (nd, tile).
+bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const int2* d_items,
+                        int n_items, cudaStream_t st);
 
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                      const DeviceAlloc& alloc, MixedBufs& mb, std::string& err);
@@ -63,6 +89,8 @@ void mixed_step(MixedBufs& mb, const Phys& ph, cudaStream_t st, cudaEvent_t* ev 
 void mixed_reset(MixedBufs& mb, cudaStream_t st);
 // Applies the pending residual so U[parity] holds the current state.
 void mixed_materialize(MixedBufs& mb, const Phys& ph, cudaStream_t st);
+// The same for problem p of a device descriptor array.
+void mixed_apply(const ProbDesc* d_probs, int p, long long cells, cudaStream_t st);
 // Current state buffer (host must have pulled ctl->parity).
 double* mixed_state(MixedBufs& mb, int parity);
 
