@@ -315,6 +315,174 @@ def run_ours(args, rank, ws, lr, dist):
         print(json.dumps(line), flush=True)
 
 
+def tubes_cell_updates(infos, probs):
+    return float(sum(c["nx"] * inf["iteration"] for (c, _), inf in zip(probs, infos)))
+
+
+def run_tubes(args, rank, ws, lr, dist):
+    """Batched 1D tubes: one step = the whole batch solved to t_end."""
+    import torch
+
+    from turbostructred_gb300 import build, capi, workloads
+    if rank == 0 or dist is None:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    capi.load()
+    probs = workloads.tubes(args.tubes, seed=4096 + rank)
+    budget = int(1.5 * sum(capi.batch_problem_bytes(c) for c, _ in probs)) + (64 << 20)
+    cells = sum(c["nx"] for c, _ in probs)
+
+    def solve(subset, tune):
+        b = capi.Batch(budget, device=lr)
+        t0 = time.perf_counter()
+        ids = [b.add(c, v) for c, v in subset]
+        t1 = time.perf_counter()
+        choice = b.autotune(args.tune_stages) if tune else None
+        torch.cuda.synchronize()
+        t2 = time.perf_counter()
+        left = b.run()
+        t3 = time.perf_counter()
+        outs = [b.get(i) for i in ids]
+        t4 = time.perf_counter()
+        st = b.stats()
+        b.close()
+        assert left == 0
+        return dict(add_s=t1 - t0, run_s=t3 - t2, get_s=t4 - t3, stats=st, choice=choice,
+                    infos=[o[1] for o in outs], states=outs)
+
+    for _ in range(args.warmup):
+        solve(probs[:128], False)
+    uuid = gpu_uuid(lr)
+    sampler = ClockSampler(uuid)
+    if dist is not None:
+        dist.barrier()
+    runs = [solve(probs, args.tune_stages > 0) for _ in range(args.steps)]
+    clocks = sampler.stop()
+    run_s = max(r["run_s"] for r in runs) if args.steps == 1 else statistics.median(r["run_s"] for r in runs)
+    cu = tubes_cell_updates(runs[0]["infos"], probs)
+    value = ws * cu / run_s
+    e2e_s = statistics.median(r["add_s"] + r["run_s"] + r["get_s"] for r in runs)
+    health = sum(1 for inf in runs[0]["infos"] if inf["health"])
+    iters = [inf["iteration"] for inf in runs[0]["infos"]]
+    st = runs[0]["stats"]
+    # accuracy: a sample of tubes against the FP64 plain path
+    errs = []
+    for k in range(0, len(probs), max(1, len(probs) // args.err_tubes)):
+        c, ic = probs[k]
+        with capi.Solver(c, capi.PRECISION_FP64, device=lr) as s:
+            s.set_state(ic)
+            inf = s.run()
+            ref = s.get_state()
+        got = runs[0]["states"][k][0]
+        if inf["iteration"] == iters[k]:
+            errs.append(rel_errors(got, ref))
+    err = {k: max(e[k] for e in errs) for k in errs[0]} if errs else None
+    bytes_in = sum(v.size * 8 for _, v in probs)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
+                "warmup": args.warmup, "ms_per_step": 1e3 * run_s, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64 state / f32 flux", "data": "synthetic (seeded tubes, no dataset)",
+                "config": {"workload": f"{len(probs)} batched 1D shock tubes to t_end 0.1 (sizes 64-4096 "
+                                       "log-uniform, half stiffened gas, PWC/Linear2psLim mixed, Roe, CFL 0.5)",
+                           "tubes": len(probs), "cells": cells, "step": "the whole batch solved to t_end",
+                           "warmup_step": "the first 128 tubes solved to t_end",
+                           "l2": "state resident in HBM; each stage touches every active tube once",
+                           "tile": runs[0]["choice"]},
+                "e2e": {"value": ws * cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_in,
+                        "d2h_bytes_per_step": bytes_in, "seconds_per_job": e2e_s},
+                "clocks": clocks, "gpu_launches": st["launches"],
+                "batch": {"stages": st["stages"], "launches": st["launches"], "cell_updates": cu,
+                          "max_iterations": max(iters), "unhealthy": health, "add_s": runs[0]["add_s"],
+                          "get_s": runs[0]["get_s"]},
+                "mixed_error_vs_fp64": {"tubes_sampled": len(errs), **(err or {})}}
+        print(json.dumps(line), flush=True)
+
+
+def run_served(args, rank, ws, lr, dist):
+    """Served stream: Poisson arrivals of 2D quadrant problems."""
+    import threading
+
+    from turbostructred_gb300 import build, capi, workloads
+    if rank == 0 or dist is None:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    capi.load()
+    reqs = workloads.stream(args.rate, args.seconds, seed=200 + rank, steps=args.served_steps)
+    srv = capi.Server(int(args.budget_gb * 2**30), chunk_ms=args.chunk_ms, device=lr)
+    # warm-up: a few solves of each size through the same server
+    for side in workloads.SIDES:
+        c = workloads.quadrant_case(side, capi.RS_ROE, 20)
+        srv.wait(srv.submit(c, workloads.stream_state(c, [1.0, 0.0, 0.0, 1.0] * 4, 1), keep_state=False))
+    st0 = srv.stats()
+    ids = []
+    lat = []
+    done = threading.Event()
+
+    def collector():
+        k = 0
+        while not (done.is_set() and k >= len(ids)):
+            if k >= len(ids):
+                time.sleep(0.001)
+                continue
+            _, info, t = srv.wait(ids[k])
+            lat.append((t["submit_s"], t["admit_s"], t["finish_s"], info["iteration"]))
+            k += 1
+
+    th = threading.Thread(target=collector)
+    th.start()
+    sampler = ClockSampler(gpu_uuid(lr))
+    t0 = time.perf_counter()
+    late = 0.0
+    for at, case, params, seed in reqs:
+        ic = workloads.stream_state(case, params, seed)
+        now = time.perf_counter() - t0
+        if now < at:
+            time.sleep(at - now)
+        else:
+            late = max(late, now - at)
+        ids.append(srv.submit(case, ic, keep_state=True))
+    done.set()
+    th.join()
+    t_end = time.perf_counter() - t0
+    clocks = sampler.stop()
+    st = srv.stats()
+    srv.close()
+    lat_ms = sorted(1e3 * (f - s) for s, a, f, it in lat)
+    wait_ms = sorted(1e3 * (a - s) for s, a, f, it in lat)
+
+    def pct(v, p):
+        import math
+        return v[min(len(v), max(1, math.ceil(p / 100 * len(v)))) - 1] if v else None
+
+    cu = st["cell_updates"] - st0["cell_updates"]
+    first = min(s for s, a, f, it in lat)
+    last = max(f for s, a, f, it in lat)
+    value = cu / (last - first)
+    bytes_io = sum(c["nx"] * c["ny"] * 40 for _, c, _, _ in reqs)
+    if rank == 0:
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": len(reqs),
+                "warmup": len(workloads.SIDES), "ms_per_step": 1e3 * (last - first) / max(1, len(reqs)),
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 flux",
+                "data": "synthetic (seeded Poisson stream of quadrant problems, no dataset)",
+                "config": {"workload": f"served stream: Poisson {args.rate:g} req/s for {args.seconds:g} s of 2D "
+                                       f"quadrant Riemann problems, sides {list(workloads.SIDES)}, Roe/HLLC at "
+                                       f"random, {args.served_steps} RK steps each, HBM budget {args.budget_gb:g} GB",
+                           "requests": len(reqs), "step": "one served request", "chunk_ms": args.chunk_ms},
+                "latency_ms": {"p50": pct(lat_ms, 50), "p99": pct(lat_ms, 99), "max": lat_ms[-1] if lat_ms else None},
+                "admission_wait_ms": {"p50": pct(wait_ms, 50), "p99": pct(wait_ms, 99)},
+                "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_io / max(1, len(reqs)),
+                        "d2h_bytes_per_step": bytes_io / max(1, len(reqs)),
+                        "note": "latency and throughput are end to end: host submit (copy of the initial state) "
+                                "to the final state back in host memory"},
+                "server": {k: st[k] for k in ("submitted", "completed", "rejected", "stages", "launches", "busy_s")},
+                "offered_cell_updates_per_s": sum(c["nx"] * c["ny"] * args.served_steps for _, c, _, _ in reqs)
+                / args.seconds, "client_max_lateness_s": late, "wall_s": t_end,
+                "clocks": clocks, "gpu_launches": st["launches"] - st0["launches"]}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -331,13 +499,22 @@ def main():
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
+    p.add_argument("--workload", choices=["blast3d", "tubes", "served"], default="blast3d")
+    p.add_argument("--tubes", type=int, default=4096)
+    p.add_argument("--tune-stages", type=int, default=8)
+    p.add_argument("--err-tubes", type=int, default=16)
+    p.add_argument("--rate", type=float, default=200.0)
+    p.add_argument("--seconds", type=float, default=60.0)
+    p.add_argument("--served-steps", type=int, default=500)
+    p.add_argument("--budget-gb", type=float, default=150.0)
+    p.add_argument("--chunk-ms", type=float, default=2.0)
     args = p.parse_args()
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))
         return
     rank, ws, lr, dist = dist_init()
-    run_ours(args, rank, ws, lr, dist)
+    {"blast3d": run_ours, "tubes": run_tubes, "served": run_served}[args.workload](args, rank, ws, lr, dist)
     if dist is not None:
         dist.destroy_process_group()
 

@@ -274,6 +274,61 @@ ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx, int32_t* t
 /* Totals since creation: cell-updates done, stages launched, kernel launches. */
 ts_status ts_batch_stats(ts_batch* b, double* cell_updates, int64_t* stages, int64_t* launches);
 
+/* ---------------------------------------------------------------------------
+   Served solves: a request loop over one batch.  No counterpart in the
+   reference.  Requests (1D/2D, mixed precision, any EOS / solver /
+   reconstruction) are submitted from any thread and queue in arrival order;
+   a worker thread admits the head of the queue whenever the batch arena has
+   room for it (and fewer than max_active solves are running), advances all
+   admitted solves together in chunks of stages, and retires each one as it
+   reaches its MaxTime / MaxIteration.  Requests that arrive while others run
+   join at the next chunk boundary (continuous batching): each result is that
+   of the problem alone in a batch, bit for bit.
+   --------------------------------------------------------------------------- */
+typedef struct ts_server ts_server;
+
+typedef struct ts_request_times {
+    double submit_s;   /* seconds since the server was created */
+    double admit_s;    /* state uploaded, first chunk pending */
+    double finish_s;   /* retired: final state read back */
+} ts_request_times;
+
+typedef struct ts_server_stats {
+    int64_t submitted, admitted, completed, rejected;
+    int64_t queued, active;            /* right now */
+    int64_t stages, launches;          /* batch totals */
+    double cell_updates;               /* of all solves, retired or running */
+    double busy_s;                     /* time the worker had solves admitted */
+    double latency_p50_ms, latency_p99_ms, latency_max_ms;  /* submit -> finish, completed solves */
+    double wait_p50_ms, wait_p99_ms;   /* submit -> admit */
+    size_t bytes_budget, bytes_in_use;
+    ts_status worker_status;           /* first error the worker met (TS_OK if none) */
+} ts_server_stats;
+
+/* max_active: cap on admitted solves (0 = memory is the only limit);
+   chunk_ms: target duration of one chunk of stages (0 = 2 ms). */
+ts_status ts_server_create(int32_t device, size_t memory_budget, int32_t max_active, double chunk_ms,
+                           ts_server** out);
+/* Stops the worker (solves in flight are dropped) and frees everything. */
+void ts_server_destroy(ts_server* s);
+
+/* Queues a solve; cfg and values are copied.  keep_state = 0 keeps only the
+   step info and times (no final state).  TS_ERR_UNSUPPORTED for a problem a
+   batch cannot hold, TS_ERR_NO_MEMORY for one larger than the whole budget. */
+ts_status ts_server_submit(ts_server* s, const ts_config* cfg, const double* values, int32_t keep_state,
+                           int32_t* request_id);
+
+/* Waits up to timeout_ms (< 0: forever) for a request; TS_ERR_TIMEOUT if it
+   has not finished.  On success copies the final state (if kept and values is
+   not NULL), its step info and times, and forgets the request. */
+ts_status ts_server_wait(ts_server* s, int32_t request_id, int32_t timeout_ms, double* values, ts_step_info* info,
+                         ts_request_times* times);
+
+/* Waits up to timeout_ms (< 0: forever) until nothing is queued or running. */
+ts_status ts_server_drain(ts_server* s, int32_t timeout_ms);
+
+ts_status ts_server_stats_get(ts_server* s, ts_server_stats* out);
+
 /* Advance a state by n_steps of the mixed-precision fused step without
    allocating any device memory.  No counterpart in the reference: this is
    for callers that are not allowed to call cudaMalloc themselves or through

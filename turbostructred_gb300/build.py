@@ -33,6 +33,7 @@ UNITS = {
     "ts_capi.cu": [],
     "ts_batch.cu": [],
     "ts_host.cpp": [],
+    "ts_server.cpp": [],
 }
 
 
@@ -75,7 +76,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
     with cf.ThreadPoolExecutor(max_workers=len(UNITS)) as ex:
         objs = list(ex.map(_compile, UNITS))
     if _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-Xcompiler", "-fPIC"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB + ".tmp"] + objs + ["-Xcompiler", "-fPIC", "-lpthread"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")

@@ -87,6 +87,21 @@ class Timing(C.Structure):
                     kernels={self.kernel_name[k].value.decode(): self.kernel_ms[k] for k in range(self.n_kernels)})
 
 
+class RequestTimes(C.Structure):
+    _fields_ = [("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [(n, C.c_int64) for n in ("submitted", "admitted", "completed", "rejected", "queued", "active",
+                                         "stages", "launches")] + \
+               [(n, C.c_double) for n in ("cell_updates", "busy_s", "latency_p50_ms", "latency_p99_ms",
+                                          "latency_max_ms", "wait_p50_ms", "wait_p99_ms")] + \
+               [("bytes_budget", C.c_size_t), ("bytes_in_use", C.c_size_t), ("worker_status", C.c_int)]
+
+    def as_dict(self):
+        return {n: getattr(self, n) for n, _ in self._fields_}
+
+
 EXPORTS = [
     "ts_create", "ts_destroy", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
     "ts_run", "ts_set_tile",
@@ -95,6 +110,8 @@ EXPORTS = [
     "ts_batch_create", "ts_batch_destroy", "ts_batch_add", "ts_batch_problem_bytes", "ts_batch_step",
     "ts_batch_run", "ts_batch_finished", "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile",
     "ts_batch_autotune", "ts_batch_stats",
+    "ts_server_create", "ts_server_destroy", "ts_server_submit", "ts_server_wait", "ts_server_drain",
+    "ts_server_stats_get",
 ]
 
 _lib = None
@@ -145,6 +162,15 @@ def load(path: str = LIB_PATH):
     L.ts_batch_stats.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), P(C.c_int64)]
     for name in ("ts_batch_create", "ts_batch_add", "ts_batch_step", "ts_batch_run", "ts_batch_finished",
                  "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile", "ts_batch_autotune", "ts_batch_stats"):
+        getattr(L, name).restype = C.c_int
+    L.ts_server_create.argtypes = [C.c_int32, C.c_size_t, C.c_int32, C.c_double, P(C.c_void_p)]
+    L.ts_server_destroy.argtypes = [C.c_void_p]
+    L.ts_server_destroy.restype = None
+    L.ts_server_submit.argtypes = [C.c_void_p, P(Config), P(C.c_double), C.c_int32, P(C.c_int32)]
+    L.ts_server_wait.argtypes = [C.c_void_p, C.c_int32, C.c_int32, P(C.c_double), P(StepInfo), P(RequestTimes)]
+    L.ts_server_drain.argtypes = [C.c_void_p, C.c_int32]
+    L.ts_server_stats_get.argtypes = [C.c_void_p, P(ServerStats)]
+    for name in ("ts_server_create", "ts_server_submit", "ts_server_wait", "ts_server_drain", "ts_server_stats_get"):
         getattr(L, name).restype = C.c_int
     L.ts_last_error.restype = C.c_char_p
     L.ts_status_string.restype = C.c_char_p
@@ -392,3 +418,60 @@ class Batch:
         cu, st, la = C.c_double(), C.c_int64(), C.c_int64()
         check(self.lib.ts_batch_stats(self.b, C.byref(cu), C.byref(st), C.byref(la)))
         return dict(cell_updates=cu.value, stages=st.value, launches=la.value)
+
+
+class Server:
+    """Served solves: submit from any thread, a native worker admits them into
+    one batch as memory frees up and retires them as they finish."""
+
+    def __init__(self, memory_budget: int, max_active: int = 0, chunk_ms: float = 2.0, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        check(self.lib.ts_server_create(device, memory_budget, max_active, chunk_ms, C.byref(h)))
+        self.h = h
+        self.cases = {}
+
+    def close(self):
+        if self.h:
+            self.lib.ts_server_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def submit(self, case: dict, values: np.ndarray, keep_state: bool = True) -> int:
+        cfg, keep = to_config(case, PRECISION_MIXED)
+        v = np.ascontiguousarray(values, dtype=np.float64)
+        assert v.size == int(np.prod(interior_shape(case)))
+        rid = C.c_int32()
+        check(self.lib.ts_server_submit(self.h, C.byref(cfg), v.ctypes.data_as(C.POINTER(C.c_double)),
+                                        int(keep_state), C.byref(rid)))
+        self.cases[rid.value] = (case, keep_state)
+        return rid.value
+
+    def wait(self, rid: int, timeout_ms: int = -1):
+        """(state or None, step info, times) of a finished request."""
+        case, kept = self.cases.get(rid, (None, False))
+        out = np.empty(interior_shape(case)) if kept else None
+        si, tm = StepInfo(), RequestTimes()
+        ptr = out.ctypes.data_as(C.POINTER(C.c_double)) if out is not None else None
+        check(self.lib.ts_server_wait(self.h, rid, timeout_ms, ptr, C.byref(si), C.byref(tm)))
+        self.cases.pop(rid, None)
+        return out, si.as_dict(), dict(submit_s=tm.submit_s, admit_s=tm.admit_s, finish_s=tm.finish_s)
+
+    def drain(self, timeout_ms: int = -1):
+        check(self.lib.ts_server_drain(self.h, timeout_ms))
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        check(self.lib.ts_server_stats_get(self.h, C.byref(st)))
+        return st.as_dict()

@@ -1,0 +1,323 @@
+// Served solves over one batch (include/ts_fvm.h, ts_server_*).
+//
+// Threads: callers submit and wait; one worker owns the batch.  The worker
+// repeats: admit queued requests in arrival order while the arena has room,
+// run one chunk of stages of everything admitted, retire what finished
+// (state read back, slot and memory freed).  The chunk length adapts so one
+// chunk takes about chunk_ms, which bounds how long a new arrival waits for
+// the next admission point and how late a finished solve is noticed.
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <mutex>
+#include <string>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+#include "ts_fvm.h"
+#include "ts_internal.h"
+
+namespace {
+
+using Clock = std::chrono::steady_clock;
+
+struct Request {
+    int32_t id = -1;
+    ts_config cfg{};
+    std::vector<ts_block_node> blocks[3];
+    std::vector<double> values;  // initial state; the final one when kept
+    bool keep = true;
+    size_t bytes = 0;
+    double cells = 0.0;
+    int32_t batch_id = -1;
+    bool done = false;
+    ts_status status = TS_OK;
+    std::string error;
+    ts_step_info info{};
+    ts_request_times t{};
+};
+
+using Req = std::shared_ptr<Request>;
+
+double percentile(std::vector<double> v, double p) {
+    if (v.empty()) return 0.0;
+    std::sort(v.begin(), v.end());
+    // nearest rank
+    size_t k = (size_t)std::ceil(p / 100.0 * (double)v.size());
+    k = std::min(std::max<size_t>(k, 1), v.size());
+    return v[k - 1];
+}
+
+}  // namespace
+
+struct ts_server {
+    int device = 0;
+    size_t budget = 0;
+    int max_active = 0;
+    double chunk_ms = 2.0;
+    ts_batch* batch = nullptr;
+    Clock::time_point t0 = Clock::now();
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Req> queue;
+    std::unordered_map<int32_t, Req> requests;  // submitted and not yet collected
+    std::unordered_map<int32_t, Req> running;   // by batch id
+    std::vector<double> lat_ms, wait_ms;
+    int64_t submitted = 0, admitted = 0, completed = 0, rejected = 0;
+    int64_t stages = 0, launches = 0;
+    double cell_updates = 0.0, busy_s = 0.0;
+    size_t in_use = 0;
+    ts_status worker_status = TS_OK;
+    std::string worker_error;
+    bool stop = false;
+    int32_t next_id = 0;
+    std::thread worker;
+
+    double now() const { return std::chrono::duration<double>(Clock::now() - t0).count(); }
+
+    // Under the lock.
+    void retire(const Req& r, ts_status st, const std::string& err) {
+        r->status = st;
+        r->error = err;
+        r->done = true;
+        r->t.finish_s = now();
+        if (st == TS_OK) {
+            ++completed;
+            lat_ms.push_back(1e3 * (r->t.finish_s - r->t.submit_s));
+        } else {
+            ++rejected;
+        }
+    }
+
+    void worker_failed(ts_status st) {
+        std::lock_guard<std::mutex> lk(mu);
+        worker_status = st;
+        worker_error = ts_last_error();
+        for (auto& kv : running) retire(kv.second, st, worker_error);
+        running.clear();
+        for (auto& r : queue) retire(r, st, worker_error);
+        queue.clear();
+        in_use = 0;
+        cv_done.notify_all();
+    }
+
+    void loop() {
+        int chunk = 4;
+        std::vector<int32_t> fin(1024);
+        for (;;) {
+            std::vector<Req> admit;
+            {
+                std::unique_lock<std::mutex> lk(mu);
+                if (running.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+                if (stop) return;
+                size_t room = budget - in_use;
+                while (!queue.empty()) {
+                    const Req& r = queue.front();
+                    if (max_active > 0 && running.size() + admit.size() >= (size_t)max_active) break;
+                    if (r->bytes > room) break;  // arrival order: the head waits for memory
+                    room -= r->bytes;
+                    admit.push_back(r);
+                    queue.pop_front();
+                }
+            }
+            for (size_t k = 0; k < admit.size(); ++k) {
+                const Req& r = admit[k];
+                int32_t bid = -1;
+                const ts_status s = ts_batch_add(batch, &r->cfg, r->values.data(), &bid);
+                if (s == TS_ERR_NO_MEMORY) {
+                    // the arena is fragmented: the rest goes back to the head, in order
+                    std::lock_guard<std::mutex> lk(mu);
+                    for (size_t j = admit.size(); j-- > k;) queue.push_front(admit[j]);
+                    break;
+                }
+                std::lock_guard<std::mutex> lk(mu);
+                if (s != TS_OK) {
+                    retire(r, s, ts_last_error());
+                    cv_done.notify_all();
+                    continue;
+                }
+                r->batch_id = bid;
+                r->t.admit_s = now();
+                if (!r->keep) std::vector<double>().swap(r->values);
+                running[bid] = r;
+                in_use += r->bytes;
+                ++admitted;
+                wait_ms.push_back(1e3 * (r->t.admit_s - r->t.submit_s));
+            }
+            {
+                std::lock_guard<std::mutex> lk(mu);
+                if (running.empty()) continue;
+            }
+            const Clock::time_point c0 = Clock::now();
+            int32_t active = 0;
+            ts_status s = ts_batch_run(batch, chunk, &active);
+            if (s != TS_OK) { worker_failed(s); return; }
+            const double el = std::chrono::duration<double>(Clock::now() - c0).count();
+            // next chunk: about chunk_ms of stages at the current rate
+            const double per_stage_ms = std::max(1e3 * el / chunk, 1e-3);
+            chunk = std::min(std::max((int)(chunk_ms / per_stage_ms), 1), 4096);
+            // retire finished solves
+            for (;;) {
+                int32_t n = 0;
+                if ((s = ts_batch_finished(batch, fin.data(), (int32_t)fin.size(), &n)) != TS_OK) break;
+                for (int32_t k = 0; k < n; ++k) {
+                    Req r;
+                    {
+                        std::lock_guard<std::mutex> lk(mu);
+                        auto it = running.find(fin[k]);
+                        if (it == running.end()) continue;
+                        r = it->second;
+                    }
+                    s = ts_batch_get(batch, fin[k], r->keep ? r->values.data() : nullptr, &r->info);
+                    if (s == TS_OK) s = ts_batch_remove(batch, fin[k]);
+                    if (s != TS_OK) break;
+                    std::lock_guard<std::mutex> lk(mu);
+                    running.erase(fin[k]);
+                    in_use -= r->bytes;
+                    retire(r, TS_OK, "");
+                }
+                if (s != TS_OK || n < (int32_t)fin.size()) break;
+            }
+            if (s != TS_OK) { worker_failed(s); return; }
+            double cu = 0.0;
+            int64_t st = 0, la = 0;
+            ts_batch_stats(batch, &cu, &st, &la);
+            std::lock_guard<std::mutex> lk(mu);
+            busy_s += el;
+            cell_updates = cu;
+            stages = st;
+            launches = la;
+            cv_done.notify_all();
+        }
+    }
+};
+
+extern "C" {
+
+ts_status ts_server_create(int32_t device, size_t budget, int32_t max_active, double chunk_ms, ts_server** out) {
+    if (!out) return ts::fail(TS_ERR_INVALID, "NULL argument");
+    *out = nullptr;
+    if (max_active < 0 || chunk_ms < 0.0) return ts::fail(TS_ERR_INVALID, "bad argument");
+    std::unique_ptr<ts_server> s(new ts_server());
+    ts_status st = ts_batch_create(device, budget, &s->batch);
+    if (st != TS_OK) return st;
+    s->device = device;
+    s->budget = budget;
+    s->max_active = max_active;
+    s->chunk_ms = chunk_ms > 0.0 ? chunk_ms : 2.0;
+    s->t0 = Clock::now();
+    ts_server* p = s.get();
+    s->worker = std::thread([p] { p->loop(); });
+    *out = s.release();
+    return TS_OK;
+}
+
+void ts_server_destroy(ts_server* s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    ts_batch_destroy(s->batch);
+    delete s;
+}
+
+ts_status ts_server_submit(ts_server* s, const ts_config* cfg, const double* values, int32_t keep_state,
+                           int32_t* request_id) {
+    if (!s || !cfg || !values || !request_id) return ts::fail(TS_ERR_INVALID, "NULL argument");
+    const size_t bytes = ts_batch_problem_bytes(cfg);
+    if (bytes == 0) {
+        std::string err;
+        if (ts::validate_config(*cfg, err) != TS_OK) return ts::fail(TS_ERR_INVALID, err);
+        return ts::fail(TS_ERR_UNSUPPORTED, "served solves are 1D/2D mixed precision");
+    }
+    if (bytes > s->budget) return ts::fail(TS_ERR_NO_MEMORY, "solve larger than the server's memory budget");
+    Req r = std::make_shared<Request>();
+    r->cfg = *cfg;
+    for (int a = 0; a < 3; ++a) {
+        if (cfg->n_blocks[a] > 0 && cfg->blocks[a]) {
+            r->blocks[a].assign(cfg->blocks[a], cfg->blocks[a] + cfg->n_blocks[a]);
+            r->cfg.blocks[a] = r->blocks[a].data();
+        }
+    }
+    const double ny = cfg->n_dims > 1 ? cfg->ny : 1, nz = cfg->n_dims > 2 ? cfg->nz : 1;
+    r->cells = (double)cfg->nx * ny * nz;
+    r->values.assign(values, values + (size_t)r->cells * 5);
+    r->keep = keep_state != 0;
+    r->bytes = bytes;
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->worker_status != TS_OK) return ts::fail(s->worker_status, "server stopped: " + s->worker_error);
+    r->id = s->next_id++;
+    r->t.submit_s = s->now();
+    s->requests[r->id] = r;
+    s->queue.push_back(r);
+    ++s->submitted;
+    *request_id = r->id;
+    s->cv_work.notify_one();
+    return TS_OK;
+}
+
+ts_status ts_server_wait(ts_server* s, int32_t id, int32_t timeout_ms, double* values, ts_step_info* info,
+                         ts_request_times* times) {
+    if (!s) return ts::fail(TS_ERR_INVALID, "NULL server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(id);
+    if (it == s->requests.end()) return ts::fail(TS_ERR_NOT_FOUND, "unknown request id");
+    Req r = it->second;
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, [&] { return r->done; });
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), [&] { return r->done; })) {
+        return ts::fail(TS_ERR_TIMEOUT, "request not finished");
+    }
+    s->requests.erase(id);
+    if (r->status != TS_OK) return ts::fail(r->status, r->error);
+    if (values && r->keep) std::copy(r->values.begin(), r->values.end(), values);
+    if (info) *info = r->info;
+    if (times) *times = r->t;
+    return TS_OK;
+}
+
+ts_status ts_server_drain(ts_server* s, int32_t timeout_ms) {
+    if (!s) return ts::fail(TS_ERR_INVALID, "NULL server");
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto idle = [&] { return s->queue.empty() && s->running.empty(); };
+    if (timeout_ms < 0) {
+        s->cv_done.wait(lk, idle);
+    } else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), idle)) {
+        return ts::fail(TS_ERR_TIMEOUT, "server still busy");
+    }
+    return s->worker_status == TS_OK ? TS_OK : ts::fail(s->worker_status, s->worker_error);
+}
+
+ts_status ts_server_stats_get(ts_server* s, ts_server_stats* o) {
+    if (!s || !o) return ts::fail(TS_ERR_INVALID, "NULL argument");
+    std::lock_guard<std::mutex> lk(s->mu);
+    o->submitted = s->submitted;
+    o->admitted = s->admitted;
+    o->completed = s->completed;
+    o->rejected = s->rejected;
+    o->queued = (int64_t)s->queue.size();
+    o->active = (int64_t)s->running.size();
+    o->stages = s->stages;
+    o->launches = s->launches;
+    o->cell_updates = s->cell_updates;
+    o->busy_s = s->busy_s;
+    o->latency_p50_ms = percentile(s->lat_ms, 50.0);
+    o->latency_p99_ms = percentile(s->lat_ms, 99.0);
+    o->latency_max_ms = s->lat_ms.empty() ? 0.0 : *std::max_element(s->lat_ms.begin(), s->lat_ms.end());
+    o->wait_p50_ms = percentile(s->wait_ms, 50.0);
+    o->wait_p99_ms = percentile(s->wait_ms, 99.0);
+    o->bytes_budget = s->budget;
+    o->bytes_in_use = s->in_use;
+    o->worker_status = s->worker_status;
+    return TS_OK;
+}
+
+}  // extern "C"
