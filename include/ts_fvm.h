@@ -183,11 +183,13 @@ ts_status ts_run(ts_handle* h, ts_step_info* info);
 ts_status ts_get_step_info(ts_handle* h, ts_step_info* info);
 ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info);
 
-/* Launch shape of the mixed-precision fused kernel: the tile (cells per CTA
-   along x and y; compiled shapes: 3D 32x8, 16x16, 64x4; 2D 32x8, 16x16;
-   1D 256, 128) and the number of z chunks each tile column is cut into
-   (0 = chosen from the grid and the SM count).  Results do not depend on
-   either: every face flux is a function of its two cells only.
+/* Launch shape of the mixed-precision fused kernel: the tile (threads per
+   CTA along x and y; compiled shapes: 3D 32x8, 16x16, 64x4, each thread one
+   cell, marching z; 2D 260, 132, 68 one-row tiles marching y; 1D 512, 256,
+   128; one-row tiles own tx - 4 cells) and the number of chunks each tile
+   column's march is cut into (0 = chosen from the grid and the SM count).
+   Every face flux is a function of its two cells only; other tiles are
+   other compiled instances and agree to FP32 rounding.
    TS_ERR_UNSUPPORTED for the FP64 path or an uncompiled tile. */
 ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty, int32_t z_chunks);
 
@@ -261,14 +263,17 @@ ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* in
 /* Frees a problem's slot and memory. */
 ts_status ts_batch_remove(ts_batch* b, int32_t id);
 
-/* Launch shape for the problems of dimension nd (tile along x, y; see
-   ts_set_tile) and CTAs per SM of the persistent grid (0 = as many as fit). */
+/* Launch shape for the problems of dimension nd: tx = threads of the
+   one-row tile along x (1D: 512, 256, 128; 2D: 260, 132, 68; the tile owns
+   tx - 4 cells), or 0 to pick per problem from its x extent; ty is ignored;
+   and CTAs per SM of the persistent grid (0 = as many as fit). */
 ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int32_t ctas_per_sm);
 
-/* Autotuner: times `stages` stages of the current batch for every compiled
-   tile and CTA count, restoring the problems' states after each trial, and
-   keeps the fastest; *tx, *ty, *ctas_per_sm receive the choice for the
-   batch's dominant dimension. */
+/* Autotuner: times `stages` stages of the current batch for the per-problem
+   policy and every compiled tile, each at several CTA counts, restoring the
+   problems' states after each trial, and keeps the fastest; *tx (0: per
+   problem), *ty, *ctas_per_sm receive the choice for the batch's dominant
+   dimension. */
 ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx, int32_t* ty, int32_t* ctas_per_sm);
 
 /* Totals since creation: cell-updates done, stages launched, kernel launches. */

@@ -202,7 +202,7 @@ def test_batch_unhealthy_problem_is_stopped(tslib):
     assert np.array_equal(res[0][0], ref[0][0]) and np.array_equal(res[2][0], ref[1][0])
 
 
-@pytest.mark.parametrize("tile", [(1, 128, 1, 0), (2, 16, 16, 0), (2, 32, 8, 1)])
+@pytest.mark.parametrize("tile", [(1, 128, 1, 0), (1, 512, 1, 2), (2, 68, 1, 0), (2, 260, 1, 1), (2, 0, 1, 2)])
 def test_batch_tiles_agree(tile, tslib):
     probs = mixed_problems(max_time=1e30, max_iter=15)
     base = run_batch(probs)
@@ -221,7 +221,7 @@ def test_batch_autotune_restores_state(tslib):
         b.step(5)
         st0 = b.stats()
         tx, ty, ct = b.autotune(4)
-        assert (tx, ty) in ((32, 8), (16, 16), (256, 1), (128, 1))
+        assert tx in (0, 260, 132, 68) and ty == 1
         assert b.stats()["stages"] == st0["stages"]
         assert all(b.get(i, want_state=False)[1]["iteration"] == 5 for i in ids)
         b.run()

@@ -117,10 +117,11 @@ def test_mixed_tile_and_chunk_independent(nd, tslib):
     elif nd == 2:
         case = O.make_case(ndims=2, nx=70, ny=45, periodic=(1, 0, 1), recon=3, solver=3, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, NAT, NAT])
-        tiles, scen, params = [(32, 8, 0), (16, 16, 0)], 1, [2.0, 1.0, 0.5, 2.5, 0.01]
+        tiles = [(260, 1, 0), (132, 1, 0), (68, 1, 0), (260, 1, 4), (68, 1, 1)]
+        scen, params = 1, [2.0, 1.0, 0.5, 2.5, 0.01]
     else:
         case = O.make_case(ndims=1, nx=1000, periodic=(0, 1, 1), recon=3, cfl=0.5, bc=[NAT] * 6)
-        tiles, scen, params = [(256, 1, 0), (128, 1, 0)], 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
+        tiles, scen, params = [(512, 1, 0), (256, 1, 0), (128, 1, 0)], 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
     full = _full(case, scen, 3, params)
     outs = [run(case, full, 9, 1, tile=t)[0] for t in tiles]
     # the same launch configuration is deterministic bit for bit

@@ -16,6 +16,8 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <memory>
@@ -110,20 +112,44 @@ struct Slot {
     int id = -1;
     bool collected = false;   // reported by ts_batch_finished
     long long cells = 0;
+    int tx = 0, ty = 0;       // tile of this problem
     std::vector<void*> mem;
     ts_config cfg;
 };
 
 struct Group {
-    int nd = 0, solver = 0;
+    int nd = 0, solver = 0, tx = 0, ty = 0;
     int2* d_items = nullptr;
     int cap = 0, n = 0;
     int grid = 0;
 };
 
+// Launch policy of one dimension: a fixed tile or (tx = 0) a tile chosen per
+// problem from its x extent; ctas = resident CTAs per SM (0: as many as fit).
 struct Tune {
-    int tx, ty, ctas;  // ctas 0: as many as fit
+    int tx, ty, ctas;
 };
+
+// One-row tiles compiled for batched problems (threads along x).
+const int kTiles1D[3] = {512, 256, 128};
+const int kTiles2D[3] = {260, 132, 68};
+constexpr int kRowsPerItem = 64;  // marching-axis rows per work item of a 2D problem
+
+// The one-row tile that covers nx cells with the fewest warp-slots per cell,
+// charging each column ~4 warps of fixed cost (setup, barriers, close).
+int pick_tile(int nd, int nx) {
+    const int* c = nd == 1 ? kTiles1D : kTiles2D;
+    int best = c[0];
+    double best_cost = 1e300;
+    for (int k = 0; k < 3; ++k) {
+        int cx, cy;
+        mixed_tile_cells(nd, c[k], 1, &cx, &cy);
+        const double cols = std::ceil((double)nx / cx);
+        const double cost = cols * ((c[k] + 31) / 32 + 4) / (double)nx;
+        if (cost < best_cost - 1e-12) { best_cost = cost; best = c[k]; }
+    }
+    return best;
+}
 
 }  // namespace
 }  // namespace ts
@@ -145,7 +171,7 @@ struct ts_batch {
     std::vector<Group> groups;
     bool dirty = true;
     std::map<int, cudaGraphExec_t> graphs;
-    Tune tune[4] = {{0, 0, 0}, {256, 1, 0}, {32, 8, 0}, {32, 8, 0}};
+    Tune tune[4] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 0}};
     double* stage_buf = nullptr;
     size_t stage_doubles = 0;
     double done_cell_updates = 0.0;  // of removed problems
@@ -205,27 +231,39 @@ struct ts_batch {
         return TS_OK;
     }
 
-    int per_sm(int nd, int solver) const {
+    int per_sm(const Group& g) const {
         size_t b;
         int n = 0;
-        mixed_tile_info(nd, tune[nd].tx, tune[nd].ty, solver, &b, &n, true);
-        if (tune[nd].ctas > 0) n = std::min(n, tune[nd].ctas);
+        mixed_tile_info(g.nd, g.tx, g.ty, g.solver, &b, &n, true);
+        if (tune[g.nd].ctas > 0) n = std::min(n, tune[g.nd].ctas);
         return std::max(n, 0);
+    }
+
+    // Tile of a problem under the current policy, and its work items.
+    void place(int s) {
+        ProbDesc& d = desc[s];
+        const int nd = d.L.nd;
+        slots[s].tx = tune[nd].tx > 0 ? tune[nd].tx : pick_tile(nd, d.kn[0]);
+        slots[s].ty = 1;
+        const int chunks = nd >= 2 ? std::max(1, d.kn[2] / kRowsPerItem) : 1;
+        mixed_items(d, slots[s].tx, 1, chunks, (long long)sms);
     }
 
     // Work items of unfinished problems, grouped by (nd, solver), each group
     // sorted by problem size, largest first.
     ts_status rebuild() {
-        std::map<std::pair<int, int>, std::vector<int>> bykey;
+        std::map<std::array<int, 4>, std::vector<int>> bykey;
         for (int s = 0; s < capacity; ++s) {
             if (!slots[s].used || h_ctl[s].stop_req) continue;
-            bykey[{desc[s].L.nd, desc[s].mp.solver}].push_back(s);
+            bykey[{desc[s].L.nd, desc[s].mp.solver, slots[s].tx, slots[s].ty}].push_back(s);
         }
         std::vector<Group> ng;
         for (auto& kv : bykey) {
             Group g;
-            g.nd = kv.first.first;
-            g.solver = kv.first.second;
+            g.nd = kv.first[0];
+            g.solver = kv.first[1];
+            g.tx = kv.first[2];
+            g.ty = kv.first[3];
             auto& v = kv.second;
             std::stable_sort(v.begin(), v.end(), [&](int a, int b2) { return slots[a].cells > slots[b2].cells; });
             std::vector<int2> items;
@@ -234,7 +272,7 @@ struct ts_batch {
             g.n = (int)items.size();
             // reuse an old buffer of the same key when large enough
             for (auto& og : groups)
-                if (og.d_items && og.nd == g.nd && og.solver == g.solver && og.cap >= g.n) {
+                if (og.d_items && og.cap >= g.n) {
                     g.d_items = og.d_items; g.cap = og.cap; og.d_items = nullptr;
                     break;
                 }
@@ -243,7 +281,7 @@ struct ts_batch {
                 TB_CUDA(cudaMalloc(&g.d_items, sizeof(int2) * g.cap));
             }
             TB_CUDA(cudaMemcpyAsync(g.d_items, items.data(), sizeof(int2) * g.n, cudaMemcpyHostToDevice, stream));
-            g.grid = std::min(g.n, std::max(1, per_sm(g.nd, g.solver)) * sms);
+            g.grid = std::min(g.n, std::max(1, per_sm(g)) * sms);
             ng.push_back(g);
         }
         for (auto& og : groups) cudaFree(og.d_items);
@@ -255,8 +293,7 @@ struct ts_batch {
 
     void enqueue_stage() {
         for (auto& g : groups) {
-            const Tune& t = tune[g.nd];
-            mixed_launch_batch(g.nd, t.tx, t.ty, g.solver, g.grid, d_desc, g.d_items, g.n, stream);
+            mixed_launch_batch(g.nd, g.tx, g.ty, g.solver, g.grid, d_desc, g.d_items, g.n, stream);
             ++launches;
         }
         ++stages;
@@ -420,8 +457,7 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
         if ((s = take(sizeof(double) * NV * L.plane, (void**)&d.U[k])) != TS_OK) { undo(); return s; }
         if ((s = take(sizeof(float) * NV * L.plane, (void**)&d.R[k])) != TS_OK) { undo(); return s; }
     }
-    const Tune& t = b->tune[L.nd];
-    mixed_items(d, t.tx, L.nd == 1 ? 1 : t.ty, 0, (long long)b->sms);
+    b->place(slot);
     // initial state: host -> staging -> U[0]; no pending residual
     const size_t nvals = (size_t)L.cells() * NV;
     if (b->stage_doubles < nvals) {
@@ -558,18 +594,20 @@ ts_status ts_batch_remove(ts_batch* b, int32_t id) {
 }
 
 ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int32_t ctas) {
-    if (!b || nd < 1 || nd > 2) return fail(TS_ERR_INVALID, "bad argument");
-    if (nd == 1) ty = 1;
-    size_t bytes;
-    int per;
-    if (!mixed_tile_info(nd, tx, ty, TS_RS_ROE_PIKE, &bytes, &per, true) || per < 1)
-        return fail(TS_ERR_UNSUPPORTED, "no compiled tile of that shape");
+    if (!b || nd < 1 || nd > 2 || ctas < 0) return fail(TS_ERR_INVALID, "bad argument");
+    ty = 1;
+    if (tx != 0) {
+        size_t bytes;
+        int per;
+        if (!mixed_tile_info(nd, tx, ty, TS_RS_ROE_PIKE, &bytes, &per, true) || per < 1)
+            return fail(TS_ERR_UNSUPPORTED, "no compiled tile of that shape");
+    }
     DevGuard g(b->device);
     TB_CUDA(cudaStreamSynchronize(b->stream));
     b->tune[nd] = Tune{tx, ty, ctas};
     for (int s = 0; s < b->capacity; ++s) {
         if (!b->slots[s].used || b->desc[s].L.nd != nd) continue;
-        mixed_items(b->desc[s], tx, ty, 0, (long long)b->sms);
+        b->place(s);
         TB_CUDA(cudaMemcpyAsync(b->d_desc + s, &b->desc[s], sizeof(ProbDesc), cudaMemcpyHostToDevice, b->stream));
     }
     TB_CUDA(cudaStreamSynchronize(b->stream));
@@ -602,8 +640,20 @@ ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx_out, int32_
     };
     TB_CUDA(cudaMemcpyAsync(snap, b->arena.base, hb, cudaMemcpyDeviceToDevice, b->stream));
     TB_CUDA(cudaMemcpyAsync(snap_ctl, b->d_ctl, sizeof(Ctl) * b->capacity, cudaMemcpyDeviceToDevice, b->stream));
-    const std::vector<std::pair<int, int>> tiles =
-        nd == 1 ? std::vector<std::pair<int, int>>{{256, 1}, {128, 1}} : std::vector<std::pair<int, int>>{{32, 8}, {16, 16}};
+    // candidates: the per-problem policy, then every compiled one-row tile;
+    // each with as many resident CTAs as fit, and capped at 2 and 1
+    std::vector<Tune> cand;
+    const int* tiles = nd == 1 ? kTiles1D : kTiles2D;
+    for (int k = -1; k < 3; ++k) {
+        const int tx = k < 0 ? 0 : tiles[k];
+        size_t bytes;
+        int per = 0;
+        mixed_tile_info(nd, tx > 0 ? tx : tiles[0], 1, TS_RS_ROE_PIKE, &bytes, &per, true);
+        if (per < 1) continue;
+        cand.push_back(Tune{tx, 1, 0});
+        for (int c : {2, 1})
+            if (c < per) cand.push_back(Tune{tx, 1, c});
+    }
     const Tune saved = b->tune[nd];
     const long long st0 = b->stages, la0 = b->launches;
     Tune best = saved;
@@ -611,25 +661,18 @@ ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx_out, int32_
     cudaEvent_t e0, e1;
     cudaEventCreate(&e0);
     cudaEventCreate(&e1);
-    for (auto tl : tiles) {
-        size_t bytes;
-        int per;
-        if (!mixed_tile_info(nd, tl.first, tl.second, TS_RS_ROE_PIKE, &bytes, &per, true) || per < 1) continue;
-        for (int ctas = per; ctas >= 1; ctas = (ctas > 1 ? ctas / 2 : 0)) {
-            if ((s = ts_batch_set_tile(b, nd, tl.first, tl.second, ctas)) != TS_OK) break;
-            if ((s = b->launch(1)) != TS_OK) break;  // rebuild + warm-up
-            if ((s = restore()) != TS_OK) break;
-            cudaEventRecord(e0, b->stream);
-            if ((s = b->launch(stages)) != TS_OK) break;
-            cudaEventRecord(e1, b->stream);
-            cudaEventSynchronize(e1);
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, e0, e1);
-            if (ms < best_ms) { best_ms = ms; best = Tune{tl.first, tl.second, ctas}; }
-            if ((s = restore()) != TS_OK) break;
-            if (ctas == 1) break;
-        }
-        if (s != TS_OK) break;
+    for (const Tune& t : cand) {
+        if ((s = ts_batch_set_tile(b, nd, t.tx, t.ty, t.ctas)) != TS_OK) break;
+        if ((s = b->launch(1)) != TS_OK) break;  // rebuild + warm-up
+        if ((s = restore()) != TS_OK) break;
+        cudaEventRecord(e0, b->stream);
+        if ((s = b->launch(stages)) != TS_OK) break;
+        cudaEventRecord(e1, b->stream);
+        cudaEventSynchronize(e1);
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (ms < best_ms) { best_ms = ms; best = t; }
+        if ((s = restore()) != TS_OK) break;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);

@@ -227,38 +227,56 @@ __device__ __forceinline__ float flux32(const MixPhys& p, int A, const float UL[
 // ---------------------------------------------------------------------------
 // Compile-time tile geometry and shared-memory layout (floats)
 // ---------------------------------------------------------------------------
-template <int ND_, int TX_, int TY_>
+// Kernel axes: 0 = x, 1 = the tile's second axis (3D only), 2 = the marching
+// axis (z in 3D, y in 2D).  ProbDesc maps each kernel axis to the problem's
+// geometry, extent, strides and physical direction.
+//
+// Two-axis tiles (3D): TX_ x TY_ threads own TX_ x TY_ cells.  One-row tiles
+// (1D, and 2D marching along y): TX_ threads own TX_ - 4 cells, so every
+// thread has exactly one box position, at most one reconstruction position
+// and at most one face per axis (no thread does a second round).
+template <int TX_, int TY_, bool MARCH_>
 struct Tile {
-    static constexpr int ND = ND_;
-    static constexpr int TX = TX_;
-    static constexpr int TY = ND_ >= 2 ? TY_ : 1;
-    static constexpr int NT = TX * TY;
+    static constexpr bool HAS_Y = TY_ > 1;
+    static constexpr bool MARCH = MARCH_;
+    static constexpr int NT = TX_ * TY_;
+    static constexpr int TX = HAS_Y ? TX_ : TX_ - 2 * HB;  // cells along x
+    static constexpr int TY = HAS_Y ? TY_ : 1;             // cells along kernel axis 1
+    static constexpr int NAX = 1 + (HAS_Y ? 1 : 0) + (MARCH ? 1 : 0);  // active axes
+    static constexpr int AZ = HAS_Y ? 2 : 1;               // slope slot of the marching axis
     static constexpr int BX = TX + 2 * HB;                 // working-state box
-    static constexpr int BY = ND >= 2 ? TY + 2 * HB : 1;
+    static constexpr int BY = HAS_Y ? TY + 2 * HB : 1;
     static constexpr int RX = TX + 2;                      // reconstruction ring
-    static constexpr int RY = ND >= 2 ? TY + 2 : 1;
+    static constexpr int RY = HAS_Y ? TY + 2 : 1;
     static constexpr int NBOX = BX * BY;
     static constexpr int NRING = RX * RY;
     static constexpr int NA = (NBOX + NT - 1) / NT;        // box positions per thread
     static constexpr int NB = (NRING + NT - 1) / NT;       // ring positions per thread
-    static constexpr int WS = ND == 3 ? 3 : 1;             // working-state planes kept
-    static constexpr int DS = ND == 3 ? 2 : 1;             // slope planes kept
+    static constexpr int WS = MARCH ? 3 : 1;               // working-state planes kept
+    static constexpr int DS = MARCH ? 2 : 1;               // slope planes kept
     static constexpr int W_OFF = 0;
     static constexpr int D_OFF = W_OFF + WS * NV * NBOX;
-    static constexpr int FX_OFF = D_OFF + DS * ND * NV * NRING;
+    static constexpr int FX_OFF = D_OFF + DS * NAX * NV * NRING;
     static constexpr int FY_OFF = FX_OFF + 6 * TY * (TX + 1);
-    static constexpr int FZ_OFF = FY_OFF + (ND >= 2 ? 6 * (TY + 1) * TX : 0);
-    static constexpr int TOTAL = FZ_OFF + (ND == 3 ? 2 * 6 * TY * TX : 0);
+    static constexpr int FZ_OFF = FY_OFF + (HAS_Y ? 6 * (TY + 1) * TX : 0);
+    static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TY * TX : 0);
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
+    static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
 
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
     static __device__ __forceinline__ int d(int s, int ax, int v, int ring) {
-        return D_OFF + ((s * ND + ax) * NV + v) * NRING + ring;
+        return D_OFF + ((s * NAX + ax) * NV + v) * NRING + ring;
     }
     static __device__ __forceinline__ int fx(int v, int y, int x) { return FX_OFF + (v * TY + y) * (TX + 1) + x; }
     static __device__ __forceinline__ int fy(int v, int y, int x) { return FY_OFF + (v * (TY + 1) + y) * TX + x; }
     static __device__ __forceinline__ int fz(int s, int v, int y, int x) {
         return FZ_OFF + ((s * 6 + v) * TY + y) * TX + x;
+    }
+    // the cell (x, y) of this thread in the tile; false if it owns none
+    static __device__ __forceinline__ bool cell(int tid, int& x, int& y) {
+        if (HAS_Y) { x = tid % TX; y = tid / TX; return true; }
+        x = tid; y = 0;
+        return tid < TX;
     }
 };
 
@@ -266,11 +284,11 @@ __device__ __forceinline__ int wslot(int p) { return (p + 3) % 3; }
 __device__ __forceinline__ int dslot(int p) { return (p + 2) & 1; }
 
 // One working-state position of a thread: where its source cell lives in a
-// z-plane and how to turn it into the working copy.
+// plane and how to turn it into the working copy.
 struct BoxPos {
-    int off;        // element offset of the source cell within a z-plane; -1: not used
+    int off;        // element offset of the source cell within a plane; -1: not used
     int box;        // box index in shared memory
-    float cfxy;     // 1 / (hx hy) of the source cell
+    float cfxy;     // 1 / (h0 h1) of the source cell (kernel axes 0 and 1)
     int xs, ys;     // boundary side applied after mirroring, or -1
     bool own;       // the cell belongs to this tile: write U^{n+1}
 };
@@ -282,7 +300,6 @@ struct Prefetch {
 
 template <class T>
 __device__ __forceinline__ void setup_box(const ProbDesc& d, int i0, int j0, BoxPos (&bp)[T::NA]) {
-    const Layout& L = d.L;
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
         const int t = threadIdx.x + k * T::NT;
@@ -290,27 +307,30 @@ __device__ __forceinline__ void setup_box(const ProbDesc& d, int i0, int j0, Box
         if (t >= T::NBOX) continue;
         const int lx = t % T::BX, ly = t / T::BX;
         const int dx = lx < HB ? HB - lx : (lx >= T::TX + HB ? lx - T::TX - HB + 1 : 0);
-        const int dy = T::ND >= 2 ? (ly < HB ? HB - ly : (ly >= T::TY + HB ? ly - T::TY - HB + 1 : 0)) : 0;
+        const int dy = T::HAS_Y ? (ly < HB ? HB - ly : (ly >= T::TY + HB ? ly - T::TY - HB + 1 : 0)) : 0;
         if (dx + dy > HB) continue;
         const int gi = i0 + lx - HB;
-        const int gj = T::ND >= 2 ? j0 + ly - HB : 0;
-        if (gi >= L.nx + HB) continue;
-        if (T::ND >= 2 && gj >= L.ny + HB) continue;
+        const int gj = T::HAS_Y ? j0 + ly - HB : 0;
+        if (gi >= d.kn[0] + HB) continue;
+        if (T::HAS_Y && gj >= d.kn[1] + HB) continue;
         int si, sj = 0;
-        resolve(gi, L.nx, d.mp.periodic[0], 0, si, bp[k].xs);
+        resolve(gi, d.kn[0], d.kper[0], 0, si, bp[k].xs);
         bp[k].ys = -1;
-        if (T::ND >= 2) resolve(gj, L.ny, d.mp.periodic[1], 2, sj, bp[k].ys);
-        bp[k].off = (sj + L.gy) * L.px + (si + L.gx);
+        if (T::HAS_Y) resolve(gj, d.kn[1], d.kper[1], 2 * d.kphys[1], sj, bp[k].ys);
+        bp[k].off = (int)(si + sj * d.kstr[1]);
         bp[k].box = t;
-        bp[k].cfxy = __ldg(&d.geo[0][si + d.goff[0]].ih) * __ldg(&d.geo[1][sj + d.goff[1]].ih);
-        bp[k].own = dx == 0 && dy == 0 && gi < L.nx && gj < L.ny;
+        bp[k].cfxy = __ldg(&d.kgeo[0][si + d.kgoff[0]].ih) * __ldg(&d.kgeo[1][sj + d.kgoff[1]].ih);
+        bp[k].own = dx == 0 && dy == 0 && gi < d.kn[0] && gj < d.kn[1];
     }
 }
 
+// Source plane of marching index p (wrapped or mirrored), and the boundary
+// side to apply (-1: none).
+template <class T>
 __device__ __forceinline__ int plane_of(const ProbDesc& d, int p, int& zs) {
     int sk = 0;
     zs = -1;
-    resolve(p, d.L.nz, d.mp.periodic[2], 4, sk, zs);
+    if (T::MARCH) resolve(p, d.kn[2], d.kper[2], 2 * d.kphys[2], sk, zs);
     return sk;
 }
 
@@ -319,18 +339,18 @@ template <class T>
 __device__ __forceinline__ void issue(const ProbDesc& d, const double* __restrict__ Uin,
                                       const float* __restrict__ Rin, int p, const BoxPos (&bp)[T::NA],
                                       Prefetch (&pf)[T::NA]) {
-    const Layout& L = d.L;
+    const long long plane = d.L.plane;
     int zs;
-    const int sk = T::ND == 3 ? plane_of(d, p, zs) : 0;
-    const int zoff = (sk + L.gz) * L.px * L.ey;
+    const int sk = plane_of<T>(d, p, zs);
+    const long long zoff = d.kbase + sk * d.kstr[2];
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
         if (bp[k].off < 0) continue;
         const long long c = zoff + bp[k].off;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) pf[k].u[v] = __ldcg(Uin + v * L.plane + c);
+        for (int v = 0; v < NV; ++v) pf[k].u[v] = __ldcg(Uin + v * plane + c);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) pf[k].r[v] = __ldcg(Rin + v * L.plane + c);
+        for (int v = 0; v < NV; ++v) pf[k].r[v] = __ldcg(Rin + v * plane + c);
     }
 }
 
@@ -340,13 +360,13 @@ template <class T>
 __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __restrict__ Uout, int p, int z0, int z1,
                                       float dtf, const BoxPos (&bp)[T::NA], const Prefetch (&pf)[T::NA],
                                       unsigned int& health) {
-    const Layout& L = d.L;
     const MixPhys& mp = d.mp;
+    const long long plane = d.L.plane;
     int zs = -1;
-    const int sk = T::ND == 3 ? plane_of(d, p, zs) : 0;
-    const int zoff = (sk + L.gz) * L.px * L.ey;
-    const float cfz = dtf * __ldg(&d.geo[2][sk + d.goff[2]].ih);
-    const int slot = T::ND == 3 ? wslot(p) : 0;
+    const int sk = plane_of<T>(d, p, zs);
+    const long long zoff = d.kbase + sk * d.kstr[2];
+    const float cfz = dtf * __ldg(&d.kgeo[2][sk + d.kgoff[2]].ih);
+    const int slot = T::MARCH ? wslot(p) : 0;
     const bool own_plane = p >= z0 && p < z1;
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
@@ -360,8 +380,8 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
         w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf[k].u[4] - mp.einf_d) : f64_to_f32(pf[k].u[4])) +
                inc[4];
         if (bp[k].xs >= 0) bc32(mp, bp[k].xs, 0, w);
-        if (T::ND >= 2 && bp[k].ys >= 0) bc32(mp, bp[k].ys, 1, w);
-        if (T::ND == 3 && zs >= 0) bc32(mp, zs, 2, w);
+        if (T::HAS_Y && bp[k].ys >= 0) bc32(mp, bp[k].ys, bp[k].ys >> 1, w);
+        if (T::MARCH && zs >= 0) bc32(mp, zs, zs >> 1, w);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp[k].box)] = w[v];
         if (own_plane && bp[k].own) {
@@ -370,7 +390,7 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 un[v] = pf[k].u[v] + f32_to_f64(inc[v]);
-                __stcg(Uout + v * L.plane + c, un[v]);
+                __stcg(Uout + v * plane + c, un[v]);
             }
             if (!(un[0] > 0.0)) health |= (un[0] == un[0]) ? TS_HEALTH_NEG_DENSITY : TS_HEALTH_NAN;
             if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
@@ -382,45 +402,44 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
 // excluded); ring cells outside a non-periodic boundary are not needed.
 template <class T>
 __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int j0, int p) {
-    const Layout& L = d.L;
     const MixPhys& mp = d.mp;
     int sk = 0, zs;
-    if (T::ND == 3) {
-        if ((p < 0 || p >= L.nz) && !mp.periodic[2]) return;
-        resolve(p, L.nz, 1, 4, sk, zs);
+    if (T::MARCH) {
+        if ((p < 0 || p >= d.kn[2]) && !d.kper[2]) return;
+        resolve(p, d.kn[2], 1, 0, sk, zs);
     }
-    const int ws = T::ND == 3 ? wslot(p) : 0;
-    const int wd = T::ND == 3 ? wslot(p - 1) : 0, wu = T::ND == 3 ? wslot(p + 1) : 0;
-    const int ds = T::ND == 3 ? dslot(p) : 0;
+    const int ws = T::MARCH ? wslot(p) : 0;
+    const int wd = T::MARCH ? wslot(p - 1) : 0, wu = T::MARCH ? wslot(p + 1) : 0;
+    const int ds = T::MARCH ? dslot(p) : 0;
     AxisGeo gz;
-    if (T::ND == 3) gz = d.geo[2][sk + d.goff[2]];
+    if (T::MARCH) gz = d.kgeo[2][sk + d.kgoff[2]];
 #pragma unroll
     for (int k = 0; k < T::NB; ++k) {
         const int t = threadIdx.x + k * T::NT;
         if (t >= T::NRING) continue;
         const int rx = t % T::RX, ry = t / T::RX;
         const bool ox = rx < 1 || rx > T::TX;
-        const bool oy = T::ND >= 2 && (ry < 1 || ry > T::TY);
+        const bool oy = T::HAS_Y && (ry < 1 || ry > T::TY);
         if (ox && oy) continue;
-        const int gi = i0 + rx - 1, gj = T::ND >= 2 ? j0 + ry - 1 : 0;
-        if (gi > L.nx || (T::ND >= 2 && gj > L.ny)) continue;
-        if ((gi < 0 || gi >= L.nx) && !mp.periodic[0]) continue;
-        if (T::ND >= 2 && (gj < 0 || gj >= L.ny) && !mp.periodic[1]) continue;
+        const int gi = i0 + rx - 1, gj = T::HAS_Y ? j0 + ry - 1 : 0;
+        if (gi > d.kn[0] || (T::HAS_Y && gj > d.kn[1])) continue;
+        if ((gi < 0 || gi >= d.kn[0]) && !d.kper[0]) continue;
+        if (T::HAS_Y && (gj < 0 || gj >= d.kn[1]) && !d.kper[1]) continue;
         int si, sj = 0, xs, ys;
-        resolve(gi, L.nx, 1, 0, si, xs);
-        if (T::ND >= 2) resolve(gj, L.ny, 1, 2, sj, ys);
+        resolve(gi, d.kn[0], 1, 0, si, xs);
+        if (T::HAS_Y) resolve(gj, d.kn[1], 1, 0, sj, ys);
         AxisGeo g[3];
-        g[0] = d.geo[0][si + d.goff[0]];
-        if (T::ND >= 2) g[1] = d.geo[1][sj + d.goff[1]];
-        if (T::ND == 3) g[2] = gz;
-        const int box = (T::ND >= 2 ? (ry + 1) * T::BX : 0) + rx + 1;
+        g[0] = d.kgeo[0][si + d.kgoff[0]];
+        if (T::HAS_Y) g[1] = d.kgeo[1][sj + d.kgoff[1]];
+        if (T::MARCH) g[T::AZ] = gz;
+        const int box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
         float eps2 = 0.0f;
         if (mp.limiter == TS_LIM_VENKATAKRISHNAN && mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
-            // eps^2 = (K (hx hy hz)^(1/nd))^3 with K = 5 (Limiters.h:93-96, Constants.h:11)
+            // eps^2 = (K (h1 ... hnd)^(1/nd))^3 with K = 5 (Limiters.h:93-96, Constants.h:11)
             float vol = g[0].h;
-            if (T::ND >= 2) vol *= g[1].h;
-            if (T::ND == 3) vol *= g[2].h;
-            eps2 = 125.0f * (T::ND == 3 ? vol : (T::ND == 2 ? vol * sqrtf(vol) : vol * vol * vol));
+#pragma unroll
+            for (int ax = 1; ax < T::NAX; ++ax) vol *= g[ax].h;
+            eps2 = 125.0f * (T::NAX == 3 ? vol : (T::NAX == 2 ? vol * sqrtf(vol) : vol * vol * vol));
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
@@ -428,23 +447,23 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
             float nm[3], np[3];
             nm[0] = sm[T::w(ws, v, box - 1)];
             np[0] = sm[T::w(ws, v, box + 1)];
-            if (T::ND >= 2) { nm[1] = sm[T::w(ws, v, box - T::BX)]; np[1] = sm[T::w(ws, v, box + T::BX)]; }
-            if (T::ND == 3) { nm[2] = sm[T::w(wd, v, box)]; np[2] = sm[T::w(wu, v, box)]; }
+            if (T::HAS_Y) { nm[1] = sm[T::w(ws, v, box - T::BX)]; np[1] = sm[T::w(ws, v, box + T::BX)]; }
+            if (T::MARCH) { nm[T::AZ] = sm[T::w(wd, v, box)]; np[T::AZ] = sm[T::w(wu, v, box)]; }
             float dd[3];
             if (mp.recon == TS_RECON_ENO2_2POINTS) {
 #pragma unroll
-                for (int ax = 0; ax < T::ND; ++ax) {
+                for (int ax = 0; ax < T::NAX; ++ax) {
                     const float gl = (w0 - nm[ax]) * g[ax].il, gr = (np[ax] - w0) * g[ax].ir;
                     dd[ax] = (fabsf(gl) < fabsf(gr) ? gl : gr) * g[ax].hh;
                 }
             } else {
 #pragma unroll
-                for (int ax = 0; ax < T::ND; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
+                for (int ax = 0; ax < T::NAX; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
             }
             if (mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
                 float umax = w0, umin = w0;
 #pragma unroll
-                for (int ax = 0; ax < T::ND; ++ax) {
+                for (int ax = 0; ax < T::NAX; ++ax) {
                     umax = fmaxf(umax, fmaxf(nm[ax], np[ax]));
                     umin = fminf(umin, fminf(nm[ax], np[ax]));
                 }
@@ -454,7 +473,7 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
                         // Limiters.h:86-115, per face projection +-dd
                         const float iun = 2.0f / (umax - umin);
 #pragma unroll
-                        for (int ax = 0; ax < T::ND; ++ax) {
+                        for (int ax = 0; ax < T::NAX; ++ax) {
 #pragma unroll
                             for (int sg = 0; sg < 2; ++sg) {
                                 const float d2 = sg ? -dd[ax] : dd[ax];
@@ -471,79 +490,87 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
                         // ratio over the 2*nd face projections +-dd.
                         float dmax = 0.0f;
 #pragma unroll
-                        for (int ax = 0; ax < T::ND; ++ax) dmax = fmaxf(dmax, fabsf(dd[ax]));
+                        for (int ax = 0; ax < T::NAX; ++ax) dmax = fmaxf(dmax, fabsf(dd[ax]));
                         if (dmax > 0.0f) lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
                     }
                 }
 #pragma unroll
-                for (int ax = 0; ax < T::ND; ++ax) dd[ax] *= lim;
+                for (int ax = 0; ax < T::NAX; ++ax) dd[ax] *= lim;
             }
 #pragma unroll
-            for (int ax = 0; ax < T::ND; ++ax) sm[T::d(ds, ax, v, t)] = dd[ax];
+            for (int ax = 0; ax < T::NAX; ++ax) sm[T::d(ds, ax, v, t)] = dd[ax];
         }
     }
 }
 
-// The faces of plane z this thread computes: k = 0 x face left of its cell,
-// 1 y face below, 2 z face above (between z and z+1), 3 one far face of the
-// tile (x face TX for threads < TY, y face TY for the next TX threads).
+// The faces of plane z this thread computes: k = 0 the face on kernel axis 0
+// left of its cell, 1 the face on kernel axis 1 below it, 2 the face on the
+// marching axis above it (between z and z+1), 3 one far face of a two-axis
+// tile (axis-0 face TX for threads < TY, axis-1 face TY for the next TX
+// threads).  In one-row tiles thread TX computes the far axis-0 face.
 template <class T, int SOLVER>
 __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int j0, int z, bool pwc, bool do_xy,
                                        bool do_z) {
-    const Layout& L = d.L;
     const int tid = threadIdx.x;
-    const int tx = tid % T::TX, ty = tid / T::TX;
-    const int ws = T::ND == 3 ? wslot(z) : 0, ds = T::ND == 3 ? dslot(z) : 0;
+    const int tx = T::HAS_Y ? tid % T::TX : tid, ty = T::HAS_Y ? tid / T::TX : 0;
+    const int ws = T::MARCH ? wslot(z) : 0, ds = T::MARCH ? dslot(z) : 0;
 #pragma unroll 1
     for (int k = 0; k < 4; ++k) {
         int axis, fx, fy;
-        if (k == 0) { if (!do_xy) continue; axis = 0; fx = tx; fy = ty; }
-        else if (k == 1) { if (!do_xy || T::ND < 2) continue; axis = 1; fx = tx; fy = ty; }
-        else if (k == 2) { if (!do_z || T::ND < 3) continue; axis = 2; fx = tx; fy = ty; }
-        else {
-            if (!do_xy) continue;
+        if (k == 0) {
+            if (!do_xy || (!T::HAS_Y && tx > T::TX)) continue;
+            axis = 0; fx = tx; fy = ty;
+        } else if (k == 1) {
+            if (!do_xy || !T::HAS_Y) continue;
+            axis = 1; fx = tx; fy = ty;
+        } else if (k == 2) {
+            if (!do_z || !T::MARCH || (!T::HAS_Y && tx >= T::TX)) continue;
+            axis = 2; fx = tx; fy = ty;
+        } else {
+            if (!do_xy || !T::HAS_Y) continue;
             if (tid < T::TY) { axis = 0; fx = T::TX; fy = tid; }
-            else if (T::ND >= 2 && tid < T::TY + T::TX) { axis = 1; fx = tid - T::TY; fy = T::TY; }
+            else if (tid < T::TY + T::TX) { axis = 1; fx = tid - T::TY; fy = T::TY; }
             else continue;
         }
         const int gi = i0 + fx, gj = j0 + fy;
-        int bl, br, rl, rr, wl = ws, wr = ws, dl = ds, dr = ds, g, n, per, out;
+        int bl, br, rl, rr, wl = ws, wr = ws, dl = ds, dr = ds, g, n, per, out, sa;
         if (axis == 0) {
-            if (gi > L.nx || gj >= L.ny) continue;
-            bl = (T::ND >= 2 ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
-            rl = (T::ND >= 2 ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
-            g = gi; n = L.nx; per = d.mp.periodic[0];
+            if (gi > d.kn[0] || gj >= d.kn[1]) continue;
+            bl = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
+            rl = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
+            g = gi; n = d.kn[0]; per = d.kper[0]; sa = 0;
             out = T::fx(0, fy, fx);
         } else if (axis == 1) {
-            if (gi >= L.nx || gj > L.ny) continue;
+            if (gi >= d.kn[0] || gj > d.kn[1]) continue;
             bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
             rl = fy * T::RX + fx + 1; rr = rl + T::RX;
-            g = gj; n = L.ny; per = d.mp.periodic[1];
+            g = gj; n = d.kn[1]; per = d.kper[1]; sa = 1;
             out = T::fy(0, fy, fx);
         } else {
-            if (gi >= L.nx || gj >= L.ny) continue;
-            bl = br = (fy + HB) * T::BX + fx + HB;
-            rl = rr = (fy + 1) * T::RX + fx + 1;
+            if (gi >= d.kn[0] || gj >= d.kn[1]) continue;
+            bl = br = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + HB;
+            rl = rr = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx + 1;
             wr = wslot(z + 1); dr = dslot(z + 1);
-            g = z + 1; n = L.nz; per = d.mp.periodic[2];
+            g = z + 1; n = d.kn[2]; per = d.kper[2]; sa = T::AZ;
             out = T::fz(dslot(z + 1), 0, fy, fx);
         }
+        const int A = d.kphys[axis];
         float UL[NV], UR[NV], F[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, axis, v, rl)]);
-            UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, axis, v, rr)]);
+            UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, sa, v, rl)]);
+            UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, sa, v, rr)]);
         }
         if (g == 0 && !per) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) UL[v] = UR[v];
-            bc32(d.mp, 2 * axis, axis, UL);
+            bc32(d.mp, 2 * A, A, UL);
         } else if (g == n && !per) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) UR[v] = UL[v];
-            bc32(d.mp, 2 * axis + 1, axis, UR);
+            bc32(d.mp, 2 * A + 1, A, UR);
         }
-        const float lam = flux32<SOLVER>(d.mp, axis, UL, UR, F);
+        const float lam = flux32<SOLVER>(d.mp, A, UL, UR, F);
         // the v-stride of each flux array is its plane of faces
         const int vs = axis == 0 ? T::TY * (T::TX + 1) : (axis == 1 ? (T::TY + 1) * T::TX : T::TY * T::TX);
 #pragma unroll
@@ -556,11 +583,11 @@ __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int
 template <class T>
 __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
                                          int z, float& srmax) {
-    const Layout& L = d.L;
-    const int tx = threadIdx.x % T::TX, ty = threadIdx.x / T::TX;
+    int tx, ty;
+    if (!T::cell(threadIdx.x, tx, ty)) return;
     const int gi = i0 + tx, gj = j0 + ty;
-    if (gi >= L.nx || gj >= L.ny) return;
-    const AxisGeo gx = d.geo[0][gi + d.goff[0]], gy = d.geo[1][gj + d.goff[1]], gz = d.geo[2][z + d.goff[2]];
+    if (gi >= d.kn[0] || gj >= d.kn[1]) return;
+    const AxisGeo gx = d.kgeo[0][gi + d.kgoff[0]], gy = d.kgeo[1][gj + d.kgoff[1]], gz = d.kgeo[2][z + d.kgoff[2]];
     const float fsx = gy.h * gz.h, fsy = gx.h * gz.h, fsz = gx.h * gy.h;
     const float iv = gx.ih * gy.ih * gz.ih;
     float R[NV];
@@ -568,26 +595,27 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
 #pragma unroll
     for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * fsx;
     float sr = fsx * (lxl + lxr);
-    if (gi == L.nx - 1) srmax = fmaxf(srmax, fsx * lxr * d.geo[0][L.nx + d.goff[0]].ih * gy.ih * gz.ih);
-    if (T::ND >= 2) {
+    if (gi == d.kn[0] - 1) srmax = fmaxf(srmax, fsx * lxr * d.kgeo[0][d.kn[0] + d.kgoff[0]].ih * gy.ih * gz.ih);
+    if (T::HAS_Y) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * fsy;
         const float lyr = sm[T::fy(5, ty + 1, tx)];
         sr += fsy * (sm[T::fy(5, ty, tx)] + lyr);
-        if (gj == L.ny - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * d.geo[1][L.ny + d.goff[1]].ih * gz.ih);
+        if (gj == d.kn[1] - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * d.kgeo[1][d.kn[1] + d.kgoff[1]].ih * gz.ih);
     }
-    if (T::ND == 3) {
+    if (T::MARCH) {
         const int dn = dslot(z), up = dslot(z + 1);
 #pragma unroll
         for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * fsz;
         const float lzr = sm[T::fz(up, 5, ty, tx)];
         sr += fsz * (sm[T::fz(dn, 5, ty, tx)] + lzr);
-        if (z == L.nz - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * d.geo[2][L.nz + d.goff[2]].ih);
+        if (z == d.kn[2] - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * d.kgeo[2][d.kn[2] + d.kgoff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
-    const long long c = L.at(gi, gj, z);
+    const long long c = d.kbase + gi + gj * d.kstr[1] + z * d.kstr[2];
+    const long long plane = d.L.plane;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) __stcg(Rout + v * L.plane + c, R[v]);
+    for (int v = 0; v < NV; ++v) __stcg(Rout + v * plane + c, R[v]);
 }
 
 // dt of one problem from its CFL maximum, and the step's bookkeeping
@@ -617,11 +645,10 @@ __device__ void finish_problem(Ctl* ctl, double cfl) {
 // The fused step kernel
 // ---------------------------------------------------------------------------
 
-// One work item (tile column and z chunk q of problem d).
+// One work item (tile column and chunk q of problem d).
 template <class T, int SOLVER>
 __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm, BoxPos (&bp)[T::NA],
                                              Prefetch (&pf)[T::NA], float& srmax, unsigned int& health) {
-    const Layout& L = d.L;
     const int par = d.ctl->parity;
     const double* __restrict__ Uin = d.U[par];
     double* __restrict__ Uout = d.U[par ^ 1];
@@ -632,7 +659,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm
     const int col = q % d.ncol;
     const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
     setup_box<T>(d, i0, j0, bp);
-    if (T::ND < 3) {
+    if (!T::MARCH) {
         issue<T>(d, Uin, Rin, 0, bp, pf);
         store<T>(d, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
         __syncthreads();
@@ -641,9 +668,9 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm
         __syncthreads();
         residual<T>(d, sm, Rout, i0, j0, 0, srmax);
     } else {
-        const int z0 = (q / d.ncol) * d.ch, z1 = min(L.nz, z0 + d.ch);
+        const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
-        // build the slopes of planes z0-1, z0 and the z face z0-1/2.
+        // build the slopes of planes z0-1, z0 and the marching face z0-1/2.
         issue<T>(d, Uin, Rin, z0 - 2, bp, pf);
         store<T>(d, sm, Uout, z0 - 2, z0, z1, dtf, bp, pf, health);
         issue<T>(d, Uin, Rin, z0 - 1, bp, pf);
@@ -669,15 +696,18 @@ template <class T>
 __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsigned int health, float* wmax,
                                            unsigned int* whealth) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) srmax = fmaxf(srmax, __shfl_xor_sync(0xffffffffu, srmax, o));
-    health = __reduce_or_sync(0xffffffffu, health);
-    if (lane == 0) { wmax[wid] = srmax; whealth[wid] = health; }
+    // the last warp of a block whose size is not a multiple of 32 is partial
+    const int live = min(32, T::NT - (threadIdx.x & ~31));
+    const unsigned int mask = live == 32 ? 0xffffffffu : ((1u << live) - 1u);
+    // srmax >= 0: its bits order like unsigned integers
+    const unsigned int mbits = __reduce_max_sync(mask, __float_as_uint(srmax));
+    health = __reduce_or_sync(mask, health);
+    if (lane == 0) { wmax[wid] = __uint_as_float(mbits); whealth[wid] = health; }
     __syncthreads();
     if (threadIdx.x == 0) {
         float m = 0.0f;
         unsigned int hh = 0;
-        for (int k = 0; k < T::NT / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
+        for (int k = 0; k < (T::NT + 31) / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
         Ctl* ctl = d.ctl;
         if (m > 0.0f) atomicMax(&ctl->srmax_bits, __float_as_uint(m));
         if (hh) atomicOr(&ctl->health, hh);
@@ -691,7 +721,10 @@ __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsig
 
 // BATCH = false: one problem whose descriptor is a kernel parameter (constant
 // bank: every field is a free operand).  BATCH = true: a list of (problem,
-// item) pairs; each item's descriptor is staged in shared memory.
+// item) pairs; the descriptor is staged in shared memory when the problem
+// changes from one item of the CTA to the next.  A problem's stop flag only
+// changes when its last item of the launch closes, so it is read once per
+// problem.
 template <class T, int SOLVER, bool BATCH>
 __global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ ProbDesc one,
                                                     const ProbDesc* __restrict__ probs,
@@ -714,13 +747,17 @@ __global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ Prob
         __shared__ ProbDesc sd;
         __shared__ int s_skip;
         const int nwords = (int)(sizeof(ProbDesc) / sizeof(int));
+        int cur = -1;
         for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
             const int2 pq = items[it];
             __syncthreads();  // the previous item is finished with shared memory
-            for (int k = threadIdx.x; k < nwords; k += T::NT) ((int*)&sd)[k] = ((const int*)(probs + pq.x))[k];
-            __syncthreads();
-            if (threadIdx.x == 0) s_skip = *(volatile int*)&sd.ctl->stop_req;
-            __syncthreads();
+            if (pq.x != cur) {
+                for (int k = threadIdx.x; k < nwords; k += T::NT) ((int*)&sd)[k] = ((const int*)(probs + pq.x))[k];
+                __syncthreads();
+                if (threadIdx.x == 0) s_skip = *(volatile int*)&sd.ctl->stop_req;
+                __syncthreads();
+                cur = pq.x;
+            }
             if (s_skip) continue;
             float srmax = 0.0f;
             unsigned int health = 0;
@@ -731,7 +768,8 @@ __global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ Prob
 }
 
 // U[parity] += dt R[parity] / V, R[parity] = 0 for problem p (materialise the
-// pending update with the fused kernel's own rounding: (1/hx hy) (dt / hz)).
+// pending update with the fused kernel's own rounding: (1/h0 h1) (dt / h2)
+// over kernel axes).
 __global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
     const ProbDesc& d = probs[p];
     const Layout& L = d.L;
@@ -740,9 +778,11 @@ __global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
     if (t >= n) return;
     const int i = (int)(t % L.nx), j = (int)((t / L.nx) % L.ny), k = (int)(t / ((long long)L.nx * L.ny));
     const long long c = L.at(i, j, k);
+    const int a1 = L.nd == 3 ? j : 0, a2 = L.nd == 3 ? k : (L.nd == 2 ? j : 0);
     const int par = d.ctl->parity;
     const float dtf = f64_to_f32(d.ctl->dt_apply);
-    const float cf = (d.geo[0][i + d.goff[0]].ih * d.geo[1][j + d.goff[1]].ih) * (dtf * d.geo[2][k + d.goff[2]].ih);
+    const float cf = (d.kgeo[0][i + d.kgoff[0]].ih * d.kgeo[1][a1 + d.kgoff[1]].ih) *
+                     (dtf * d.kgeo[2][a2 + d.kgoff[2]].ih);
     double* U = d.U[par];
     float* R = d.R[par];
 #pragma unroll
@@ -754,21 +794,26 @@ __global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
 
 __global__ void k_mix_clear_pending(const ProbDesc* __restrict__ probs, int p) { probs[p].ctl->dt_apply = 0.0; }
 
-// Tile shapes compiled per dimension (one thread per tile cell).
+// Compiled tiles: (problem dimension, threads along x, threads along y).
+// 3D: two-axis tiles marching z.  2D: one-row tiles marching y.  1D: one-row
+// tiles, one plane.
 #define TS_MIXED_TILES_3D(X) X(3, 32, 8) X(3, 16, 16) X(3, 64, 4)
-#define TS_MIXED_TILES_2D(X) X(2, 32, 8) X(2, 16, 16)
-#define TS_MIXED_TILES_1D(X) X(1, 256, 1) X(1, 128, 1)
+#define TS_MIXED_TILES_2D(X) X(2, 260, 1) X(2, 132, 1) X(2, 68, 1)
+#define TS_MIXED_TILES_1D(X) X(1, 512, 1) X(1, 256, 1) X(1, 128, 1)
+
+template <int ND, int TX, int TY>
+using TileFor = Tile<TX, (ND == 3 ? TY : 1), (ND >= 2)>;
 
 // Calls f.template operator()<Tile, SOLVER>() for the compiled tile matching
 // (nd, tx, ty); returns false when there is none.
 template <class F>
 bool with_tile(int nd, int tx, int ty, int solver, F&& f) {
     bool found = false;
-#define TS_TRY(ND_, TX_, TY_)                                                                     \
-    if (!found && nd == ND_ && tx == TX_ && (ND_ == 1 || ty == TY_)) {                           \
-        found = true;                                                                            \
-        if (solver == TS_RS_HLLC) f.template operator()<Tile<ND_, TX_, TY_>, TS_RS_HLLC>();      \
-        else f.template operator()<Tile<ND_, TX_, TY_>, TS_RS_ROE_PIKE>();                       \
+#define TS_TRY(ND_, TX_, TY_)                                                                           \
+    if (!found && nd == ND_ && tx == TX_ && (ND_ < 3 || ty == TY_)) {                                  \
+        found = true;                                                                                  \
+        if (solver == TS_RS_HLLC) f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_HLLC>();         \
+        else f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_ROE_PIKE>();                          \
     }
     TS_MIXED_TILES_3D(TS_TRY)
     TS_MIXED_TILES_2D(TS_TRY)
@@ -786,11 +831,11 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
         const int b = (int)T::BYTES;
         bool ok = cudaFuncSetAttribute(k_mix_step<T, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                   cudaSuccess;
-        if constexpr (T::ND < 3)
+        if constexpr (!T::HAS_Y)
             ok = ok && cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                            cudaSuccess;
         if (!ok) return;
-        if constexpr (T::ND < 3) {
+        if constexpr (!T::HAS_Y) {
             if (batch) {
                 cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, true>, T::NT, T::BYTES);
                 return;
@@ -814,18 +859,26 @@ bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const Prob
     ProbDesc none;
     std::memset(&none, 0, sizeof none);
     return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
-        if constexpr (T::ND < 3)
+        if constexpr (!T::HAS_Y)
             k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_items, n_items);
     });
 }
 
+void mixed_tile_cells(int nd, int tx, int ty, int* cx, int* cy) {
+    *cx = nd == 3 ? tx : tx - 2 * HB;
+    *cy = nd == 3 ? ty : 1;
+}
+
 void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots) {
     const int nd = d.L.nd;
-    d.ncx = (d.L.nx + tx - 1) / tx;
-    const int ncy = nd >= 2 ? (d.L.ny + ty - 1) / ty : 1;
+    int cx, cy;
+    mixed_tile_cells(nd, tx, ty, &cx, &cy);
+    d.ncx = (d.kn[0] + cx - 1) / cx;
+    const int ncy = (d.kn[1] + cy - 1) / cy;
     d.ncol = d.ncx * ncy;
-    const int nz = nd == 3 ? d.L.nz : 1;
-    if (nd == 3 && zchunks <= 0) {
+    const bool march = nd >= 2;
+    const int nz = march ? d.kn[2] : 1;
+    if (march && zchunks <= 0) {
         // Chunks of >= 16 planes; pick the count that best fills the
         // persistent grid, charging ~2 planes of start-up per chunk.
         double best = -1.0;
@@ -838,14 +891,14 @@ void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots) {
             if (score > best + 1e-9) { best = score; zchunks = c; }
         }
     }
-    zchunks = nd == 3 ? std::max(1, std::min(zchunks, nz)) : 1;
-    d.ch = nd == 3 ? (nz + zchunks - 1) / zchunks : 1;
+    zchunks = march ? std::max(1, std::min(zchunks, nz)) : 1;
+    d.ch = march ? (nz + zchunks - 1) / zchunks : 1;
     d.nq = d.ncol * ((nz + d.ch - 1) / d.ch);
 }
 
 ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err) {
     const int nd = mb.desc.L.nd;
-    if (nd == 1) ty = 1;
+    if (nd < 3) ty = 1;
     size_t bytes = 0;
     int per_sm = 0;
     if (!mixed_tile_info(nd, tx, ty, mb.desc.mp.solver, &bytes, &per_sm)) {
@@ -858,7 +911,7 @@ ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string
     mb.smem = bytes;
     const long long slots = (long long)mb.sms * per_sm;
     mixed_items(mb.desc, tx, ty, zchunks, slots);
-    mb.zchunks = nd == 3 ? (mb.desc.L.nz + mb.desc.ch - 1) / mb.desc.ch : 1;
+    mb.zchunks = nd >= 2 ? (mb.desc.kn[2] + mb.desc.ch - 1) / mb.desc.ch : 1;
     mb.grid = (int)std::min<long long>(mb.desc.nq, slots);
     if (cudaMemcpy(mb.d_desc, &mb.desc, sizeof(ProbDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
         err = "descriptor upload failed";
@@ -872,7 +925,8 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
     if (L.plane > (1LL << 31) - 1) { err = "grid too large for the mixed path"; return TS_ERR_INVALID; }
     d.L = L;
     d.ctl = ctl;
-    d.goff[0] = L.gx; d.goff[1] = L.gy; d.goff[2] = L.gz;
+    const AxisGeo* axis_geo[3];
+    const int goff[3] = {L.gx, L.gy, L.gz};
     ts_status s;
     // per-axis geometry with ghost entries on active axes
     for (int a = 0; a < 3; ++a) {
@@ -912,8 +966,20 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
             err = "geometry upload failed";
             return TS_ERR_CUDA;
         }
-        d.geo[a] = (const AxisGeo*)p;
+        axis_geo[a] = (const AxisGeo*)p;
     }
+    // kernel axes: x, the tile's second axis, the marching axis
+    // (3D: x, y, z; 2D: x, inactive z, y; 1D: x, inactive y, inactive z)
+    const int map[3] = {0, L.nd == 2 ? 2 : 1, L.nd == 2 ? 1 : 2};
+    for (int a = 0; a < 3; ++a) {
+        d.kgeo[a] = axis_geo[map[a]];
+        d.kgoff[a] = goff[map[a]];
+        d.kn[a] = L.n(map[a]);
+        d.kper[a] = ph.periodic[map[a]];
+        d.kphys[a] = map[a];
+        d.kstr[a] = L.stride(map[a]);
+    }
+    d.kbase = L.at(0, 0, 0);
     MixPhys& m = d.mp;
     std::memset(&m, 0, sizeof m);
     m.nd = L.nd;
@@ -963,8 +1029,8 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&mb.sms, cudaDevAttrMultiProcessorCount, dev);
-    const int tx = L.nd == 1 ? 256 : 32;
-    const int ty = L.nd == 1 ? 1 : 8;
+    const int tx = L.nd == 3 ? 32 : (L.nd == 2 ? 260 : 256);
+    const int ty = L.nd == 3 ? 8 : 1;
     return mixed_set_tile(mb, tx, ty, 0, err);
 }
 
@@ -1133,3 +1199,4 @@ extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* stat
     }
     return TS_OK;
 }
+

@@ -36,16 +36,24 @@ struct MixPhys {
 };
 
 // Everything the fused kernel needs about one problem (lives in device memory).
+// The kernel works on kernel axes 0 (x), 1 (the tile's second axis, 3D
+// only) and 2 (the marching axis: z in 3D, y in 2D); the k* fields map them
+// to the problem's axes.  Inactive kernel axes have one cell.
 struct ProbDesc {
     Layout L;
     double* U[2];          // NV FP64 planes each: U^n and U^{n+1}
     float* R[2];           // NV FP32 planes each: pending residual
-    const AxisGeo* geo[3];
-    int goff[3];           // ghost offset into geo per axis
     Ctl* ctl;              // per-problem step control word
+    const AxisGeo* kgeo[3];  // geometry per kernel axis, indexed cell + kgoff
+    int kgoff[3];
+    int kn[3];             // cells along each kernel axis
+    int kper[3];           // periodic
+    int kphys[3];          // problem axis (momentum component; BC sides 2a, 2a+1)
+    long long kstr[3];     // element strides
+    long long kbase;       // element offset of cell (0, 0, 0)
     MixPhys mp;
     int ncx, ncol;         // tile columns along x, in total
-    int ch, nq;            // planes per z chunk, work items (columns x chunks)
+    int ch, nq;            // planes per marching chunk, work items (columns x chunks)
 };
 
 struct MixedBufs {
@@ -63,8 +71,11 @@ using DeviceAlloc = std::function<ts_status(size_t bytes, void** out)>;
 // Geometry and physics of one problem (host work + uploads through `alloc`).
 ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                         const DeviceAlloc& alloc, ProbDesc& d, std::string& err);
-// Work items of a problem for a tile and z chunking (0 = automatic, given
-// the persistent grid size `slots`).
+// Cells per tile along x and y of a compiled tile of tx x ty threads (one-row
+// tiles of 1D and 2D problems own tx - 4 cells).
+void mixed_tile_cells(int nd, int tx, int ty, int* cx, int* cy);
+// Work items of a problem for a tile and chunking of the marching axis
+// (0 = automatic, given the persistent grid size `slots`).
 void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots);
 // Compiled tile lookup: smem bytes and resident CTAs per SM (of the batched
 // kernel when `batch`), or false.
