@@ -121,8 +121,8 @@ __device__ __forceinline__ float harten32(float z, float e) {
 __device__ __forceinline__ float pick3(int a, float x, float y, float z) { return a == 0 ? x : (a == 1 ? y : z); }
 
 // ---------------------------------------------------------------------------
-// FP32 Riemann solvers along axis A (a runtime argument: one copy of the
-// solver serves all three face directions).  States carry the shifted energy
+// FP32 Riemann solvers along axis A (a compile-time argument: the normal
+// components fold into register choices).  States carry the shifted energy
 // E' = E - einf, so p = (g-1)(E' - rho |u|^2 / 2) for both equations of state
 // without cancellation; E = E' + einf where the total energy enters.
 // ---------------------------------------------------------------------------
@@ -130,7 +130,8 @@ __device__ __forceinline__ float pick3(int a, float x, float y, float z) { retur
 // Roe-Pike flux (RoeSolverPerfectGasEOS.h:74-160) in the equivalent form
 // 1/2 [F(UL) + F(UR) + |A|(UL - UR)], |A| dU = a1 dU + Ac Qa + Bc Qb with
 // Qa = (0, e_A, un), Qb = (1, u, H), Ac = Ea dR + Eb dD, Bc = Ea dD + Eb dR / c^2.
-__device__ __forceinline__ float roe32(const MixPhys& p, int A, const float UL[NV], const float UR[NV], float F[NV]) {
+template <int A>
+__device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
     const float gm1 = p.gm1;
     const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
     const float ulx = UL[1] * rl, uly = UL[2] * rl, ulz = UL[3] * rl;
@@ -173,7 +174,8 @@ __device__ __forceinline__ float roe32(const MixPhys& p, int A, const float UL[N
 }
 
 // HLLC (Toro ch. 10.4), Einfeldt-type speeds from Roe averages.
-__device__ __forceinline__ float hllc32(const MixPhys& p, int A, const float UL[NV], const float UR[NV],
+template <int A>
+__device__ __forceinline__ float hllc32(const MixPhys& p, const float UL[NV], const float UR[NV],
                                         float F[NV]) {
     const float g = p.gamma, gm1 = p.gm1;
     const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
@@ -218,10 +220,10 @@ __device__ __forceinline__ float hllc32(const MixPhys& p, int A, const float UL[
     return fmaxf(fabsf(SL), fabsf(SR));
 }
 
-template <int SOLVER>
-__device__ __forceinline__ float flux32(const MixPhys& p, int A, const float UL[NV], const float UR[NV], float F[NV]) {
-    if (SOLVER == TS_RS_HLLC) return hllc32(p, A, UL, UR, F);
-    return roe32(p, A, UL, UR, F);
+template <int SOLVER, int A>
+__device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
+    if (SOLVER == TS_RS_HLLC) return hllc32<A>(p, UL, UR, F);
+    return roe32<A>(p, UL, UR, F);
 }
 
 // ---------------------------------------------------------------------------
@@ -262,6 +264,11 @@ struct Tile {
     static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TY * TX : 0);
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
     static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
+    // resident CTAs per SM the register allocation is sized for (about 24-32
+    // warps per SM for one-row tiles; two per SM for the shared-memory-heavy
+    // two-axis tiles)
+    static constexpr int WARPS = (NT + 31) / 32;
+    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : (24 + WARPS - 1) / WARPS);
 
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
     static __device__ __forceinline__ int d(int s, int ax, int v, int ring) {
@@ -279,6 +286,13 @@ struct Tile {
         return tid < TX;
     }
 };
+
+// Problem axis of kernel axis AX: fixed by the tile kind (3D two-axis tiles:
+// x, y, z; one-row marching tiles serve 2D problems: x, -, y; 1D: x).
+template <class T, int AX>
+__device__ __forceinline__ constexpr int phys_axis() {
+    return AX == 0 ? 0 : (AX == 1 ? 1 : (T::HAS_Y ? 2 : 1));
+}
 
 __device__ __forceinline__ int wslot(int p) { return (p + 3) % 3; }
 __device__ __forceinline__ int dslot(int p) { return (p + 2) & 1; }
@@ -380,8 +394,8 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
         w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf[k].u[4] - mp.einf_d) : f64_to_f32(pf[k].u[4])) +
                inc[4];
         if (bp[k].xs >= 0) bc32(mp, bp[k].xs, 0, w);
-        if (T::HAS_Y && bp[k].ys >= 0) bc32(mp, bp[k].ys, bp[k].ys >> 1, w);
-        if (T::MARCH && zs >= 0) bc32(mp, zs, zs >> 1, w);
+        if (T::HAS_Y && bp[k].ys >= 0) bc32(mp, bp[k].ys, 1, w);
+        if (T::MARCH && zs >= 0) bc32(mp, zs, phys_axis<T, 2>(), w);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp[k].box)] = w[v];
         if (own_plane && bp[k].own) {
@@ -398,24 +412,39 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
     }
 }
 
-// Limited half-slopes of plane p on the tile and its 1-cell ring (corners
-// excluded); ring cells outside a non-periodic boundary are not needed.
+// Ring slots of the marching planes around plane p (working state: p-1, p,
+// p+1; slopes: p, p+1), computed once per plane.
+struct Slots {
+    int wm, w0, wp;  // working-state slots of planes p-1, p, p+1
+    int d0, d1;      // slope slots of planes p, p+1
+};
+
 template <class T>
-__device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int j0, int p) {
-    const MixPhys& mp = d.mp;
-    int sk = 0, zs;
+__device__ __forceinline__ Slots slots_of(int p) {
+    Slots s;
     if (T::MARCH) {
-        if ((p < 0 || p >= d.kn[2]) && !d.kper[2]) return;
-        resolve(p, d.kn[2], 1, 0, sk, zs);
+        s.wm = wslot(p - 1); s.w0 = wslot(p); s.wp = wslot(p + 1);
+        s.d0 = dslot(p); s.d1 = dslot(p + 1);
+    } else {
+        s.wm = s.w0 = s.wp = 0;
+        s.d0 = s.d1 = 0;
     }
-    const int ws = T::MARCH ? wslot(p) : 0;
-    const int wd = T::MARCH ? wslot(p - 1) : 0, wu = T::MARCH ? wslot(p + 1) : 0;
-    const int ds = T::MARCH ? dslot(p) : 0;
-    AxisGeo gz;
-    if (T::MARCH) gz = d.kgeo[2][sk + d.kgoff[2]];
+    return s;
+}
+
+// One reconstruction position of a thread for the current item: its ring
+// index, box index and geometry entries (fixed while the item marches).
+struct RingPos {
+    int box;      // box index of the cell; -1: nothing to do
+    int g0, g1;   // geometry indices along kernel axes 0 and 1
+};
+
+template <class T>
+__device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, int j0, RingPos (&rp)[T::NB]) {
 #pragma unroll
     for (int k = 0; k < T::NB; ++k) {
         const int t = threadIdx.x + k * T::NT;
+        rp[k].box = -1;
         if (t >= T::NRING) continue;
         const int rx = t % T::RX, ry = t / T::RX;
         const bool ox = rx < 1 || rx > T::TX;
@@ -428,13 +457,47 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
         int si, sj = 0, xs, ys;
         resolve(gi, d.kn[0], 1, 0, si, xs);
         if (T::HAS_Y) resolve(gj, d.kn[1], 1, 0, sj, ys);
+        rp[k].box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
+        rp[k].g0 = si + d.kgoff[0];
+        rp[k].g1 = sj + d.kgoff[1];
+    }
+}
+
+// Reconstruction kinds (the limiter choice folded in).
+enum { RK_LINEAR = 1, RK_ENO2 = 2, RK_LIM_BJ = 3, RK_LIM_VK = 4 };
+
+__host__ __device__ __forceinline__ int recon_kind(const MixPhys& mp) {
+    if (mp.recon == TS_RECON_LINEAR_2POINTS) return RK_LINEAR;
+    if (mp.recon == TS_RECON_ENO2_2POINTS) return RK_ENO2;
+    if (mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED)
+        return mp.limiter == TS_LIM_VENKATAKRISHNAN ? RK_LIM_VK : RK_LIM_BJ;
+    return 0;
+}
+
+// Limited half-slopes of plane p on the tile and its 1-cell ring (corners
+// excluded); ring cells outside a non-periodic boundary are not needed.
+template <class T, int KIND>
+__device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, const Slots& s,
+                                        const RingPos (&rp)[T::NB]) {
+    int sk = 0;
+    if (T::MARCH) {
+        if ((p < 0 || p >= d.kn[2]) && !d.kper[2]) return;
+        int zs;
+        resolve(p, d.kn[2], 1, 0, sk, zs);
+    }
+    AxisGeo gz;
+    if (T::MARCH) gz = d.kgeo[2][sk + d.kgoff[2]];
+#pragma unroll
+    for (int k = 0; k < T::NB; ++k) {
+        if (rp[k].box < 0) continue;
+        const int t = threadIdx.x + k * T::NT;
+        const int box = rp[k].box;
         AxisGeo g[3];
-        g[0] = d.kgeo[0][si + d.kgoff[0]];
-        if (T::HAS_Y) g[1] = d.kgeo[1][sj + d.kgoff[1]];
+        g[0] = d.kgeo[0][rp[k].g0];
+        if (T::HAS_Y) g[1] = d.kgeo[1][rp[k].g1];
         if (T::MARCH) g[T::AZ] = gz;
-        const int box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
         float eps2 = 0.0f;
-        if (mp.limiter == TS_LIM_VENKATAKRISHNAN && mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
+        if (KIND == RK_LIM_VK) {
             // eps^2 = (K (h1 ... hnd)^(1/nd))^3 with K = 5 (Limiters.h:93-96, Constants.h:11)
             float vol = g[0].h;
 #pragma unroll
@@ -443,14 +506,14 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            const float w0 = sm[T::w(ws, v, box)];
+            const float w0 = sm[T::w(s.w0, v, box)];
             float nm[3], np[3];
-            nm[0] = sm[T::w(ws, v, box - 1)];
-            np[0] = sm[T::w(ws, v, box + 1)];
-            if (T::HAS_Y) { nm[1] = sm[T::w(ws, v, box - T::BX)]; np[1] = sm[T::w(ws, v, box + T::BX)]; }
-            if (T::MARCH) { nm[T::AZ] = sm[T::w(wd, v, box)]; np[T::AZ] = sm[T::w(wu, v, box)]; }
+            nm[0] = sm[T::w(s.w0, v, box - 1)];
+            np[0] = sm[T::w(s.w0, v, box + 1)];
+            if (T::HAS_Y) { nm[1] = sm[T::w(s.w0, v, box - T::BX)]; np[1] = sm[T::w(s.w0, v, box + T::BX)]; }
+            if (T::MARCH) { nm[T::AZ] = sm[T::w(s.wm, v, box)]; np[T::AZ] = sm[T::w(s.wp, v, box)]; }
             float dd[3];
-            if (mp.recon == TS_RECON_ENO2_2POINTS) {
+            if (KIND == RK_ENO2) {
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) {
                     const float gl = (w0 - nm[ax]) * g[ax].il, gr = (np[ax] - w0) * g[ax].ir;
@@ -460,7 +523,7 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
             }
-            if (mp.recon == TS_RECON_LINEAR_2POINTS_LIMITED) {
+            if (KIND == RK_LIM_BJ || KIND == RK_LIM_VK) {
                 float umax = w0, umin = w0;
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) {
@@ -469,7 +532,7 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
                 }
                 float lim = 1.0f;
                 if (umax - umin > 0.0f) {
-                    if (mp.limiter == TS_LIM_VENKATAKRISHNAN) {
+                    if (KIND == RK_LIM_VK) {
                         // Limiters.h:86-115, per face projection +-dd
                         const float iun = 2.0f / (umax - umin);
 #pragma unroll
@@ -498,91 +561,107 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int i0, int 
                 for (int ax = 0; ax < T::NAX; ++ax) dd[ax] *= lim;
             }
 #pragma unroll
-            for (int ax = 0; ax < T::NAX; ++ax) sm[T::d(ds, ax, v, t)] = dd[ax];
+            for (int ax = 0; ax < T::NAX; ++ax) sm[T::d(s.d0, ax, v, t)] = dd[ax];
         }
     }
 }
 
-// The faces of plane z this thread computes: k = 0 the face on kernel axis 0
-// left of its cell, 1 the face on kernel axis 1 below it, 2 the face on the
-// marching axis above it (between z and z+1), 3 one far face of a two-axis
-// tile (axis-0 face TX for threads < TY, axis-1 face TY for the next TX
-// threads).  In one-row tiles thread TX computes the far axis-0 face.
+template <class T>
+__device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int p, int kind, const Slots& s,
+                                      const RingPos (&rp)[T::NB]) {
+    switch (kind) {
+    case RK_LINEAR: recon_k<T, RK_LINEAR>(d, sm, p, s, rp); break;
+    case RK_ENO2: recon_k<T, RK_ENO2>(d, sm, p, s, rp); break;
+    case RK_LIM_VK: recon_k<T, RK_LIM_VK>(d, sm, p, s, rp); break;
+    default: recon_k<T, RK_LIM_BJ>(d, sm, p, s, rp); break;
+    }
+}
+
+// One face on kernel axis AX between the cells (fx-1, fy) and (fx, fy) of the
+// tile (AX = 0), (fx, fy-1) and (fx, fy) (AX = 1), or (fx, fy) of planes z and
+// z+1 (AX = 2): face states, boundary image, Riemann flux and eigenvalue into
+// the face array.  s holds the slots of plane z.
+template <class T, int SOLVER, int AX>
+__device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
+                                     const Slots& s, bool pwc) {
+    constexpr int A = phys_axis<T, AX>();
+    constexpr int SA = AX == 0 ? 0 : (AX == 1 ? 1 : T::AZ);
+    int bl, br, rl, rr, g, n, per, out, vs;
+    int wl = s.w0, wr = s.w0, dl = s.d0, dr = s.d0;
+    if (AX == 0) {
+        if (gi > d.kn[0] || gj >= d.kn[1]) return;
+        bl = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
+        rl = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
+        g = gi; n = d.kn[0]; per = d.kper[0];
+        out = T::fx(0, fy, fx); vs = T::TY * (T::TX + 1);
+    } else if (AX == 1) {
+        if (gi >= d.kn[0] || gj > d.kn[1]) return;
+        bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
+        rl = fy * T::RX + fx + 1; rr = rl + T::RX;
+        g = gj; n = d.kn[1]; per = d.kper[1];
+        out = T::fy(0, fy, fx); vs = (T::TY + 1) * T::TX;
+    } else {
+        if (gi >= d.kn[0] || gj >= d.kn[1]) return;
+        bl = br = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + HB;
+        rl = rr = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx + 1;
+        wr = s.wp; dr = s.d1;
+        g = z + 1; n = d.kn[2]; per = d.kper[2];
+        out = T::fz(s.d1, 0, fy, fx); vs = T::TY * T::TX;
+    }
+    float UL[NV], UR[NV], F[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, SA, v, rl)]);
+        UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, SA, v, rr)]);
+    }
+    if (g == 0 && !per) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) UL[v] = UR[v];
+        bc32(d.mp, 2 * A, A, UL);
+    } else if (g == n && !per) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) UR[v] = UL[v];
+        bc32(d.mp, 2 * A + 1, A, UR);
+    }
+    const float lam = flux32<SOLVER, A>(d.mp, UL, UR, F);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) sm[out + v * vs] = F[v];
+    sm[out + NV * vs] = lam;
+}
+
+// The faces of plane z this thread computes: on kernel axis 0 the face left
+// of its cell, on axis 1 the face below it, on the marching axis the face
+// above it (between z and z+1).  The tile's far faces go to the first TY
+// threads (axis 0, face TX) and the next TX threads (axis 1, face TY) of a
+// two-axis tile, and to thread TX of a one-row tile.
 template <class T, int SOLVER>
 __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int j0, int z, bool pwc, bool do_xy,
-                                       bool do_z) {
+                                       bool do_z, const Slots& s) {
     const int tid = threadIdx.x;
     const int tx = T::HAS_Y ? tid % T::TX : tid, ty = T::HAS_Y ? tid / T::TX : 0;
-    const int ws = T::MARCH ? wslot(z) : 0, ds = T::MARCH ? dslot(z) : 0;
+    if (do_xy) {
+        const int reps0 = (T::HAS_Y && tid < T::TY) ? 2 : 1;
 #pragma unroll 1
-    for (int k = 0; k < 4; ++k) {
-        int axis, fx, fy;
-        if (k == 0) {
-            if (!do_xy || (!T::HAS_Y && tx > T::TX)) continue;
-            axis = 0; fx = tx; fy = ty;
-        } else if (k == 1) {
-            if (!do_xy || !T::HAS_Y) continue;
-            axis = 1; fx = tx; fy = ty;
-        } else if (k == 2) {
-            if (!do_z || !T::MARCH || (!T::HAS_Y && tx >= T::TX)) continue;
-            axis = 2; fx = tx; fy = ty;
-        } else {
-            if (!do_xy || !T::HAS_Y) continue;
-            if (tid < T::TY) { axis = 0; fx = T::TX; fy = tid; }
-            else if (tid < T::TY + T::TX) { axis = 1; fx = tid - T::TY; fy = T::TY; }
-            else continue;
+        for (int r = 0; r < reps0; ++r) {
+            const int fx = r ? T::TX : tx, fy = r ? tid : ty;
+            if (T::HAS_Y || fx <= T::TX) face<T, SOLVER, 0>(d, sm, fx, fy, i0 + fx, j0 + fy, z, s, pwc);
         }
-        const int gi = i0 + fx, gj = j0 + fy;
-        int bl, br, rl, rr, wl = ws, wr = ws, dl = ds, dr = ds, g, n, per, out, sa;
-        if (axis == 0) {
-            if (gi > d.kn[0] || gj >= d.kn[1]) continue;
-            bl = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
-            rl = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
-            g = gi; n = d.kn[0]; per = d.kper[0]; sa = 0;
-            out = T::fx(0, fy, fx);
-        } else if (axis == 1) {
-            if (gi >= d.kn[0] || gj > d.kn[1]) continue;
-            bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
-            rl = fy * T::RX + fx + 1; rr = rl + T::RX;
-            g = gj; n = d.kn[1]; per = d.kper[1]; sa = 1;
-            out = T::fy(0, fy, fx);
-        } else {
-            if (gi >= d.kn[0] || gj >= d.kn[1]) continue;
-            bl = br = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + HB;
-            rl = rr = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx + 1;
-            wr = wslot(z + 1); dr = dslot(z + 1);
-            g = z + 1; n = d.kn[2]; per = d.kper[2]; sa = T::AZ;
-            out = T::fz(dslot(z + 1), 0, fy, fx);
+        if (T::HAS_Y) {
+            const int reps1 = (tid >= T::TY && tid < T::TY + T::TX) ? 2 : 1;
+#pragma unroll 1
+            for (int r = 0; r < reps1; ++r) {
+                const int fx = r ? tid - T::TY : tx, fy = r ? T::TY : ty;
+                face<T, SOLVER, 1>(d, sm, fx, fy, i0 + fx, j0 + fy, z, s, pwc);
+            }
         }
-        const int A = d.kphys[axis];
-        float UL[NV], UR[NV], F[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, sa, v, rl)]);
-            UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, sa, v, rr)]);
-        }
-        if (g == 0 && !per) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) UL[v] = UR[v];
-            bc32(d.mp, 2 * A, A, UL);
-        } else if (g == n && !per) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) UR[v] = UL[v];
-            bc32(d.mp, 2 * A + 1, A, UR);
-        }
-        const float lam = flux32<SOLVER>(d.mp, A, UL, UR, F);
-        // the v-stride of each flux array is its plane of faces
-        const int vs = axis == 0 ? T::TY * (T::TX + 1) : (axis == 1 ? (T::TY + 1) * T::TX : T::TY * T::TX);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) sm[out + v * vs] = F[v];
-        sm[out + NV * vs] = lam;
     }
+    if (T::MARCH && do_z && (T::HAS_Y || tx < T::TX)) face<T, SOLVER, 2>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
 }
 
 // Residual and spectral radius of the owned cell of this thread in plane z.
 template <class T>
 __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
-                                         int z, float& srmax) {
+                                         int z, const Slots& s, float& srmax) {
     int tx, ty;
     if (!T::cell(threadIdx.x, tx, ty)) return;
     const int gi = i0 + tx, gj = j0 + ty;
@@ -604,7 +683,7 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
         if (gj == d.kn[1] - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * d.kgeo[1][d.kn[1] + d.kgoff[1]].ih * gz.ih);
     }
     if (T::MARCH) {
-        const int dn = dslot(z), up = dslot(z + 1);
+        const int dn = s.d0, up = s.d1;
 #pragma unroll
         for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * fsz;
         const float lzr = sm[T::fz(up, 5, ty, tx)];
@@ -648,25 +727,29 @@ __device__ void finish_problem(Ctl* ctl, double cfl) {
 // One work item (tile column and chunk q of problem d).
 template <class T, int SOLVER>
 __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm, BoxPos (&bp)[T::NA],
-                                             Prefetch (&pf)[T::NA], float& srmax, unsigned int& health) {
+                                             Prefetch (&pf)[T::NA], RingPos (&rp)[T::NB], float& srmax,
+                                             unsigned int& health) {
     const int par = d.ctl->parity;
     const double* __restrict__ Uin = d.U[par];
     double* __restrict__ Uout = d.U[par ^ 1];
     const float* __restrict__ Rin = d.R[par];
     float* __restrict__ Rout = d.R[par ^ 1];
     const float dtf = f64_to_f32(d.ctl->dt_apply);
-    const bool pwc = d.mp.recon == TS_RECON_PIECEWISE_CONSTANT;
+    const int kind = recon_kind(d.mp);
+    const bool pwc = kind == 0;
     const int col = q % d.ncol;
     const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
     setup_box<T>(d, i0, j0, bp);
+    if (!pwc) setup_ring<T>(d, i0, j0, rp);
     if (!T::MARCH) {
+        const Slots s = slots_of<T>(0);
         issue<T>(d, Uin, Rin, 0, bp, pf);
         store<T>(d, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
         __syncthreads();
-        if (!pwc) { recon<T>(d, sm, i0, j0, 0); __syncthreads(); }
-        fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false);
+        if (!pwc) { recon<T>(d, sm, 0, kind, s, rp); __syncthreads(); }
+        fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false, s);
         __syncthreads();
-        residual<T>(d, sm, Rout, i0, j0, 0, srmax);
+        residual<T>(d, sm, Rout, i0, j0, 0, s, srmax);
     } else {
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
@@ -678,14 +761,15 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm
         issue<T>(d, Uin, Rin, z0, bp, pf);
 #pragma unroll 1
         for (int z = z0 - 2; z < z1; ++z) {
+            const Slots sf = slots_of<T>(z), sr = slots_of<T>(z + 1);
             // plane z+2 was prefetched during the previous pass
             store<T>(d, sm, Uout, z + 2, z0, z1, dtf, bp, pf, health);
             if (z + 3 <= z1 + 1) issue<T>(d, Uin, Rin, z + 3, bp, pf);
             __syncthreads();
-            if (!pwc) { recon<T>(d, sm, i0, j0, z + 1); __syncthreads(); }
-            if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true);
+            if (!pwc) { recon<T>(d, sm, z + 1, kind, sr, rp); __syncthreads(); }
+            if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true, sf);
             __syncthreads();
-            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, srmax);
+            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, sf, srmax);
         }
     }
 }
@@ -726,7 +810,7 @@ __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsig
 // changes when its last item of the launch closes, so it is read once per
 // problem.
 template <class T, int SOLVER, bool BATCH>
-__global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ ProbDesc one,
+__global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_constant__ ProbDesc one,
                                                     const ProbDesc* __restrict__ probs,
                                                     const int2* __restrict__ items, int n_items) {
     extern __shared__ float sm[];
@@ -734,13 +818,14 @@ __global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ Prob
     __shared__ unsigned int whealth[32];
     BoxPos bp[T::NA];
     Prefetch pf[T::NA];
+    RingPos rp[T::NB];
     if constexpr (!BATCH) {
         if (one.ctl->stop_req) return;
         for (int q = blockIdx.x; q < n_items; q += gridDim.x) {
             __syncthreads();  // the previous item is finished with shared memory
             float srmax = 0.0f;
             unsigned int health = 0;
-            process_item<T, SOLVER>(one, q, sm, bp, pf, srmax, health);
+            process_item<T, SOLVER>(one, q, sm, bp, pf, rp, srmax, health);
             close_item<T>(one, srmax, health, wmax, whealth);
         }
     } else {
@@ -761,7 +846,7 @@ __global__ void __launch_bounds__(T::NT) k_mix_step(const __grid_constant__ Prob
             if (s_skip) continue;
             float srmax = 0.0f;
             unsigned int health = 0;
-            process_item<T, SOLVER>(sd, pq.y, sm, bp, pf, srmax, health);
+            process_item<T, SOLVER>(sd, pq.y, sm, bp, pf, rp, srmax, health);
             close_item<T>(sd, srmax, health, wmax, whealth);
         }
     }
@@ -831,6 +916,10 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
         const int b = (int)T::BYTES;
         bool ok = cudaFuncSetAttribute(k_mix_step<T, S, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                   cudaSuccess;
+        // all of the unified L1 / shared storage as shared memory: more resident CTAs
+        cudaFuncSetAttribute(k_mix_step<T, S, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        if constexpr (!T::HAS_Y)
+            cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
         if constexpr (!T::HAS_Y)
             ok = ok && cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
                            cudaSuccess;
