@@ -159,6 +159,13 @@ using namespace ts;
 struct ts_batch {
     int device = 0, sms = 0;
     cudaStream_t stream = nullptr;
+    // groups beyond the first run concurrently on side streams (forked and
+    // joined inside the captured stage graph)
+    static constexpr int kSide = 4;
+    cudaStream_t side[kSide] = {};
+    cudaEvent_t fork = nullptr, join[kSide] = {};
+    int* d_slots = nullptr;   // listed problems (closed by the finish kernel)
+    int slots_cap = 0, n_listed = 0;
     Arena arena;
     std::vector<Slot> slots;
     std::vector<ProbDesc> desc;
@@ -183,6 +190,12 @@ struct ts_batch {
         cudaSetDevice(device);
         drop_graphs();
         for (auto& g : groups) cudaFree(g.d_items);
+        cudaFree(d_slots);
+        for (int k = 0; k < kSide; ++k) {
+            if (side[k]) cudaStreamDestroy(side[k]);
+            if (join[k]) cudaEventDestroy(join[k]);
+        }
+        if (fork) cudaEventDestroy(fork);
         cudaFree(d_desc);
         cudaFree(d_ctl);
         cudaFreeHost(h_ctl);
@@ -286,16 +299,45 @@ struct ts_batch {
         }
         for (auto& og : groups) cudaFree(og.d_items);
         groups.swap(ng);
+        // the listed problems, for the stage's finish kernel
+        std::vector<int> listed;
+        for (auto& kv : bykey) listed.insert(listed.end(), kv.second.begin(), kv.second.end());
+        n_listed = (int)listed.size();
+        if (n_listed > slots_cap) {
+            cudaFree(d_slots);
+            d_slots = nullptr;
+            slots_cap = std::max(2 * slots_cap, std::max(n_listed, 256));
+            TB_CUDA(cudaMalloc(&d_slots, sizeof(int) * slots_cap));
+        }
+        if (n_listed)
+            TB_CUDA(cudaMemcpyAsync(d_slots, listed.data(), sizeof(int) * n_listed, cudaMemcpyHostToDevice, stream));
+        TB_CUDA(cudaStreamSynchronize(stream));
         drop_graphs();
         dirty = false;
         return TS_OK;
     }
 
+    // One stage: every group's launch (concurrently when there are several),
+    // then the finish kernel that closes each listed problem's step.
     void enqueue_stage() {
-        for (auto& g : groups) {
-            mixed_launch_batch(g.nd, g.tx, g.ty, g.solver, g.grid, d_desc, g.d_items, g.n, stream);
+        const int ng = (int)groups.size();
+        if (ng > 1) cudaEventRecord(fork, stream);
+        for (int k = 0; k < ng; ++k) {
+            const Group& g = groups[k];
+            cudaStream_t st = stream;
+            if (k > 0) {
+                st = side[(k - 1) % kSide];
+                if (k - 1 < kSide) cudaStreamWaitEvent(st, fork, 0);
+            }
+            mixed_launch_batch(g.nd, g.tx, g.ty, g.solver, g.grid, d_desc, d_ctl, g.d_items, g.n, st);
             ++launches;
         }
+        for (int k = 0; k < std::min(ng - 1, kSide); ++k) {
+            cudaEventRecord(join[k], side[k]);
+            cudaStreamWaitEvent(stream, join[k], 0);
+        }
+        mixed_batch_finish(d_desc, d_slots, n_listed, stream);
+        ++launches;
         ++stages;
     }
 
@@ -325,7 +367,7 @@ struct ts_batch {
                 }
                 TB_CUDA(cudaGraphLaunch(ex, stream));
                 stages += c;
-                launches += (long long)c * (long long)groups.size();
+                launches += (long long)c * (long long)(groups.size() + 1);
                 n -= c;
             }
         }
@@ -401,6 +443,11 @@ ts_status ts_batch_create(int32_t device, size_t budget, ts_batch** out) {
     DevGuard g(device);
     cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, device);
     TB_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+    for (int k = 0; k < ts_batch::kSide; ++k) {
+        TB_CUDA(cudaStreamCreateWithFlags(&b->side[k], cudaStreamNonBlocking));
+        TB_CUDA(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
+    }
+    TB_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
     TB_CUDA(b->arena.init(budget));
     ts_status s = b->grow(64);
     if (s != TS_OK) return s;

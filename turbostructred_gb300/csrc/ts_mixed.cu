@@ -726,15 +726,13 @@ __device__ void finish_problem(Ctl* ctl, double cfl) {
 
 // One work item (tile column and chunk q of problem d).
 template <class T, int SOLVER>
-__device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm, BoxPos (&bp)[T::NA],
-                                             Prefetch (&pf)[T::NA], RingPos (&rp)[T::NB], float& srmax,
-                                             unsigned int& health) {
-    const int par = d.ctl->parity;
+__device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, float dtf, float* sm,
+                                             BoxPos (&bp)[T::NA], Prefetch (&pf)[T::NA], RingPos (&rp)[T::NB],
+                                             float& srmax, unsigned int& health) {
     const double* __restrict__ Uin = d.U[par];
     double* __restrict__ Uout = d.U[par ^ 1];
     const float* __restrict__ Rin = d.R[par];
     float* __restrict__ Rout = d.R[par ^ 1];
-    const float dtf = f64_to_f32(d.ctl->dt_apply);
     const int kind = recon_kind(d.mp);
     const bool pwc = kind == 0;
     const int col = q % d.ncol;
@@ -774,9 +772,11 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, float* sm
     }
 }
 
-// The item's CFL maximum and health into the problem's control word; the CTA
-// that completes the problem's last item closes the problem's step.
-template <class T>
+// The item's CFL maximum and health into the problem's control word.  COUNT:
+// the CTA that completes the problem's last item closes the problem's step;
+// otherwise (batches) a separate kernel closes every listed problem's step
+// after the stage, and items only post their maxima (no returned atomics).
+template <class T, bool COUNT>
 __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsigned int health, float* wmax,
                                            unsigned int* whealth) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
@@ -795,10 +795,12 @@ __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsig
         Ctl* ctl = d.ctl;
         if (m > 0.0f) atomicMax(&ctl->srmax_bits, __float_as_uint(m));
         if (hh) atomicOr(&ctl->health, hh);
-        __threadfence();
-        if (atomicAdd(&ctl->blocks_done, 1u) == (unsigned)(d.nq - 1)) {
+        if (COUNT) {
             __threadfence();
-            finish_problem(ctl, d.mp.cfl);
+            if (atomicAdd(&ctl->blocks_done, 1u) == (unsigned)(d.nq - 1)) {
+                __threadfence();
+                finish_problem(ctl, d.mp.cfl);
+            }
         }
     }
 }
@@ -806,12 +808,13 @@ __device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsig
 // BATCH = false: one problem whose descriptor is a kernel parameter (constant
 // bank: every field is a free operand).  BATCH = true: a list of (problem,
 // item) pairs; the descriptor is staged in shared memory when the problem
-// changes from one item of the CTA to the next.  A problem's stop flag only
-// changes when its last item of the launch closes, so it is read once per
-// problem.
+// changes from one item of the CTA to the next, and the problem's stop flag,
+// parity and pending dt (constant during a batched stage: steps are closed
+// by k_batch_finish) are read alongside it from the control-word array.
 template <class T, int SOLVER, bool BATCH>
 __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_constant__ ProbDesc one,
                                                     const ProbDesc* __restrict__ probs,
+                                                    const Ctl* __restrict__ ctls,
                                                     const int2* __restrict__ items, int n_items) {
     extern __shared__ float sm[];
     __shared__ float wmax[32];
@@ -821,16 +824,19 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
     RingPos rp[T::NB];
     if constexpr (!BATCH) {
         if (one.ctl->stop_req) return;
+        const int par = one.ctl->parity;
+        const float dtf = f64_to_f32(one.ctl->dt_apply);
         for (int q = blockIdx.x; q < n_items; q += gridDim.x) {
             __syncthreads();  // the previous item is finished with shared memory
             float srmax = 0.0f;
             unsigned int health = 0;
-            process_item<T, SOLVER>(one, q, sm, bp, pf, rp, srmax, health);
-            close_item<T>(one, srmax, health, wmax, whealth);
+            process_item<T, SOLVER>(one, q, par, dtf, sm, bp, pf, rp, srmax, health);
+            close_item<T, true>(one, srmax, health, wmax, whealth);
         }
     } else {
         __shared__ ProbDesc sd;
-        __shared__ int s_skip;
+        __shared__ int s_skip, s_par;
+        __shared__ double s_dt;
         const int nwords = (int)(sizeof(ProbDesc) / sizeof(int));
         int cur = -1;
         for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -838,16 +844,20 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
             __syncthreads();  // the previous item is finished with shared memory
             if (pq.x != cur) {
                 for (int k = threadIdx.x; k < nwords; k += T::NT) ((int*)&sd)[k] = ((const int*)(probs + pq.x))[k];
-                __syncthreads();
-                if (threadIdx.x == 0) s_skip = *(volatile int*)&sd.ctl->stop_req;
+                if (threadIdx.x == 0) {
+                    const Ctl& c = ctls[pq.x];
+                    s_skip = c.stop_req;
+                    s_par = c.parity;
+                    s_dt = c.dt_apply;
+                }
                 __syncthreads();
                 cur = pq.x;
             }
             if (s_skip) continue;
             float srmax = 0.0f;
             unsigned int health = 0;
-            process_item<T, SOLVER>(sd, pq.y, sm, bp, pf, rp, srmax, health);
-            close_item<T>(sd, srmax, health, wmax, whealth);
+            process_item<T, SOLVER>(sd, pq.y, s_par, f64_to_f32(s_dt), sm, bp, pf, rp, srmax, health);
+            close_item<T, false>(sd, srmax, health, wmax, whealth);
         }
     }
 }
@@ -878,6 +888,16 @@ __global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
 }
 
 __global__ void k_mix_clear_pending(const ProbDesc* __restrict__ probs, int p) { probs[p].ctl->dt_apply = 0.0; }
+
+// Closes the stage of every listed problem that ran (batches): dt from its
+// CFL maximum and the Run bookkeeping.
+__global__ void k_batch_finish(const ProbDesc* __restrict__ probs, const int* __restrict__ slots, int n) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n) return;
+    const ProbDesc& d = probs[slots[t]];
+    if (d.ctl->stop_req) return;
+    finish_problem(d.ctl, d.mp.cfl);
+}
 
 // Compiled tiles: (problem dimension, threads along x, threads along y).
 // 3D: two-axis tiles marching z.  2D: one-row tiles marching y.  1D: one-row
@@ -937,19 +957,19 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
 void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const ProbDesc& h_desc, cudaStream_t st) {
     if (grid <= 0 || h_desc.nq <= 0) return;
     with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
-        k_mix_step<T, S, false><<<grid, T::NT, T::BYTES, st>>>(h_desc, nullptr, nullptr, h_desc.nq);
+        k_mix_step<T, S, false><<<grid, T::NT, T::BYTES, st>>>(h_desc, nullptr, nullptr, nullptr, h_desc.nq);
     });
 }
 
-bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const int2* d_items,
-                        int n_items, cudaStream_t st) {
+bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const Ctl* d_ctls,
+                        const int2* d_items, int n_items, cudaStream_t st) {
     if (nd == 3) return false;
     if (grid <= 0 || n_items <= 0) return true;
     ProbDesc none;
     std::memset(&none, 0, sizeof none);
     return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
         if constexpr (!T::HAS_Y)
-            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_items, n_items);
+            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items);
     });
 }
 
@@ -1139,6 +1159,10 @@ void mixed_reset(MixedBufs& mb, cudaStream_t st) {
 void mixed_apply(const ProbDesc* d_probs, int p, long long cells, cudaStream_t st) {
     k_mix_apply<<<(unsigned)((cells + 255) / 256), 256, 0, st>>>(d_probs, p);
     k_mix_clear_pending<<<1, 1, 0, st>>>(d_probs, p);
+}
+
+void mixed_batch_finish(const ProbDesc* d_probs, const int* d_slots, int n, cudaStream_t st) {
+    if (n > 0) k_batch_finish<<<(n + 127) / 128, 128, 0, st>>>(d_probs, d_slots, n);
 }
 
 void mixed_materialize(MixedBufs& mb, const Phys&, cudaStream_t st) { mixed_apply(mb.d_desc, 0, mb.desc.L.cells(), st); }

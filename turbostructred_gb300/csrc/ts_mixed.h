@@ -83,9 +83,12 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
 // One stage of one problem (descriptor passed by value).
 void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const ProbDesc& h_desc, cudaStream_t st);
 // One stage of a list of (problem, item) pairs of 1D or 2D problems sharing
-// the solver; false when no batched kernel exists for (nd, tile).
-bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const int2* d_items,
-                        int n_items, cudaStream_t st);
+// the solver and tile (d_ctls[p] is problem p's control word); false when no
+// batched kernel exists for (nd, tile).  The stage is closed afterwards by
+// mixed_batch_finish over the listed problems.
+bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const Ctl* d_ctls,
+                        const int2* d_items, int n_items, cudaStream_t st);
+void mixed_batch_finish(const ProbDesc* d_probs, const int* d_slots, int n, cudaStream_t st);
 
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                      const DeviceAlloc& alloc, MixedBufs& mb, std::string& err);
