@@ -221,6 +221,38 @@ ts_status ts_fill_scenario(const ts_config* cfg, int32_t scenario, uint64_t seed
 double ts_hash_uniform(uint64_t seed, int64_t i, int64_t j, int64_t k);
 
 /* ---------------------------------------------------------------------------
+   Solution files in the reference's formats, for one domain (the reference's
+   rank 0).
+   --------------------------------------------------------------------------- */
+
+/* Kernel::SaveSolution (kernel.h:992-1028): binary file of the current time
+   (double), the rank (int32, 0) and the interior cells' conserved values
+   (k, j, i order, x fastest, 5 doubles each). */
+ts_status ts_save_solution(ts_handle* h, const char* path);
+
+/* Kernel::LoadSolution (kernel.h:1029-1079): reads such a file into the state
+   and sets the time; the iteration count is kept and the next snapshot times
+   restart after the loaded time, as the reference does.  Files whose first
+   block is not rank 0 are refused (TS_ERR_UNSUPPORTED). */
+ts_status ts_load_solution(ts_handle* h, const char* path);
+
+/* Kernel::SaveSolutionToTecplot (kernel.h:1082-1413): Tecplot text, byte-
+   identical to the reference's for the same state.  molar_mass and
+   gas_constant are KernelConfiguration::MolarMass and ::UniversalGasConstant
+   (defaults 0 and 8.3144598; they only enter the temperature column).
+   async != 0 snapshots the state and writes the file on a worker thread;
+   ts_wait_writes joins the pending writes (ts_destroy does too). */
+ts_status ts_save_tecplot(ts_handle* h, const char* path, double molar_mass, double gas_constant, int32_t async);
+ts_status ts_wait_writes(ts_handle* h);
+
+/* The same three formats from and to host arrays (TS_LAYOUT_INTERIOR), with
+   no device work. */
+ts_status ts_write_solution_file(const ts_config* cfg, const double* values, double time, const char* path);
+ts_status ts_read_solution_file(const ts_config* cfg, const char* path, double* values, double* time);
+ts_status ts_write_tecplot_file(const ts_config* cfg, const double* values, double time, double molar_mass,
+                                double gas_constant, const char* path);
+
+/* ---------------------------------------------------------------------------
    Batches: many independent problems of different sizes advanced together.
    No counterpart in the reference (one Kernel per process there); each
    problem follows Kernel::Run semantics with its own dt (CFL minimum over its

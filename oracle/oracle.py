@@ -194,7 +194,8 @@ def ref_available() -> bool:
     return os.path.exists(REF_RUN)
 
 
-def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, steps: int = -1) -> str:
+def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, steps: int = -1,
+                     extra: list | None = None) -> str:
     lines = [f"ndims {case['ndims']}", f"nx {case['nx']}", f"ny {case['ny']}", f"nz {case['nz']}"]
     for a, n in enumerate("xyz"):
         lines.append(f"periodic_{n} {int(case['periodic'][a])}")
@@ -214,6 +215,7 @@ def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, ste
         lines.append(f"toro {toro}")
     if steps >= 0:
         lines.append(f"steps {steps}")
+    lines += extra or []
     return "\n".join(lines) + "\n"
 
 
@@ -240,9 +242,13 @@ def read_ref_output(path: str) -> dict:
     return out
 
 
-def run_reference(case: dict, interior_ic: np.ndarray | None, toro: int = 0, steps: int = -1) -> dict:
+def run_reference(case: dict, interior_ic: np.ndarray | None, toro: int = 0, steps: int = -1,
+                  load_solution: bytes | None = None, save_solution: bool = False, save_tecplot: bool = False,
+                  molar_mass: float | None = None, gas_constant: float | None = None) -> dict:
     """Run the reference's own ExplicitRungeKuttaFVM on this case (in a scratch
-    directory, since the reference writes history.dat to its cwd)."""
+    directory, since the reference writes history.dat to its cwd).  Optionally
+    Kernel::LoadSolution a file before stepping, and return the bytes of
+    Kernel::SaveSolution / SaveSolutionToTecplot after it."""
     if not ref_available():
         raise RuntimeError("oracle/_ref/ref_run is not built")
     with tempfile.TemporaryDirectory() as d:
@@ -250,8 +256,27 @@ def run_reference(case: dict, interior_ic: np.ndarray | None, toro: int = 0, ste
         out = os.path.join(d, "out.bin")
         if interior_ic is not None:
             np.ascontiguousarray(interior_ic, dtype="<f8").tofile(ic)
+        extra = []
+        if load_solution is not None:
+            with open(os.path.join(d, "load.bin"), "wb") as f:
+                f.write(load_solution)
+            extra.append(f"load_solution {os.path.join(d, 'load.bin')}")
+        if save_solution:
+            extra.append(f"save_solution {os.path.join(d, 'sol.bin')}")
+        if save_tecplot:
+            extra.append(f"save_tecplot {os.path.join(d, 'sol.dat')}")
+        if molar_mass is not None:
+            extra.append(f"molar_mass {molar_mass!r}")
+        if gas_constant is not None:
+            extra.append(f"gas_constant {gas_constant!r}")
         cfg = os.path.join(d, "case.txt")
         with open(cfg, "w") as f:
-            f.write(_ref_config_text(case, ic, out, toro, steps))
+            f.write(_ref_config_text(case, ic, out, toro, steps, extra))
         subprocess.run([REF_RUN, cfg], cwd=d, check=True, stdout=subprocess.DEVNULL)
-        return read_ref_output(out)
+        r = read_ref_output(out)
+        for key, name, flag in (("solution_bytes", "sol.bin", save_solution),
+                                ("tecplot_bytes", "sol.dat", save_tecplot)):
+            if flag:
+                with open(os.path.join(d, name), "rb") as f:
+                    r[key] = f.read()
+        return r

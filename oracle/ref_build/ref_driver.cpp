@@ -20,6 +20,10 @@
 //                  cell-averaged quadrature, ToroTests.h:426-446, plus the
 //                  exact solution and error norms, ToroTests.h:451-457)
 //   steps N       (optional: call IterationStep N times instead of Run)
+//   load_solution path   (optional: Kernel::LoadSolution before stepping)
+//   save_solution path   (optional: Kernel::SaveSolution after stepping)
+//   save_tecplot path    (optional: Kernel::SaveSolutionToTecplot after stepping)
+//   molar_mass x, gas_constant x   (KernelConfiguration MolarMass, UniversalGasConstant)
 #include "Methods/ExplicitRungeKuttaFVM.h"
 #include "Tests/1DTests/ToroTests.h"
 
@@ -30,6 +34,7 @@ namespace {
 struct DriverConfig {
     KernelConfiguration conf;
     std::string ic_file, out_file;
+    std::string load_solution, save_solution, save_tecplot;
     int toro = 0;
     int steps = -1;
     std::vector<BlockNode> blocks[3];
@@ -114,6 +119,11 @@ DriverConfig parse(const char* path) {
         else if (k == "out_file") d.out_file = w[1];
         else if (k == "toro") d.toro = I(1);
         else if (k == "steps") d.steps = I(1);
+        else if (k == "load_solution") d.load_solution = w[1];
+        else if (k == "save_solution") d.save_solution = w[1];
+        else if (k == "save_tecplot") d.save_tecplot = w[1];
+        else if (k == "molar_mass") c.MolarMass = D(1);
+        else if (k == "gas_constant") c.UniversalGasConstant = D(1);
         else { std::fprintf(stderr, "unknown key %s\n", k.c_str()); std::exit(2); }
     }
     if (d.has_blocks[0]) c.CompressionX = d.blocks[0];
@@ -185,6 +195,7 @@ int main(int argc, char** argv) {
                     ic.read(reinterpret_cast<char*>(kernel->getCellValues(i, j, k)), 5 * sizeof(double));
         if (!ic) { std::fprintf(stderr, "short ic file\n"); return 2; }
     }
+    if (!d.load_solution.empty()) kernel->LoadSolution(d.load_solution);
     std::valarray<double> initial = kernel->values;
 
     auto t0 = std::chrono::steady_clock::now();
@@ -195,6 +206,8 @@ int main(int argc, char** argv) {
     }
     auto t1 = std::chrono::steady_clock::now();
     double seconds = std::chrono::duration<double>(t1 - t0).count();
+    if (!d.save_solution.empty()) kernel->SaveSolution(d.save_solution);
+    if (!d.save_tecplot.empty()) kernel->SaveSolutionToTecplot(d.save_tecplot);
 
     std::ofstream o(d.out_file, std::ios::binary);
     const int32_t hdr[8] = {0x54534631, kernel->nDims, g.nlocalXAll, g.nlocalYAll, g.nlocalZAll,

@@ -34,6 +34,7 @@ UNITS = {
     "ts_batch.cu": [],
     "ts_host.cpp": [],
     "ts_server.cpp": [],
+    "ts_io.cpp": [],
 }
 
 

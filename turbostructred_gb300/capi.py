@@ -112,6 +112,8 @@ EXPORTS = [
     "ts_batch_autotune", "ts_batch_stats",
     "ts_server_create", "ts_server_destroy", "ts_server_submit", "ts_server_wait", "ts_server_drain",
     "ts_server_stats_get",
+    "ts_save_solution", "ts_load_solution", "ts_save_tecplot", "ts_wait_writes", "ts_write_solution_file",
+    "ts_read_solution_file", "ts_write_tecplot_file",
 ]
 
 _lib = None
@@ -171,6 +173,16 @@ def load(path: str = LIB_PATH):
     L.ts_server_drain.argtypes = [C.c_void_p, C.c_int32]
     L.ts_server_stats_get.argtypes = [C.c_void_p, P(ServerStats)]
     for name in ("ts_server_create", "ts_server_submit", "ts_server_wait", "ts_server_drain", "ts_server_stats_get"):
+        getattr(L, name).restype = C.c_int
+    L.ts_save_solution.argtypes = [C.c_void_p, C.c_char_p]
+    L.ts_load_solution.argtypes = [C.c_void_p, C.c_char_p]
+    L.ts_save_tecplot.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_double, C.c_int32]
+    L.ts_wait_writes.argtypes = [C.c_void_p]
+    L.ts_write_solution_file.argtypes = [P(Config), P(C.c_double), C.c_double, C.c_char_p]
+    L.ts_read_solution_file.argtypes = [P(Config), C.c_char_p, P(C.c_double), P(C.c_double)]
+    L.ts_write_tecplot_file.argtypes = [P(Config), P(C.c_double), C.c_double, C.c_double, C.c_double, C.c_char_p]
+    for name in ("ts_save_solution", "ts_load_solution", "ts_save_tecplot", "ts_wait_writes",
+                 "ts_write_solution_file", "ts_read_solution_file", "ts_write_tecplot_file"):
         getattr(L, name).restype = C.c_int
     L.ts_last_error.restype = C.c_char_p
     L.ts_status_string.restype = C.c_char_p
@@ -260,6 +272,34 @@ def fill_scenario(case: dict, scenario: int, seed: int, params) -> np.ndarray:
     return out
 
 
+GAS_CONSTANT = 8.3144598  # KernelConfiguration::UniversalGasConstant default
+
+
+def write_solution_file(case: dict, values: np.ndarray, time: float, path: str):
+    """Kernel::SaveSolution's binary layout from a host state (interior cells)."""
+    cfg, keep = to_config(case)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    check(load().ts_write_solution_file(C.byref(cfg), v.ctypes.data_as(C.POINTER(C.c_double)), time,
+                                        os.fsencode(path)))
+
+
+def read_solution_file(case: dict, path: str):
+    cfg, keep = to_config(case)
+    out = np.empty(interior_shape(case))
+    t = C.c_double()
+    check(load().ts_read_solution_file(C.byref(cfg), os.fsencode(path), out.ctypes.data_as(C.POINTER(C.c_double)),
+                                       C.byref(t)))
+    return out, t.value
+
+
+def write_tecplot_file(case: dict, values: np.ndarray, time: float, path: str, molar_mass: float = 0.0,
+                       gas_constant: float = GAS_CONSTANT):
+    cfg, keep = to_config(case)
+    v = np.ascontiguousarray(values, dtype=np.float64)
+    check(load().ts_write_tecplot_file(C.byref(cfg), v.ctypes.data_as(C.POINTER(C.c_double)), time, molar_mass,
+                                       gas_constant, os.fsencode(path)))
+
+
 class Solver:
     """One device-resident domain driven through the C ABI."""
 
@@ -336,6 +376,19 @@ class Solver:
 
     def set_tile(self, tx: int, ty: int, z_chunks: int = 0):
         check(self.lib.ts_set_tile(self.h, tx, ty, z_chunks))
+
+    def save_solution(self, path: str):
+        check(self.lib.ts_save_solution(self.h, os.fsencode(path)))
+
+    def load_solution(self, path: str):
+        check(self.lib.ts_load_solution(self.h, os.fsencode(path)))
+
+    def save_tecplot(self, path: str, molar_mass: float = 0.0, gas_constant: float = GAS_CONSTANT,
+                     asynchronous: bool = False):
+        check(self.lib.ts_save_tecplot(self.h, os.fsencode(path), molar_mass, gas_constant, int(asynchronous)))
+
+    def wait_writes(self):
+        check(self.lib.ts_wait_writes(self.h))
 
 
 def batch_problem_bytes(case: dict) -> int:

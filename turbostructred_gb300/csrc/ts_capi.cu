@@ -257,6 +257,10 @@ struct ts_handle {
     }
 };
 
+namespace ts {
+const ts_config& handle_config(const ts_handle* h) { return h->cfg; }
+}  // namespace ts
+
 extern "C" {
 
 ts_status ts_create(const ts_config* cfg, ts_handle** out) {
@@ -309,7 +313,11 @@ ts_status ts_create(const ts_config* cfg, ts_handle** out) {
     return TS_OK;
 }
 
-void ts_destroy(ts_handle* h) { delete h; }
+void ts_destroy(ts_handle* h) {
+    if (!h) return;
+    io_join_all(h, nullptr, nullptr);
+    delete h;
+}
 
 static ts_status set_state_impl(ts_handle* h, const double* values, int32_t layout, bool device_ptr) {
     if (!h || !values) return fail(TS_ERR_INVALID, "NULL argument");

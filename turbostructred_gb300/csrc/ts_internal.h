@@ -91,6 +91,11 @@ struct HostGrid {
 };
 
 ts_status build_grid(const ts_config& c, HostGrid& g, std::string& err);
+
+// The configuration a handle was created with (blocks point into the handle).
+const ts_config& handle_config(const ts_handle* h);
+// Joins a handle's pending asynchronous file writes; the first failure, if any.
+void io_join_all(const ts_handle* h, ts_status* status, std::string* error);
 ts_status validate_config(const ts_config& c, std::string& err);
 Phys make_phys(const ts_config& c);
 
