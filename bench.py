@@ -155,10 +155,69 @@ def oracle_sample_rate(steps, warmup, threads, nz=16, n=N_DEFAULT):
     return cells * steps / dt, dt, f"{steps} RK step(s) over a {n}x{n}x{nz} slab of the {n}^3 blast (planes {k0}-{k0 + nz - 1}), z periodic"
 
 
+def _cpu_job(job):
+    """One problem advanced by the oracle port on one host core: (case, interior
+    state, steps or -1 for the Run loop) -> (cell-updates, seconds)."""
+    import numpy as np
+
+    from oracle import oracle as O
+    case, ic, steps = job
+    full = O.embed(case, np.asarray(ic))
+    t0 = time.perf_counter()
+    _, info = O.advance(case, full, steps, threads=1)
+    cells = case["nx"] * (case["ny"] if case["ndims"] > 1 else 1) * (case["nz"] if case["ndims"] > 2 else 1)
+    return cells * info["iteration"], time.perf_counter() - t0
+
+
+def cpu_pool_rate(jobs, procs):
+    """Aggregate cell-updates/s of independent CPU jobs over `procs` processes
+    (spawned: no process forks after the GPU is initialised)."""
+    import multiprocessing as mp
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(procs) as pool:
+        res = pool.map(_cpu_job, jobs, chunksize=1)
+    wall = time.perf_counter() - t0
+    return sum(r[0] for r in res) / wall, wall
+
+
+def tubes_cpu_sample(every=8, cap=4000, seed=4096):
+    from turbostructred_gb300 import workloads
+    probs = workloads.tubes(4096, seed=seed)
+    jobs = []
+    for k in range(0, len(probs), every):
+        c, ic = probs[k]
+        c = dict(c, max_iter=cap)
+        jobs.append((c, ic, -1))
+    desc = (f"every {every}th of the 4096 tubes ({len(jobs)} tubes), each run to t_end or {cap} stages, "
+            "one process per host core, oracle port (the reference's algorithm restated)")
+    return jobs, desc
+
+
+def served_cpu_sample(n_req=48, steps=16, seed=200):
+    from turbostructred_gb300 import workloads
+    reqs = workloads.stream(200.0, 60.0, seed=seed)[:n_req]
+    jobs = [(c, workloads.stream_state(c, p, s), steps) for _, c, p, s in reqs]
+    desc = (f"the first {n_req} requests of the stream, {steps} RK steps each (of 500), one process per host "
+            "core, oracle port")
+    return jobs, desc
+
+
 def run_reference(args, rank, ws):
     if rank != 0:
         return
     threads = os.cpu_count() or 1
+    if args.workload in ("tubes", "served"):
+        jobs, sample = tubes_cpu_sample() if args.workload == "tubes" else served_cpu_sample()
+        rate, secs = cpu_pool_rate(jobs, threads)
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
+                "steps": 1, "warmup": 0, "ms_per_step": 1e3 * secs, "higher_is_better": True, "scaling": "weak",
+                "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": args.workload, "sample": sample},
+                "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     rate, secs, sample = oracle_sample_rate(args.steps, args.warmup, threads)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
@@ -396,6 +455,12 @@ def run_tubes(args, rank, ws, lr, dist):
                           "max_iterations": max(iters), "unhealthy": health, "add_s": runs[0]["add_s"],
                           "get_s": runs[0]["get_s"]},
                 "mixed_error_vs_fp64": {"tubes_sampled": len(errs), **(err or {})}}
+        if ws == 1 and not args.skip_cpu:
+            jobs, sample = tubes_cpu_sample()
+            procs = os.cpu_count() or 1
+            rate, secs = cpu_pool_rate(jobs, procs)
+            line["cpu_baseline"] = {"value": rate, "unit": "cell-updates/s", "cores": procs, "kind": "port",
+                                    "sample": sample, "seconds": secs}
         print(json.dumps(line), flush=True)
 
 
@@ -480,6 +545,12 @@ def run_served(args, rank, ws, lr, dist):
                 "offered_cell_updates_per_s": sum(c["nx"] * c["ny"] * args.served_steps for _, c, _, _ in reqs)
                 / args.seconds, "client_max_lateness_s": late, "wall_s": t_end,
                 "clocks": clocks, "gpu_launches": st["launches"] - st0["launches"]}
+        if ws == 1 and not args.skip_cpu:
+            jobs, sample = served_cpu_sample()
+            procs = os.cpu_count() or 1
+            rate, secs = cpu_pool_rate(jobs, procs)
+            line["cpu_baseline"] = {"value": rate, "unit": "cell-updates/s", "cores": procs, "kind": "port",
+                                    "sample": sample, "seconds": secs}
         print(json.dumps(line), flush=True)
 
 
@@ -494,8 +565,8 @@ def main():
     p.add_argument("--fp64-steps", type=int, default=5)
     p.add_argument("--err-steps", type=int, default=50)
     p.add_argument("--e2e-jobs", type=int, default=2)
-    p.add_argument("--cpu-steps", type=int, default=2)
-    p.add_argument("--cpu-nz", type=int, default=32)
+    p.add_argument("--cpu-steps", type=int, default=24)
+    p.add_argument("--cpu-nz", type=int, default=128)
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
