@@ -48,7 +48,8 @@ enum {
     TS_RECON_ENO2_2POINTS = 2,
     TS_RECON_LINEAR_2POINTS_LIMITED = 3
 };
-/* RPSolver (MethodConfiguration.h:13-17) + HLLC (new) */
+/* RPSolver (MethodConfiguration.h:13-17) + HLLC (new).  Godunov (the exact
+   solver) runs on the FP64 path with the ideal-gas EOS. */
 enum { TS_RS_GODUNOV = 0, TS_RS_ROE_PIKE = 1, TS_RS_NONE = 2, TS_RS_HLLC = 3 };
 /* LimiterType (MethodConfiguration.h:20-23) */
 enum { TS_LIM_BARTH_JESPERSEN = 0, TS_LIM_VENKATAKRISHNAN = 1 };
@@ -73,7 +74,12 @@ enum {
     TS_LAYOUT_WITH_GHOSTS = 1 /* the reference's Kernel::values array (kernel.h:88-96) */
 };
 /* Health flags reported in ts_step_info.health */
-enum { TS_HEALTH_NAN = 1u, TS_HEALTH_NEG_DENSITY = 2u, TS_HEALTH_NEG_PRESSURE = 4u };
+enum {
+    TS_HEALTH_NAN = 1u,
+    TS_HEALTH_NEG_DENSITY = 2u,
+    TS_HEALTH_NEG_PRESSURE = 4u,
+    TS_HEALTH_RIEMANN = 8u /* the exact (Godunov) solver's p* iteration did not converge at some face */
+};
 
 /* BlockNode (KernelConfiguration.h:10-19): stretched-grid block start. */
 typedef struct ts_block_node {

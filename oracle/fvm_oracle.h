@@ -82,6 +82,10 @@ int orc_advance(const orc_config* c, double* values, int n_steps, orc_step_info*
 int orc_exact_riemann(double gamma, double p_inf, double rl, double ul, double pl, double rr,
                       double ur, double pr, double s, double* rho, double* u, double* p);
 
+/* Star pressure of the ideal-gas Riemann problem by Newton-Raphson (the
+   Godunov flux's inner solve); returns 1 when converged. */
+int orc_godunov_pstar(double gamma, double rl, double ul, double pl, double rr, double ur, double pr, double* ps);
+
 #ifdef __cplusplus
 }
 #endif

@@ -87,10 +87,14 @@ def test_invalid_configurations_rejected(bad, tslib):
     assert tslib.ts_last_error()
 
 
-def test_godunov_reported_unsupported(tslib):
+def test_godunov_limits_reported_unsupported(tslib):
+    """The exact solver runs on the FP64 path with the ideal-gas EOS (as the
+    reference's); other combinations are refused before any device work."""
     from turbostructred_gb300 import capi
-    cfg, keep = capi.to_config(capi.make_case(nx=8, solver=capi.RS_GODUNOV))
     h = C.c_void_p()
+    cfg, keep = capi.to_config(capi.make_case(nx=8, solver=capi.RS_GODUNOV), precision=capi.PRECISION_MIXED)
+    assert tslib.ts_create(C.byref(cfg), C.byref(h)) == 2
+    cfg, keep = capi.to_config(capi.make_case(nx=8, solver=capi.RS_GODUNOV, eos=capi.EOS_STIFFENED, p_inf=1.0))
     assert tslib.ts_create(C.byref(cfg), C.byref(h)) == 2
 
 

@@ -1,0 +1,107 @@
+"""The exact (Godunov) flux, GodunovSolverPerfectGasEOS
+(src/RiemannSolvers/GodunovSolverPerfectGasEOS.h), on the FP64 path.
+
+The reference finds the star pressure with alglib 3.8.0's Levenberg-Marquardt
+minimiser (gradient tolerance 1e-10); the oracle and the device use Newton's
+method on the same pressure function and keep every other step of the
+reference.  Bars:
+  * oracle vs the reference's own runs (tests/golden/godunov, made by
+    make_godunov_golden.py): same step count, relative L-inf of the state and
+    of the final time <= 1e-9 (measured: <= 3e-11);
+  * device vs oracle on the same inputs: relative L-inf <= 1e-12 (the same
+    algorithm; only the last bits of pow/sqrt may differ between the host
+    libm and CUDA);
+  * device vs the reference fixture: <= 1e-9.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from conftest import ROOT
+
+GOD = os.path.join(ROOT, "tests", "golden", "godunov")
+NAMES = sorted(f[:-4] for f in os.listdir(GOD) if f.endswith(".npz"))
+REF_TOL = 1e-9
+
+
+def load(name):
+    d = dict(np.load(os.path.join(GOD, name + ".npz")))
+    meta = json.loads(bytes(d.pop("meta")).decode())
+    case = meta["case"]
+    case["periodic"] = tuple(case["periodic"])
+    case["length"] = tuple(case["length"])
+    case["bc"] = [(t, dens, tuple(vel), ps) for t, dens, vel, ps in case["bc"]]
+    case["blocks"] = {}
+    d["case"], d["meta"] = case, meta
+    d["iteration"], d["time"] = int(d["scalars"][0]), float(d["scalars"][1])
+    return d
+
+
+def rel_linf(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+@pytest.mark.parametrize("name", NAMES)
+def test_oracle_matches_reference_godunov(name, oracle_mod):
+    g = load(name)
+    vals, info = oracle_mod.advance(g["case"], g["initial"], g["meta"]["steps"])
+    assert info["iteration"] == g["iteration"]
+    assert abs(info["time"] - g["time"]) <= REF_TOL * g["time"]
+    assert rel_linf(vals, g["values"]) <= REF_TOL
+
+
+def test_star_pressure_newton(oracle_mod):
+    """Toro's test 1-5 star pressures (Toro, Table 4.2) from the Newton solve."""
+    import ctypes as C
+    lib = oracle_mod.lib()
+    lib.orc_godunov_pstar.argtypes = [C.c_double] * 7 + [C.POINTER(C.c_double)]
+    lib.orc_godunov_pstar.restype = C.c_int
+    cases = [((1.0, 0.0, 1.0), (0.125, 0.0, 0.1), 0.30313),
+             ((1.0, -2.0, 0.4), (1.0, 2.0, 0.4), 0.001894),
+             ((1.0, 0.0, 1000.0), (1.0, 0.0, 0.01), 460.894),
+             ((1.0, 0.0, 0.01), (1.0, 0.0, 100.0), 46.0950),
+             ((5.99924, 19.5975, 460.894), (5.99242, -6.19633, 46.0950), 1691.64)]
+    for (rl, ul, pl), (rr, ur, pr), want in cases:
+        ps = C.c_double()
+        assert lib.orc_godunov_pstar(1.4, rl, ul, pl, rr, ur, pr, C.byref(ps)) == 1
+        assert abs(ps.value - want) <= 1e-4 * want
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", NAMES)
+def test_device_godunov_matches_oracle_and_reference(name, tslib, oracle_mod):
+    from turbostructred_gb300 import capi
+    g = load(name)
+    case = capi.make_case(**g["case"])
+    with capi.Solver(case, precision=capi.PRECISION_FP64) as s:
+        s.set_state(g["initial"], capi.LAYOUT_WITH_GHOSTS)
+        info = s.run() if g["meta"]["steps"] < 0 else s.step(g["meta"]["steps"])
+        got = s.get_state(capi.LAYOUT_WITH_GHOSTS)
+    ref, rinfo = oracle_mod.advance(g["case"], g["initial"], g["meta"]["steps"])
+    assert info["iteration"] == rinfo["iteration"] == g["iteration"]
+    assert info["health"] == 0
+    assert abs(info["time"] - rinfo["time"]) <= 1e-12 * rinfo["time"]
+    assert rel_linf(got, ref) <= 1e-12
+    assert rel_linf(got, g["values"]) <= REF_TOL
+
+
+@pytest.mark.gpu
+def test_device_godunov_c1_full_run(tslib, oracle_mod):
+    """C1's tube with the exact flux: the Run loop to t = 0.2 on 1000 cells."""
+    from oracle import oracle as O
+    from turbostructred_gb300 import capi
+    nat = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
+    kw = dict(ndims=1, nx=1000, periodic=(0, 1, 1), recon=0, solver=capi.RS_GODUNOV, cfl=0.5, max_time=0.2,
+              max_iter=10**6, bc=[nat] * 6)
+    case = capi.make_case(**kw)
+    ic = capi.fill_scenario(capi.make_case(**dict(kw, solver=capi.RS_ROE)), capi.SCENARIO_SHOCK_TUBE, 0,
+                            [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1])
+    with capi.Solver(case, precision=capi.PRECISION_FP64) as s:
+        s.set_state(ic)
+        info = s.run()
+        got = s.get_state()
+    ref, rinfo = oracle_mod.advance(O.make_case(**kw), O.embed(case, ic), -1)
+    assert info["iteration"] == rinfo["iteration"]
+    assert rel_linf(got, ref[0, 0, 1:-1].reshape(got.shape)) <= 1e-12

@@ -29,7 +29,7 @@ EOS_IDEAL, EOS_STIFFENED = 0, 1
 PRECISION_FP64, PRECISION_MIXED = 0, 1
 LAYOUT_INTERIOR, LAYOUT_WITH_GHOSTS = 0, 1
 SCENARIO_SHOCK_TUBE, SCENARIO_SHEAR_LAYER, SCENARIO_BLAST, SCENARIO_QUADRANTS = 0, 1, 2, 3
-HEALTH_NAN, HEALTH_NEG_DENSITY, HEALTH_NEG_PRESSURE = 1, 2, 4
+HEALTH_NAN, HEALTH_NEG_DENSITY, HEALTH_NEG_PRESSURE, HEALTH_RIEMANN = 1, 2, 4, 8
 
 STATUS = {0: "ok", 1: "invalid", 2: "unsupported", 3: "cuda", 4: "no_memory", 5: "numeric",
           6: "timeout", 7: "busy", 8: "not_found"}

@@ -96,13 +96,18 @@ ts_status validate_config(const ts_config& c, std::string& err) {
     if (c.reconstruction < 0 || c.reconstruction > 3) { err = "unknown reconstruction"; return TS_ERR_INVALID; }
     if (c.limiter < 0 || c.limiter > 1) { err = "unknown limiter"; return TS_ERR_INVALID; }
     if (c.riemann_solver == TS_RS_GODUNOV) {
-        err = "the exact Godunov solver is not built in this library"; return TS_ERR_UNSUPPORTED;
+        if (c.precision != TS_PRECISION_FP64) {
+            err = "the exact Godunov solver runs on the FP64 path"; return TS_ERR_UNSUPPORTED;
+        }
+        if (c.eos != TS_EOS_IDEAL_GAS) {
+            err = "the exact Godunov solver is built for the ideal-gas EOS"; return TS_ERR_UNSUPPORTED;
+        }
     }
     if (c.riemann_solver == TS_RS_NONE) {
         // InitializeMethod asserts a solver was chosen (ExplicitRungeKuttaFVM.h:43)
         err = "no Riemann solver chosen"; return TS_ERR_INVALID;
     }
-    if (c.riemann_solver != TS_RS_ROE_PIKE && c.riemann_solver != TS_RS_HLLC) {
+    if (c.riemann_solver != TS_RS_ROE_PIKE && c.riemann_solver != TS_RS_HLLC && c.riemann_solver != TS_RS_GODUNOV) {
         err = "unknown riemann_solver"; return TS_ERR_INVALID;
     }
     if (!(c.cfl > 0.0)) { err = "cfl must be positive"; return TS_ERR_INVALID; }

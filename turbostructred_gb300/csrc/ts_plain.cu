@@ -227,6 +227,186 @@ __device__ double hllc_flux(const Phys& ph, const double UL[NV], const double UR
     return lam;
 }
 
+// Exact (Godunov) flux, GodunovSolverPerfectGasEOS::ComputeFlux
+// (GodunovSolverPerfectGasEOS.h:266-430), ideal gas.  p* solves
+// fL(p) + fR(p) + (uR - uL) = 0 (f1/f2, :56-96).  The reference minimises the
+// square of that function with alglib's Levenberg-Marquardt (stopping at a
+// gradient below 1e-10, :143-187); here a bounded Newton-Raphson iteration
+// on the root with the analytic derivative (Toro, sec. 4.3.1) from the
+// primitive-variable guess (Toro eq. 4.47), to a relative change below 1e-14.
+// Everything after p* keeps the reference's steps and operation order.
+__device__ __forceinline__ double god_f(double g, double rk, double pk, double p) {
+    double res;
+    if (p > pk) {
+        const double A = 2 / ((g + 1.0) * rk);
+        const double B = pk * (g - 1.0) / (g + 1.0);
+        res = (p - pk) * sqrt(A / (p + B));
+    } else {
+        const double a = sqrt(g * pk / rk);
+        res = pow(p / pk, (g - 1.0) / (2 * g)) - 1.0;
+        res *= 2 * a / (g - 1.0);
+    }
+    return res;
+}
+
+__device__ __forceinline__ double god_df(double g, double rk, double pk, double p) {
+    if (p > pk) {
+        const double A = 2 / ((g + 1.0) * rk);
+        const double B = pk * (g - 1.0) / (g + 1.0);
+        return sqrt(A / (B + p)) * (1.0 - (p - pk) / (2.0 * (B + p)));
+    }
+    return pow(p / pk, -(g + 1.0) / (2.0 * g)) / (rk * sqrt(g * pk / rk));
+}
+
+// Returns false when 60 iterations do not converge (the caller flags it).
+__device__ bool god_pstar(double g, double rl, double ul, double pl, double rr, double ur, double pr, double& ps) {
+    const double al = sqrt(g * pl / rl), ar = sqrt(g * pr / rr);
+    const double du = ur - ul;
+    // both pressure functions are finite above lo (a side with a negative
+    // reconstructed pressure is on its shock branch, which needs p + B > 0)
+    double lo = 0.0;
+    if (pl < 0) lo = fmax(lo, -pl * (g - 1.0) / (g + 1.0));
+    if (pr < 0) lo = fmax(lo, -pr * (g - 1.0) / (g + 1.0));
+    const double floor_p = lo + 1e-12 * (fabs(pl) + fabs(pr));
+    double p = 0.5 * (pl + pr) - 0.125 * du * (rl + rr) * (al + ar);
+    if (!(p > floor_p)) p = 0.5 * (pl + pr);
+    if (!(p > floor_p)) p = 2.0 * floor_p;
+    for (int it = 0; it < 60; ++it) {
+        const double f = god_f(g, rl, pl, p) + god_f(g, rr, pr, p) + du;
+        const double d = god_df(g, rl, pl, p) + god_df(g, rr, pr, p);
+        double pn = p - f / d;
+        if (!(pn > floor_p)) pn = floor_p;
+        const double ch = 2.0 * fabs(pn - p) / (pn + p);
+        p = pn;
+        if (ch < 1e-14) { ps = p; return true; }
+    }
+    ps = p;
+    return false;
+}
+
+template <int A>
+__device__ double godunov_flux(const Phys& ph, const double UL[NV], const double UR[NV], double flux[NV],
+                               bool& converged) {
+    const double g = ph.gamma;
+    const double roL = UL[0], roR = UR[0];
+    const double velL[3] = {UL[1] / UL[0], UL[2] / UL[0], UL[3] / UL[0]};
+    const double velR[3] = {UR[1] / UR[0], UR[2] / UR[0], UR[3] / UR[0]};
+    // GetPressure (:17-25)
+    const double pL =
+        (g - 1.0) * roL * (UL[4] / roL - (velL[0] * velL[0] + velL[1] * velL[1] + velL[2] * velL[2]) / 2.0);
+    const double pR =
+        (g - 1.0) * roR * (UR[4] / roR - (velR[0] * velR[0] + velR[1] * velR[1] + velR[2] * velR[2]) / 2.0);
+    const double uL = velL[A], uR = velR[A];
+    // ComputeStarVariables (:143-264)
+    double pStar;
+    converged = god_pstar(g, roL, uL, pL, roR, uR, pR, pStar);
+    const double uStar = 0.5 * (uL + uR) + 0.5 * (god_f(g, roR, pR, pStar) - god_f(g, roL, pL, pStar));
+    const double C = (g - 1.0) / (g + 1.0);
+    double maxs = 0, roStarL, roStarR, SL = 0, SHL = 0, STL = 0, SR = 0, SHR = 0, STR = 0;
+    bool shockL, shockR;
+    const double pRatioL = pStar / pL, aL = sqrt(g * pL / roL);
+    if (pStar > pL) {
+        shockL = true;
+        roStarL = pRatioL + C;
+        roStarL /= C * pRatioL + 1.0;
+        roStarL *= roL;
+        SL = sqrt((g + 1) * pRatioL / (2 * g) + (g - 1) / (2 * g));
+        SL = uL - aL * SL;
+        maxs = fmax(maxs, fabs(SL));
+    } else {
+        shockL = false;
+        roStarL = roL * pow(pRatioL, 1.0 / g);
+        SHL = uL - aL;
+        const double aStarL = aL * pow(pRatioL, (g - 1) / (2 * g));
+        STL = uStar - aStarL;
+        maxs = fmax(maxs, fabs(SHL));
+    }
+    const double pRatioR = pStar / pR, aR = sqrt(g * pR / roR);
+    if (pStar > pR) {
+        shockR = true;
+        roStarR = pRatioR + C;
+        roStarR /= C * pRatioR + 1.0;
+        roStarR *= roR;
+        SR = sqrt((g + 1) * pRatioR / (2 * g) + (g - 1) / (2 * g));
+        SR = uR + aR * SR;
+        maxs = fmax(maxs, fabs(SR));
+    } else {
+        shockR = false;
+        roStarR = roR * pow(pRatioR, 1.0 / g);
+        SHR = uR + aR;
+        const double aStarR = aR * pow(pRatioR, (g - 1) / (2 * g));
+        STR = uStar + aStarR;
+        maxs = fmax(maxs, fabs(SHR));
+    }
+    // sampling at S = x/t = 0 (:299-393)
+    const double S = 0;
+    double ro, u, p;
+    const double* vel;
+    if (uStar >= S) {
+        vel = velL;
+        if (shockL) {
+            if (SL >= S) { ro = roL; u = uL; p = pL; }
+            else { ro = roStarL; u = uStar; p = pStar; }
+        } else if (SHL > S) {
+            ro = roL; u = uL; p = pL;
+        } else if (S > STL) {
+            ro = roStarL; u = uStar; p = pStar;
+        } else {
+            const double aL2 = sqrt(g * pL / roL);
+            const double CL = 2.0 / (g + 1) + (g - 1) * (uL - S) / ((g + 1) * aL2);
+            const double CLRo = pow(CL, 2.0 / (g - 1));
+            const double CLP = pow(CL, 2.0 * g / (g - 1));
+            ro = CLRo * roL;
+            u = aL2 + 0.5 * (g - 1) * uL + S;
+            u *= 2 / (g + 1);
+            p = CLP * pL;
+        }
+    } else {
+        vel = velR;
+        if (shockR) {
+            if (SR <= S) { ro = roR; u = uR; p = pR; }
+            else { ro = roStarR; u = uStar; p = pStar; }
+        } else if (SHR < S) {
+            ro = roR; u = uR; p = pR;
+        } else if (S < STR) {
+            ro = roStarR; u = uStar; p = pStar;
+        } else {
+            const double aR2 = sqrt(g * pR / roR);
+            const double CR = 2.0 / (g + 1) - (g - 1) * (uR - S) / ((g + 1) * aR2);
+            const double CRRo = pow(CR, 2.0 / (g - 1));
+            const double CRP = pow(CR, 2.0 * g / (g - 1));
+            ro = CRRo * roR;
+            u = -aR2 + 0.5 * (g - 1) * uR + S;
+            u *= 2 / (g + 1);
+            p = CRP * pR;
+        }
+    }
+    // face state (:396-404): normal velocity u, tangential from the upwind side
+    double Vf[3];
+#pragma unroll
+    for (int b = 0; b < 3; ++b) Vf[b] = (b == A) ? vel[b] + (u - vel[A]) : vel[b];
+    double Uf[NV];
+    Uf[0] = ro;
+    Uf[1] = ro * Vf[0];
+    Uf[2] = ro * Vf[1];
+    Uf[3] = ro * Vf[2];
+    Uf[4] = ro * (p / (ro * (g - 1.0)) + 0.5 * (Vf[0] * Vf[0] + Vf[1] * Vf[1] + Vf[2] * Vf[2]));
+    // F(Uface, n) (:28-46)
+    {
+        const double r = Uf[0];
+        const double vx = Uf[1] / r, vy = Uf[2] / r, vz = Uf[3] / r;
+        const double roE = Uf[4];
+        const double pp = (g - 1.0) * (roE - r * (vx * vx + vy * vy + vz * vz) / 2.0);
+        const double v3[3] = {vx, vy, vz};
+        const double vn = v3[A];
+        flux[0] = r * vn;
+#pragma unroll
+        for (int b = 0; b < 3; ++b) flux[1 + b] = (b == A) ? r * vn * v3[b] + pp : r * vn * v3[b];
+        flux[4] = vn * (roE + pp);
+    }
+    return maxs;
+}
+
 // ---------------------------------------------------------------------------
 // Kernels
 // ---------------------------------------------------------------------------
@@ -418,7 +598,14 @@ __global__ void k_flux(PlainBufs b, Phys ph) {
         sample(b, ph, cr, A, -0.5 * H[s + g0], UR);
     }
     double F[NV];
-    const double lam = (ph.solver == TS_RS_HLLC) ? hllc_flux<A>(ph, UL, UR, F) : roe_flux<A>(ph, UL, UR, F);
+    double lam;
+    if (ph.solver == TS_RS_GODUNOV) {
+        bool ok;
+        lam = godunov_flux<A>(ph, UL, UR, F, ok);
+        if (!ok) atomicOr(&b.ctl->health, (unsigned)TS_HEALTH_RIEMANN);
+    } else {
+        lam = (ph.solver == TS_RS_HLLC) ? hllc_flux<A>(ph, UL, UR, F) : roe_flux<A>(ph, UL, UR, F);
+    }
 #pragma unroll
     for (int v = 0; v < NV; ++v) b.F[A][vidx(L, v) + cf] = F[v];
     b.Lam[A][cf] = lam;
