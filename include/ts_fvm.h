@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define TS_FVM_ABI_VERSION 1
+#define TS_FVM_ABI_VERSION 2
 
 typedef enum ts_status {
     TS_OK = 0,
@@ -130,6 +130,12 @@ typedef struct ts_config {
     ts_bc_config bc[6];
     int32_t precision;       /* TS_PRECISION_* */
     int32_t device;          /* CUDA device ordinal */
+    /* Source terms (Kernel::ProcessExternalForces / ProcessExternalAcceleration,
+       kernel.h:941-989), added to the residual after the face fluxes. */
+    int32_t external_force;        /* IsExternalForceRequared: R_mom += V Sigma, R_E += V Sigma.u */
+    int32_t uniform_acceleration;  /* IsUnifromAccelerationRequared: R_mom += rho V g, R_E += V rho g.u */
+    double sigma[3];               /* Sigma */
+    double acceleration[3];        /* UniformAcceleration */
 } ts_config;
 
 /* StepInfo (kernel.h:31-39) plus a health word. */

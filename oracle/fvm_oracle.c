@@ -809,6 +809,47 @@ static void compute_residual(orc_ctx* w) {
     }
 }
 
+/* Source terms after the face fluxes (ExplicitRungeKuttaFVM.h:1421-1423):
+   Kernel::ProcessExternalForces (kernel.h:941-965) and
+   ProcessExternalAcceleration (:966-989), on the state the step started from. */
+static void add_sources(orc_ctx* w, const double* U) {
+    const orc_config* c = w->c;
+    if (!c->external_force && !c->uniform_acceleration) return;
+    for (int i = w->imin; i <= w->imax; ++i)
+        for (int j = w->jmin; j <= w->jmax; ++j)
+            for (int k = w->kmin; k <= w->kmax; ++k) {
+                int idx = cidx(w, i, j, k);
+                double volume = w->hx[i] * w->hy[j] * w->hz[k];
+                const double* V = U + (size_t)idx * NV;
+                vec3 vel = {V[1] / V[0], V[2] / V[0], V[3] / V[0]};
+                double* R = w->resid + (size_t)idx * NV;
+                if (c->external_force) {
+                    vec3 sg = {c->sigma[0], c->sigma[1], c->sigma[2]};
+                    R[1] += volume * sg.x;
+                    R[2] += volume * sg.y;
+                    R[3] += volume * sg.z;
+                    R[4] += dot3(sg, vel) * volume;
+                }
+            }
+    if (!c->uniform_acceleration) return;
+    for (int i = w->imin; i <= w->imax; ++i)
+        for (int j = w->jmin; j <= w->jmax; ++j)
+            for (int k = w->kmin; k <= w->kmax; ++k) {
+                int idx = cidx(w, i, j, k);
+                double volume = w->hx[i] * w->hy[j] * w->hz[k];
+                const double* V = U + (size_t)idx * NV;
+                vec3 vel = {V[1] / V[0], V[2] / V[0], V[3] / V[0]};
+                double ro = V[0];
+                vec3 g = {c->acceleration[0], c->acceleration[1], c->acceleration[2]};
+                vec3 rg = {ro * g.x, ro * g.y, ro * g.z};
+                double* R = w->resid + (size_t)idx * NV;
+                R[1] += ro * volume * g.x;
+                R[2] += ro * volume * g.y;
+                R[3] += ro * volume * g.z;
+                R[4] += dot3(rg, vel) * volume;
+            }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Step: ExplicitRungeKuttaFVM::IterationStep, :1440-1491                   */
 /* ------------------------------------------------------------------------ */
@@ -830,6 +871,7 @@ static void iteration_step(orc_ctx* w, double* U, orc_step_info* info) {
     }
     exchange_recon(w);
     compute_residual(w);
+    add_sources(w, U);
 
     /* ComputeTimeStep, :1427-1437: (volumes / spectralRadius).min() * CFL,
        min in libstdc++'s __valarray_min order. */

@@ -54,6 +54,10 @@ typedef struct {
     int bc_type[6];
     double bc_density[6], bc_velocity[6][3], bc_pstatic[6];
     int threads; /* OpenMP threads (0 = runtime default) */
+    /* Source terms: IsExternalForceRequared with Sigma, IsUnifromAccelerationRequared
+       with UniformAcceleration (KernelConfiguration.h:50-51,87-88). */
+    int external_force, uniform_acceleration;
+    double sigma[3], acceleration[3];
 } orc_config;
 
 typedef struct {

@@ -55,6 +55,8 @@ class OrcConfig(C.Structure):
         ("bc_velocity", (C.c_double * 3) * 6),
         ("bc_pstatic", C.c_double * 6),
         ("threads", C.c_int),
+        ("external_force", C.c_int), ("uniform_acceleration", C.c_int),
+        ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
     ]
 
 
@@ -103,7 +105,8 @@ def make_case(**kw) -> dict:
     case = dict(ndims=1, nx=1, ny=1, nz=1, periodic=(1, 1, 1), length=(1.0, 1.0, 1.0), blocks={},
                 gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
-                save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6)
+                save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
+                external_force=None, uniform_acceleration=None)
     case.update(kw)
     return case
 
@@ -128,6 +131,12 @@ def to_struct(case: dict, threads: int = 0) -> OrcConfig:
         for a in range(3):
             c.bc_velocity[s][a] = vel[a]
     c.threads = threads
+    for flag, vec, key in (("external_force", "sigma", "external_force"),
+                           ("uniform_acceleration", "acceleration", "uniform_acceleration")):
+        v = case.get(key)
+        setattr(c, flag, int(v is not None))
+        for a in range(3):
+            getattr(c, vec)[a] = v[a] if v is not None else 0.0
     return c
 
 
@@ -210,6 +219,10 @@ def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, ste
     for s, name in enumerate(["bc_xl", "bc_xr", "bc_yl", "bc_yr", "bc_zl", "bc_zr"]):
         t, dens, vel, ps = case["bc"][s]
         lines.append(f"{name} {t} {dens!r} {vel[0]!r} {vel[1]!r} {vel[2]!r} {ps!r}")
+    if case.get("external_force") is not None:
+        lines.append("external_force " + " ".join(repr(float(v)) for v in case["external_force"]))
+    if case.get("uniform_acceleration") is not None:
+        lines.append("uniform_acceleration " + " ".join(repr(float(v)) for v in case["uniform_acceleration"]))
     lines += [f"ic_file {ic_path}", f"out_file {out_path}"]
     if toro:
         lines.append(f"toro {toro}")

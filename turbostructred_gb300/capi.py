@@ -18,7 +18,7 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libtsfvm.so")
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 
 # enum values (include/ts_fvm.h)
 RECON_PWC, RECON_LINEAR2, RECON_ENO2, RECON_LINEAR2_LIM = 0, 1, 2, 3
@@ -61,6 +61,8 @@ class Config(C.Structure):
         ("max_iteration", C.c_int32), ("reserved2", C.c_int32), ("max_time", C.c_double),
         ("save_solution_time", C.c_double), ("save_slice_time", C.c_double),
         ("bc", BcConfig * 6), ("precision", C.c_int32), ("device", C.c_int32),
+        ("external_force", C.c_int32), ("uniform_acceleration", C.c_int32),
+        ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
     ]
 
 
@@ -205,7 +207,8 @@ def make_case(**kw) -> dict:
     case = dict(ndims=1, nx=1, ny=1, nz=1, periodic=(1, 1, 1), length=(1.0, 1.0, 1.0), blocks={},
                 gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
-                save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6)
+                save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
+                external_force=None, uniform_acceleration=None)
     case.update(kw)
     return case
 
@@ -239,6 +242,13 @@ def to_config(case: dict, precision: int = PRECISION_FP64, device: int = 0):
         for a in range(3):
             c.bc[s].velocity[a] = vel[a]
     c.precision, c.device = precision, device
+    # source terms: None (off) or a 3-vector
+    for flag, vec, key in (("external_force", "sigma", "external_force"),
+                           ("uniform_acceleration", "acceleration", "uniform_acceleration")):
+        v = case.get(key)
+        setattr(c, flag, int(v is not None))
+        for a in range(3):
+            getattr(c, vec)[a] = v[a] if v is not None else 0.0
     return c, keep
 
 

@@ -168,6 +168,12 @@ Phys make_phys(const ts_config& c) {
         for (int a = 0; a < 3; ++a) p.bc.vel[s][a] = c.bc[s].velocity[a];
         p.bc.pstatic[s] = c.bc[s].pstatic;
     }
+    p.force = c.external_force != 0;
+    p.accel = c.uniform_acceleration != 0;
+    for (int a = 0; a < 3; ++a) {
+        p.sigma[a] = p.force ? c.sigma[a] : 0.0;
+        p.g[a] = p.accel ? c.acceleration[a] : 0.0;
+    }
     return p;
 }
 

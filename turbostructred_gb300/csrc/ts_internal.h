@@ -60,6 +60,8 @@ struct Phys {
     int periodic[3];
     double gamma, p_inf, eps, cfl;
     BcSet bc;
+    int force, accel;          // source terms on (kernel.h:941-989)
+    double sigma[3], g[3];     // Sigma, UniformAcceleration
 };
 
 // Per-handle step control word in device memory (StepInfo, kernel.h:31-39).

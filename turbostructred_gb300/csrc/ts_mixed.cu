@@ -658,10 +658,22 @@ __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int
     if (T::MARCH && do_z && (T::HAS_Y || tx < T::TX)) face<T, SOLVER, 2>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
 }
 
+// The working state (rho, momentum) of the thread's own cell in plane z, for
+// the source terms; read before the barrier that precedes the residual (the
+// next plane's store reuses the slot).
+template <class T>
+__device__ __forceinline__ float4 own_state(const float* sm, const Slots& s) {
+    int tx, ty;
+    if (!T::cell(threadIdx.x, tx, ty)) return make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    const int box = (T::HAS_Y ? (ty + HB) * T::BX : 0) + tx + HB;
+    return make_float4(sm[T::w(s.w0, 0, box)], sm[T::w(s.w0, 1, box)], sm[T::w(s.w0, 2, box)],
+                       sm[T::w(s.w0, 3, box)]);
+}
+
 // Residual and spectral radius of the owned cell of this thread in plane z.
 template <class T>
 __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
-                                         int z, const Slots& s, float& srmax) {
+                                         int z, const Slots& s, float4 own, float& srmax) {
     int tx, ty;
     if (!T::cell(threadIdx.x, tx, ty)) return;
     const int gi = i0 + tx, gj = j0 + ty;
@@ -691,6 +703,26 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
         if (z == d.kn[2] - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * d.kgeo[2][d.kn[2] + d.kgoff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
+    // source terms after the face fluxes (kernel.h:941-989), on the working state
+    const MixPhys& mp = d.mp;
+    if (mp.force || mp.accel) {
+        const float ro = own.x;
+        const float iro = 1.0f / ro;
+        const float vu = own.y * iro, vv = own.z * iro, vw = own.w * iro;
+        const float vol = gx.h * gy.h * gz.h;
+        if (mp.force) {
+            R[1] += vol * mp.sigma[0];
+            R[2] += vol * mp.sigma[1];
+            R[3] += vol * mp.sigma[2];
+            R[4] += (mp.sigma[0] * vu + mp.sigma[1] * vv + mp.sigma[2] * vw) * vol;
+        }
+        if (mp.accel) {
+            R[1] += ro * vol * mp.g[0];
+            R[2] += ro * vol * mp.g[1];
+            R[3] += ro * vol * mp.g[2];
+            R[4] += ((ro * mp.g[0]) * vu + (ro * mp.g[1]) * vv + (ro * mp.g[2]) * vw) * vol;
+        }
+    }
     const long long c = d.kbase + gi + gj * d.kstr[1] + z * d.kstr[2];
     const long long plane = d.L.plane;
 #pragma unroll
@@ -735,6 +767,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
     float* __restrict__ Rout = d.R[par ^ 1];
     const int kind = recon_kind(d.mp);
     const bool pwc = kind == 0;
+    const bool src = d.mp.force || d.mp.accel;
     const int col = q % d.ncol;
     const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
     setup_box<T>(d, i0, j0, bp);
@@ -746,8 +779,9 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         __syncthreads();
         if (!pwc) { recon<T>(d, sm, 0, kind, s, rp); __syncthreads(); }
         fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false, s);
+        const float4 own = src ? own_state<T>(sm, s) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
-        residual<T>(d, sm, Rout, i0, j0, 0, s, srmax);
+        residual<T>(d, sm, Rout, i0, j0, 0, s, own, srmax);
     } else {
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
@@ -766,8 +800,9 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             __syncthreads();
             if (!pwc) { recon<T>(d, sm, z + 1, kind, sr, rp); __syncthreads(); }
             if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true, sf);
+            const float4 own = src && z >= z0 ? own_state<T>(sm, sf) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
             __syncthreads();
-            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, sf, srmax);
+            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, sf, own, srmax);
         }
     }
 }
@@ -1115,6 +1150,12 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
         // inlet ghost energy, shifted: p/(g-1) + rho|v|^2/2 (the p_inf terms cancel)
         m.bc_state[sd][4] = (float)(ph.bc.pstatic[sd] / (ph.gamma - 1) + 0.5 * r * (vx * vx + vy * vy + vz * vz));
         for (int a = 0; a < 3; ++a) m.bc_vel[sd][a] = (float)ph.bc.vel[sd][a];
+    }
+    m.force = ph.force;
+    m.accel = ph.accel;
+    for (int a = 0; a < 3; ++a) {
+        m.sigma[a] = (float)ph.sigma[a];
+        m.g[a] = (float)ph.g[a];
     }
     return TS_OK;
 }

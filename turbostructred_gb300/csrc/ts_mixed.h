@@ -33,6 +33,8 @@ struct MixPhys {
     int bc_type[6];
     float bc_state[6][5];  // SubsonicInlet ghost state (shifted energy)
     float bc_vel[6][3];    // MovingWall velocity
+    int force, accel;      // source terms on (kernel.h:941-989)
+    float sigma[3], g[3];  // Sigma, UniformAcceleration
 };
 
 // Everything the fused kernel needs about one problem (lives in device memory).

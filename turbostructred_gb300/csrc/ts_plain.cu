@@ -718,12 +718,31 @@ __global__ void k_update(PlainBufs b, Phys ph) {
                 R[v] -= (F[c + st] - F[c]) * fS;
             }
         }
-        double u[NV];
+        double uo[NV], u[NV];
+#pragma unroll
+        for (int v = 0; v < NV; ++v) uo[v] = b.U[vidx(L, v) + c];
+        // source terms after the face fluxes (ExplicitRungeKuttaFVM.h:1421-1423;
+        // ProcessExternalForces and ProcessExternalAcceleration, kernel.h:941-989)
+        if (ph.force || ph.accel) {
+            const double vu = uo[1] / uo[0], vv = uo[2] / uo[0], vw = uo[3] / uo[0];
+            if (ph.force) {
+                R[1] += V * ph.sigma[0];
+                R[2] += V * ph.sigma[1];
+                R[3] += V * ph.sigma[2];
+                R[4] += (ph.sigma[0] * vu + ph.sigma[1] * vv + ph.sigma[2] * vw) * V;
+            }
+            if (ph.accel) {
+                const double ro = uo[0];
+                R[1] += ro * V * ph.g[0];
+                R[2] += ro * V * ph.g[1];
+                R[3] += ro * V * ph.g[2];
+                R[4] += ((ro * ph.g[0]) * vu + (ro * ph.g[1]) * vv + (ro * ph.g[2]) * vw) * V;
+            }
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            double* p = b.U + vidx(L, v) + c;
-            u[v] = *p + dt * (R[v] / V);
-            *p = u[v];
+            u[v] = uo[v] + dt * (R[v] / V);
+            b.U[vidx(L, v) + c] = u[v];
             nrm[v] = V * fabs(R[v]);
         }
         const double ke = 0.5 * (u[1] * u[1] + u[2] * u[2] + u[3] * u[3]) / u[0];
