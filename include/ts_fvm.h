@@ -327,10 +327,10 @@ ts_status ts_batch_stats(ts_batch* b, double* cell_updates, int64_t* stages, int
    Served solves: a request loop over one batch.  No counterpart in the
    reference.  Requests (1D/2D, mixed precision, any EOS / solver /
    reconstruction) are submitted from any thread and queue in arrival order;
-   a worker thread admits the head of the queue whenever the batch arena has
-   room for it (and fewer than max_active solves are running), advances all
-   admitted solves together in chunks of stages, and retires each one as it
-   reaches its MaxTime / MaxIteration.  Requests that arrive while others run
+   a worker thread admits queued solves (in arrival order, or least work
+   first) whenever the batch arena has room and the caps on admitted cells
+   and solves allow, advances all admitted solves together in chunks of
+   stages, and retires each one as it reaches its MaxTime / MaxIteration.  Requests that arrive while others run
    join at the next chunk boundary (continuous batching): each result is that
    of the problem alone in a batch, bit for bit.
    --------------------------------------------------------------------------- */
@@ -354,10 +354,26 @@ typedef struct ts_server_stats {
     ts_status worker_status;           /* first error the worker met (TS_OK if none) */
 } ts_server_stats;
 
-/* max_active: cap on admitted solves (0 = memory is the only limit);
-   chunk_ms: target duration of one chunk of stages (0 = 2 ms). */
-ts_status ts_server_create(int32_t device, size_t memory_budget, int32_t max_active, double chunk_ms,
-                           ts_server** out);
+/* Admission order of queued solves. */
+enum {
+    TS_SERVE_FIFO = 0,            /* arrival order; the head waits for room */
+    TS_SERVE_SHORTEST_FIRST = 1   /* least work first (cells x MaxIteration, or cells when
+                                     only MaxTime bounds it), arrival order among equals */
+};
+
+typedef struct ts_server_config {
+    int32_t device;
+    int32_t order;          /* TS_SERVE_* */
+    size_t memory_budget;   /* bytes of device memory for admitted solves */
+    int64_t max_cells;      /* cells admitted at once (0: memory is the only limit).  The
+                               GPU's throughput saturates at a few million cells in
+                               flight; admitting more only slows every solve down */
+    int32_t max_active;     /* admitted solves at once (0: no cap) */
+    int32_t reserved;
+    double chunk_ms;        /* target duration of one chunk of stages (0: 2 ms) */
+} ts_server_config;
+
+ts_status ts_server_create(const ts_server_config* cfg, ts_server** out);
 /* Stops the worker (solves in flight are dropped) and frees everything. */
 void ts_server_destroy(ts_server* s);
 

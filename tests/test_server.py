@@ -119,3 +119,28 @@ def test_served_errors(tslib):
         srv.drain(10000)
         st = srv.stats()
         assert st["queued"] == 0 and st["active"] == 0 and st["bytes_in_use"] == 0
+
+
+def test_served_shortest_first_and_cell_cap(tslib):
+    """Least-work-first admission: with one solve admitted at a time, queued
+    small solves overtake large ones; a cap on admitted cells holds."""
+    from turbostructred_gb300 import capi
+    big = capi.make_case(ndims=2, nx=128, ny=128, periodic=(1, 1, 1), max_iter=60, max_time=1e30)
+    small = capi.make_case(ndims=2, nx=32, ny=32, periodic=(1, 1, 1), max_iter=60, max_time=1e30)
+    shear = [2.0, 1.0, 0.5, 2.5, 0.01]
+    reqs = [(big, capi.fill_scenario(big, 1, k, shear)) for k in range(3)] + \
+           [(small, capi.fill_scenario(small, 1, k, shear)) for k in range(3)]
+    alone = [run_batch([r])[0] for r in reqs]
+    with capi.Server(BUDGET, max_active=1, order=capi.SERVE_SHORTEST_FIRST) as srv:
+        ids = [srv.submit(c, v) for c, v in reqs]
+        res = [srv.wait(i) for i in ids]
+    times = [r[2] for r in res]
+    first = min(range(6), key=lambda k: times[k]["admit_s"])
+    later_big = [times[k]["finish_s"] for k in range(3) if k != first]
+    assert max(times[k]["finish_s"] for k in range(3, 6) if k != first) <= min(later_big)
+    for (got, info, _), ref in zip(res, alone):
+        assert np.array_equal(got, ref[0])
+    with capi.Server(BUDGET, max_cells=2 * 128 * 128) as srv:
+        ids = [srv.submit(c, v) for c, v in reqs[:3]]
+        res = [srv.wait(i) for i in ids]
+    assert max_concurrent([r[2] for r in res]) <= 2

@@ -89,6 +89,15 @@ class Timing(C.Structure):
                     kernels={self.kernel_name[k].value.decode(): self.kernel_ms[k] for k in range(self.n_kernels)})
 
 
+SERVE_FIFO, SERVE_SHORTEST_FIRST = 0, 1
+
+
+class ServerConfig(C.Structure):
+    _fields_ = [("device", C.c_int32), ("order", C.c_int32), ("memory_budget", C.c_size_t),
+                ("max_cells", C.c_int64), ("max_active", C.c_int32), ("reserved", C.c_int32),
+                ("chunk_ms", C.c_double)]
+
+
 class RequestTimes(C.Structure):
     _fields_ = [("submit_s", C.c_double), ("admit_s", C.c_double), ("finish_s", C.c_double)]
 
@@ -167,7 +176,7 @@ def load(path: str = LIB_PATH):
     for name in ("ts_batch_create", "ts_batch_add", "ts_batch_step", "ts_batch_run", "ts_batch_finished",
                  "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile", "ts_batch_autotune", "ts_batch_stats"):
         getattr(L, name).restype = C.c_int
-    L.ts_server_create.argtypes = [C.c_int32, C.c_size_t, C.c_int32, C.c_double, P(C.c_void_p)]
+    L.ts_server_create.argtypes = [P(ServerConfig), P(C.c_void_p)]
     L.ts_server_destroy.argtypes = [C.c_void_p]
     L.ts_server_destroy.restype = None
     L.ts_server_submit.argtypes = [C.c_void_p, P(Config), P(C.c_double), C.c_int32, P(C.c_int32)]
@@ -487,10 +496,13 @@ class Server:
     """Served solves: submit from any thread, a native worker admits them into
     one batch as memory frees up and retires them as they finish."""
 
-    def __init__(self, memory_budget: int, max_active: int = 0, chunk_ms: float = 2.0, device: int = 0):
+    def __init__(self, memory_budget: int, max_active: int = 0, chunk_ms: float = 2.0, device: int = 0,
+                 order: int = SERVE_FIFO, max_cells: int = 0):
         self.lib = load()
+        cfg = ServerConfig(device=device, order=order, memory_budget=memory_budget, max_cells=max_cells,
+                           max_active=max_active, reserved=0, chunk_ms=chunk_ms)
         h = C.c_void_p()
-        check(self.lib.ts_server_create(device, memory_budget, max_active, chunk_ms, C.byref(h)))
+        check(self.lib.ts_server_create(C.byref(cfg), C.byref(h)))
         self.h = h
         self.cases = {}
 

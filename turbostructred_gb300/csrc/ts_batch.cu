@@ -177,6 +177,7 @@ struct ts_batch {
     int next_id = 0;
     std::vector<Group> groups;
     bool dirty = true;
+    int stable = 0;  // launches since the work list last changed
     std::map<int, cudaGraphExec_t> graphs;
     Tune tune[4] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 0}};
     double* stage_buf = nullptr;
@@ -341,9 +342,23 @@ struct ts_batch {
         ++stages;
     }
 
+    // Stages are launched one by one right after the work list changed (a
+    // capture costs more than it saves when membership keeps changing, as in
+    // a served stream); once the list has been stable for a few launches,
+    // chunks of stages are captured into graphs and replayed.
     ts_status launch(int n) {
-        if (dirty) { ts_status s = rebuild(); if (s != TS_OK) return s; }
+        if (dirty) {
+            ts_status s = rebuild();
+            if (s != TS_OK) return s;
+            stable = 0;
+        }
         if (groups.empty()) return TS_OK;
+        if (stable < 2) {
+            ++stable;
+            for (int k = 0; k < n; ++k) enqueue_stage();
+            TB_CUDA(cudaGetLastError());
+            return TS_OK;
+        }
         static const int chunks[3] = {32, 4, 1};
         for (int c : chunks) {
             while (n >= c) {

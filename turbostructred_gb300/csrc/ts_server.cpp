@@ -1,9 +1,12 @@
 // Served solves over one batch (include/ts_fvm.h, ts_server_*).
 //
 // Threads: callers submit and wait; one worker owns the batch.  The worker
-// repeats: admit queued requests in arrival order while the arena has room,
+// repeats: admit queued requests (in arrival order, or least work first)
+// while the arena has room and the caps on admitted cells and solves allow,
 // run one chunk of stages of everything admitted, retire what finished
-// (state read back, slot and memory freed).  The chunk length adapts so one
+// (state read back, slot and memory freed).  The cell cap keeps the admitted
+// set near the size that saturates the GPU: beyond it, admitting more only
+// stretches every admitted solve (all of them share each stage).  The chunk length adapts so one
 // chunk takes about chunk_ms, which bounds how long a new arrival waits for
 // the next admission point and how late a finished solve is noticed.
 #include <algorithm>
@@ -27,6 +30,7 @@ using Clock = std::chrono::steady_clock;
 
 struct Request {
     int32_t id = -1;
+    double work = 0.0;  // admission key of TS_SERVE_SHORTEST_FIRST
     ts_config cfg{};
     std::vector<ts_block_node> blocks[3];
     std::vector<double> values;  // initial state; the final one when kept
@@ -58,6 +62,8 @@ struct ts_server {
     int device = 0;
     size_t budget = 0;
     int max_active = 0;
+    int order = TS_SERVE_FIFO;
+    long long max_cells = 0;
     double chunk_ms = 2.0;
     ts_batch* batch = nullptr;
     Clock::time_point t0 = Clock::now();
@@ -72,6 +78,7 @@ struct ts_server {
     int64_t stages = 0, launches = 0;
     double cell_updates = 0.0, busy_s = 0.0;
     size_t in_use = 0;
+    double in_cells = 0.0;
     ts_status worker_status = TS_OK;
     std::string worker_error;
     bool stop = false;
@@ -103,6 +110,7 @@ struct ts_server {
         for (auto& r : queue) retire(r, st, worker_error);
         queue.clear();
         in_use = 0;
+        in_cells = 0.0;
         cv_done.notify_all();
     }
 
@@ -115,12 +123,19 @@ struct ts_server {
                 std::unique_lock<std::mutex> lk(mu);
                 if (running.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
                 if (stop) return;
+                if (order == TS_SERVE_SHORTEST_FIRST)
+                    std::stable_sort(queue.begin(), queue.end(),
+                                     [](const Req& a, const Req& b) { return a.get()->work < b.get()->work; });
                 size_t room = budget - in_use;
+                double cells = in_cells;
                 while (!queue.empty()) {
                     const Req& r = queue.front();
+                    const bool idle = running.empty() && admit.empty();
                     if (max_active > 0 && running.size() + admit.size() >= (size_t)max_active) break;
-                    if (r->bytes > room) break;  // arrival order: the head waits for memory
+                    if (max_cells > 0 && cells + r->cells > (double)max_cells && !idle) break;
+                    if (r->bytes > room) break;  // the next in order waits for memory
                     room -= r->bytes;
+                    cells += r->cells;
                     admit.push_back(r);
                     queue.pop_front();
                 }
@@ -146,6 +161,7 @@ struct ts_server {
                 if (!r->keep) std::vector<double>().swap(r->values);
                 running[bid] = r;
                 in_use += r->bytes;
+                in_cells += r->cells;
                 ++admitted;
                 wait_ms.push_back(1e3 * (r->t.admit_s - r->t.submit_s));
             }
@@ -179,6 +195,7 @@ struct ts_server {
                     std::lock_guard<std::mutex> lk(mu);
                     running.erase(fin[k]);
                     in_use -= r->bytes;
+                    in_cells -= r->cells;
                     retire(r, TS_OK, "");
                 }
                 if (s != TS_OK || n < (int32_t)fin.size()) break;
@@ -199,17 +216,21 @@ struct ts_server {
 
 extern "C" {
 
-ts_status ts_server_create(int32_t device, size_t budget, int32_t max_active, double chunk_ms, ts_server** out) {
-    if (!out) return ts::fail(TS_ERR_INVALID, "NULL argument");
+ts_status ts_server_create(const ts_server_config* cfg, ts_server** out) {
+    if (!out || !cfg) return ts::fail(TS_ERR_INVALID, "NULL argument");
     *out = nullptr;
-    if (max_active < 0 || chunk_ms < 0.0) return ts::fail(TS_ERR_INVALID, "bad argument");
+    if (cfg->max_active < 0 || cfg->chunk_ms < 0.0 || cfg->max_cells < 0 ||
+        (cfg->order != TS_SERVE_FIFO && cfg->order != TS_SERVE_SHORTEST_FIRST))
+        return ts::fail(TS_ERR_INVALID, "bad server configuration");
     std::unique_ptr<ts_server> s(new ts_server());
-    ts_status st = ts_batch_create(device, budget, &s->batch);
+    ts_status st = ts_batch_create(cfg->device, cfg->memory_budget, &s->batch);
     if (st != TS_OK) return st;
-    s->device = device;
-    s->budget = budget;
-    s->max_active = max_active;
-    s->chunk_ms = chunk_ms > 0.0 ? chunk_ms : 2.0;
+    s->device = cfg->device;
+    s->budget = cfg->memory_budget;
+    s->max_active = cfg->max_active;
+    s->order = cfg->order;
+    s->max_cells = cfg->max_cells;
+    s->chunk_ms = cfg->chunk_ms > 0.0 ? cfg->chunk_ms : 2.0;
     s->t0 = Clock::now();
     ts_server* p = s.get();
     s->worker = std::thread([p] { p->loop(); });
@@ -252,6 +273,8 @@ ts_status ts_server_submit(ts_server* s, const ts_config* cfg, const double* val
     r->values.assign(values, values + (size_t)r->cells * 5);
     r->keep = keep_state != 0;
     r->bytes = bytes;
+    // work: cell-updates when MaxIteration bounds the run, else cells
+    r->work = r->cells * (cfg->max_iteration > 0 && cfg->max_iteration < (1 << 30) ? cfg->max_iteration : 1.0);
     std::lock_guard<std::mutex> lk(s->mu);
     if (s->worker_status != TS_OK) return ts::fail(s->worker_status, "server stopped: " + s->worker_error);
     r->id = s->next_id++;
