@@ -628,6 +628,47 @@ def run_shear(args, rank, ws, lr, dist):
         print(json.dumps(line), flush=True)
 
 
+def run_batch2d(args, rank, ws, lr, dist):
+    """Steady-state capacity of the served kernel: a batch of 2D quadrant
+    problems (8 each of 1024^2, 512^2, 256^2; Roe and HLLC alternating)
+    advanced together; a step is one stage of the whole batch."""
+    import torch
+
+    from turbostructred_gb300 import build, capi, workloads
+    if rank == 0 or dist is None:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    capi.load()
+    quad = [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03, 0.53, 0.0, 1.2, 0.3]
+    b = capi.Batch(8 << 30, device=lr)
+    cells = 0
+    for k in range(24):
+        side = (1024, 512, 256)[k % 3]
+        c = workloads.quadrant_case(side, capi.RS_ROE if k % 2 else capi.RS_HLLC, 10**6)
+        b.add(c, workloads.stream_state(c, quad, k))
+        cells += side * side
+    b.step(args.warmup)
+    torch.cuda.synchronize()
+    sampler = ClockSampler(gpu_uuid(lr))
+    s0 = b.stats()
+    t0 = time.perf_counter()
+    b.step(args.steps)
+    t1 = time.perf_counter()
+    s1 = b.stats()
+    clocks = sampler.stop()
+    b.close()
+    value = ws * (s1["cell_updates"] - s0["cell_updates"]) / (t1 - t0)
+    if rank == 0:
+        print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
+                          "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (t1 - t0) / args.steps,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64 state / f32 flux", "data": "synthetic",
+                          "config": {"workload": "batch of 24 2D quadrant problems (8 x 1024^2, 8 x 512^2, "
+                                                 "8 x 256^2), Linear2psLim(BJ), Roe/HLLC", "cells": cells},
+                          "clocks": clocks, "gpu_launches": s1["launches"] - s0["launches"]}), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -644,7 +685,7 @@ def main():
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
-    p.add_argument("--workload", choices=["blast3d", "tubes", "served", "shear2d"], default="blast3d")
+    p.add_argument("--workload", choices=["blast3d", "tubes", "served", "shear2d", "batch2d"], default="blast3d")
     p.add_argument("--shear-steps", type=int, default=1000)
     p.add_argument("--skip-served", action="store_true")
     p.add_argument("--served-sample-seconds", type=float, default=10.0)
@@ -664,7 +705,8 @@ def main():
         run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))
         return
     rank, ws, lr, dist = dist_init()
-    {"blast3d": run_ours, "tubes": run_tubes, "served": run_served, "shear2d": run_shear}[args.workload](
+    {"blast3d": run_ours, "tubes": run_tubes, "served": run_served, "shear2d": run_shear,
+     "batch2d": run_batch2d}[args.workload](
         args, rank, ws, lr, dist)
     if dist is not None:
         dist.destroy_process_group()
