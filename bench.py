@@ -557,7 +557,8 @@ def run_served(args, rank, ws, lr, dist, emit=True):
                         "d2h_bytes_per_step": bytes_io / max(1, len(reqs)),
                         "note": "latency and throughput are end to end: host submit (copy of the initial state) "
                                 "to the final state back in host memory"},
-                "server": {k: st[k] for k in ("submitted", "completed", "rejected", "stages", "launches", "busy_s")},
+                "server": {k: st[k] for k in ("submitted", "completed", "rejected", "stages", "launches", "busy_s",
+                                              "admit_s", "retire_s")},
                 "offered_cell_updates_per_s": sum(c["nx"] * c["ny"] * args.served_steps for _, c, _, _ in reqs)
                 / args.seconds, "client_max_lateness_s": late, "wall_s": t_end,
                 "clocks": clocks, "gpu_launches": st["launches"] - st0["launches"]}

@@ -292,6 +292,14 @@ size_t ts_batch_problem_bytes(const ts_config* cfg);
 /* n_stages stages of every unfinished problem (finished ones are skipped). */
 ts_status ts_batch_step(ts_batch* b, int32_t n_stages);
 
+/* The same split in two: ts_batch_launch queues the stages and returns;
+   ts_batch_wait waits for them and refreshes every problem's step info
+   (*active: problems still running).  Between the two, ts_batch_add uploads
+   and ts_batch_get / ts_batch_remove of finished problems run beside the
+   queued stages (their own streams). */
+ts_status ts_batch_launch(ts_batch* b, int32_t n_stages);
+ts_status ts_batch_wait(ts_batch* b, int32_t* active);
+
 /* Stages until every problem has finished (MaxTime or MaxIteration), at most
    max_stages (<= 0: no limit).  *active receives the problems still running.
    A problem whose state turns non-physical (NaN, density <= 0) is stopped
@@ -347,7 +355,8 @@ typedef struct ts_server_stats {
     int64_t queued, active;            /* right now */
     int64_t stages, launches;          /* batch totals */
     double cell_updates;               /* of all solves, retired or running */
-    double busy_s;                     /* time the worker had solves admitted */
+    double busy_s;                     /* worker time advancing admitted solves */
+    double admit_s, retire_s;          /* worker time uploading admitted / reading back finished solves */
     double latency_p50_ms, latency_p99_ms, latency_max_ms;  /* submit -> finish, completed solves */
     double wait_p50_ms, wait_p99_ms;   /* submit -> admit */
     size_t bytes_budget, bytes_in_use;

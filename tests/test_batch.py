@@ -229,3 +229,35 @@ def test_batch_autotune_restores_state(tslib):
     for (g, gi), (r, ri) in zip(got, base):
         assert gi["iteration"] == 20
         assert relmax(g, r) <= 1e-5
+
+
+def test_batch_admission_and_retirement_beside_queued_stages(tslib):
+    """Problems added, read back and removed while stages are queued (the
+    served loop's pattern: ts_batch_launch, uploads and read-backs, then
+    ts_batch_wait) give the same results as the problems alone, bit for bit;
+    a removed problem's slot is not reused before the queued stages drain."""
+    from turbostructred_gb300 import capi
+    probs = mixed_problems()
+    alone = [run_batch([p])[0] for p in probs]
+    results = {}
+    with capi.Batch(BUDGET) as b:
+        owner = {}
+        pending = list(range(len(probs)))
+        for _ in range(2):
+            k = pending.pop(0)
+            owner[b.add(*probs[k])] = k
+        finished = []
+        while owner:
+            b.launch(5)
+            # beside the queued stages: admit one, retire what finished earlier
+            if pending:
+                k = pending.pop(0)
+                owner[b.add(*probs[k])] = k
+            for pid in finished:
+                results[owner.pop(pid)] = b.get(pid)
+                b.remove(pid)
+            b.wait()
+            finished = b.finished()
+    for k in range(len(probs)):
+        assert results[k][1]["iteration"] == alone[k][1]["iteration"]
+        assert np.array_equal(results[k][0], alone[k][0]), k

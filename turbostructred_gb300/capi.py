@@ -105,7 +105,8 @@ class RequestTimes(C.Structure):
 class ServerStats(C.Structure):
     _fields_ = [(n, C.c_int64) for n in ("submitted", "admitted", "completed", "rejected", "queued", "active",
                                          "stages", "launches")] + \
-               [(n, C.c_double) for n in ("cell_updates", "busy_s", "latency_p50_ms", "latency_p99_ms",
+               [(n, C.c_double) for n in ("cell_updates", "busy_s", "admit_s", "retire_s", "latency_p50_ms",
+                                          "latency_p99_ms",
                                           "latency_max_ms", "wait_p50_ms", "wait_p99_ms")] + \
                [("bytes_budget", C.c_size_t), ("bytes_in_use", C.c_size_t), ("worker_status", C.c_int)]
 
@@ -120,7 +121,7 @@ EXPORTS = [
     "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
     "ts_batch_create", "ts_batch_destroy", "ts_batch_add", "ts_batch_problem_bytes", "ts_batch_step",
     "ts_batch_run", "ts_batch_finished", "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile",
-    "ts_batch_autotune", "ts_batch_stats",
+    "ts_batch_autotune", "ts_batch_stats", "ts_batch_launch", "ts_batch_wait",
     "ts_server_create", "ts_server_destroy", "ts_server_submit", "ts_server_wait", "ts_server_drain",
     "ts_server_stats_get",
     "ts_save_solution", "ts_load_solution", "ts_save_tecplot", "ts_wait_writes", "ts_write_solution_file",
@@ -173,6 +174,10 @@ def load(path: str = LIB_PATH):
     L.ts_batch_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
     L.ts_batch_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     L.ts_batch_stats.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), P(C.c_int64)]
+    L.ts_batch_launch.argtypes = [C.c_void_p, C.c_int32]
+    L.ts_batch_wait.argtypes = [C.c_void_p, P(C.c_int32)]
+    L.ts_batch_launch.restype = C.c_int
+    L.ts_batch_wait.restype = C.c_int
     for name in ("ts_batch_create", "ts_batch_add", "ts_batch_step", "ts_batch_run", "ts_batch_finished",
                  "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile", "ts_batch_autotune", "ts_batch_stats"):
         getattr(L, name).restype = C.c_int
@@ -458,6 +463,14 @@ class Batch:
     def run(self, max_stages: int = 0) -> int:
         a = C.c_int32()
         check(self.lib.ts_batch_run(self.b, max_stages, C.byref(a)))
+        return a.value
+
+    def launch(self, n: int):
+        check(self.lib.ts_batch_launch(self.b, n))
+
+    def wait(self) -> int:
+        a = C.c_int32()
+        check(self.lib.ts_batch_wait(self.b, C.byref(a)))
         return a.value
 
     def finished(self, cap: int = 1 << 16) -> list:

@@ -180,8 +180,16 @@ struct ts_batch {
     int stable = 0;  // launches since the work list last changed
     std::map<int, cudaGraphExec_t> graphs;
     Tune tune[4] = {{0, 0, 0}, {0, 1, 0}, {0, 1, 0}, {0, 0, 0}};
-    double* stage_buf = nullptr;
-    size_t stage_doubles = 0;
+    // uploads of admitted problems and read-backs of finished ones run on
+    // their own streams (with their own staging buffers), so they overlap
+    // stages queued on the main stream
+    cudaStream_t ustream = nullptr, dstream = nullptr;
+    cudaEvent_t uploaded = nullptr;
+    double* ustage = nullptr;
+    size_t ustage_doubles = 0;
+    double* dstage = nullptr;
+    size_t dstage_doubles = 0;
+    std::vector<int> quarantine;  // removed slots, reusable once the main stream has drained
     double done_cell_updates = 0.0;  // of removed problems
     long long stages = 0, launches = 0;
 
@@ -200,7 +208,11 @@ struct ts_batch {
         cudaFree(d_desc);
         cudaFree(d_ctl);
         cudaFreeHost(h_ctl);
-        cudaFree(stage_buf);
+        cudaFree(ustage);
+        cudaFree(dstage);
+        if (ustream) cudaStreamDestroy(ustream);
+        if (dstream) cudaStreamDestroy(dstream);
+        if (uploaded) cudaEventDestroy(uploaded);
         if (stream) cudaStreamDestroy(stream);
         if (prev >= 0) cudaSetDevice(prev);
     }
@@ -395,6 +407,9 @@ struct ts_batch {
     ts_status pull() {
         TB_CUDA(cudaMemcpyAsync(h_ctl, d_ctl, sizeof(Ctl) * capacity, cudaMemcpyDeviceToHost, stream));
         TB_CUDA(cudaStreamSynchronize(stream));
+        // the main stream has drained: removed slots can be reused
+        for (int q : quarantine) slots[q].used = false;
+        quarantine.clear();
         for (int s = 0; s < capacity; ++s) {
             if (!slots[s].used || h_ctl[s].stop_req || !h_ctl[s].health) continue;
             h_ctl[s].stop_req = 1;
@@ -463,6 +478,9 @@ ts_status ts_batch_create(int32_t device, size_t budget, ts_batch** out) {
         TB_CUDA(cudaEventCreateWithFlags(&b->join[k], cudaEventDisableTiming));
     }
     TB_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+    TB_CUDA(cudaStreamCreateWithFlags(&b->ustream, cudaStreamNonBlocking));
+    TB_CUDA(cudaStreamCreateWithFlags(&b->dstream, cudaStreamNonBlocking));
+    TB_CUDA(cudaEventCreateWithFlags(&b->uploaded, cudaEventDisableTiming));
     TB_CUDA(b->arena.init(budget));
     ts_status s = b->grow(64);
     if (s != TS_OK) return s;
@@ -520,18 +538,22 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
         if ((s = take(sizeof(float) * NV * L.plane, (void**)&d.R[k])) != TS_OK) { undo(); return s; }
     }
     b->place(slot);
-    // initial state: host -> staging -> U[0]; no pending residual
+    // initial state: host -> staging -> U[0]; no pending residual.  All on the
+    // upload stream; the main stream waits for it before its next work, so
+    // stages already queued there keep running meanwhile.
     const size_t nvals = (size_t)L.cells() * NV;
-    if (b->stage_doubles < nvals) {
-        cudaFree(b->stage_buf);
-        b->stage_buf = nullptr;
-        b->stage_doubles = 0;
-        if (cudaMalloc(&b->stage_buf, nvals * sizeof(double)) != cudaSuccess) { undo(); return fail(TS_ERR_NO_MEMORY, "staging buffer"); }
-        b->stage_doubles = nvals;
+    if (b->ustage_doubles < nvals) {
+        TB_CUDA(cudaStreamSynchronize(b->ustream));
+        cudaFree(b->ustage);
+        b->ustage = nullptr;
+        b->ustage_doubles = 0;
+        if (cudaMalloc(&b->ustage, nvals * sizeof(double)) != cudaSuccess) { undo(); return fail(TS_ERR_NO_MEMORY, "staging buffer"); }
+        b->ustage_doubles = nvals;
     }
-    TB_CUDA(cudaMemcpyAsync(b->stage_buf, values, nvals * sizeof(double), cudaMemcpyHostToDevice, b->stream));
-    k_b_scatter<<<(unsigned)((L.cells() + 255) / 256), 256, 0, b->stream>>>(b->stage_buf, L, d.U[0]);
-    TB_CUDA(cudaMemsetAsync(d.R[0], 0, sizeof(float) * NV * L.plane, b->stream));
+    cudaStream_t us = b->ustream;
+    TB_CUDA(cudaMemcpyAsync(b->ustage, values, nvals * sizeof(double), cudaMemcpyHostToDevice, us));
+    k_b_scatter<<<(unsigned)((L.cells() + 255) / 256), 256, 0, us>>>(b->ustage, L, d.U[0]);
+    TB_CUDA(cudaMemsetAsync(d.R[0], 0, sizeof(float) * NV * L.plane, us));
     Ctl& c = b->h_ctl[slot];
     std::memset(&c, 0, sizeof c);
     c.next_sol = cfg->save_solution_time;
@@ -541,9 +563,13 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
     c.max_iteration = cfg->max_iteration;
     c.max_time = cfg->max_time;
     c.run_mode = 1;
-    TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &c, sizeof(Ctl), cudaMemcpyHostToDevice, b->stream));
-    TB_CUDA(cudaMemcpyAsync(b->d_desc + slot, &d, sizeof(ProbDesc), cudaMemcpyHostToDevice, b->stream));
-    TB_CUDA(cudaStreamSynchronize(b->stream));
+    TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &c, sizeof(Ctl), cudaMemcpyHostToDevice, us));
+    TB_CUDA(cudaMemcpyAsync(b->d_desc + slot, &d, sizeof(ProbDesc), cudaMemcpyHostToDevice, us));
+    TB_CUDA(cudaEventRecord(b->uploaded, us));
+    TB_CUDA(cudaStreamWaitEvent(b->stream, b->uploaded, 0));
+    // the caller may reuse `values` on return; the upload stream only (not the
+    // stages queued on the main stream) has to finish for that
+    TB_CUDA(cudaStreamSynchronize(us));
     sl.used = true;
     sl.id = b->next_id++;
     sl.cells = L.cells();
@@ -551,6 +577,24 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
     b->id2slot[sl.id] = slot;
     b->dirty = true;
     *id = sl.id;
+    return TS_OK;
+}
+
+ts_status ts_batch_launch(ts_batch* b, int32_t n) {
+    if (!b || n < 0) return fail(TS_ERR_INVALID, "bad argument");
+    DevGuard g(b->device);
+    long long ia, il;
+    b->active(&ia, &il);
+    if (2 * ia < il) b->dirty = true;  // most listed items belong to finished problems
+    return b->launch(n);
+}
+
+ts_status ts_batch_wait(ts_batch* b, int32_t* active) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    DevGuard g(b->device);
+    ts_status s = b->pull();
+    if (s != TS_OK) return s;
+    if (active) *active = b->active(nullptr, nullptr);
     return TS_OK;
 }
 
@@ -591,7 +635,7 @@ ts_status ts_batch_finished(ts_batch* b, int32_t* ids, int32_t cap, int32_t* n) 
     int k = 0;
     for (int s = 0; s < b->capacity; ++s) {
         Slot& sl = b->slots[s];
-        if (!sl.used || sl.collected || !b->h_ctl[s].stop_req) continue;
+        if (!sl.used || sl.id < 0 || sl.collected || !b->h_ctl[s].stop_req) continue;
         if (k < cap && ids) { ids[k] = sl.id; sl.collected = true; }
         ++k;
     }
@@ -607,21 +651,28 @@ ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* in
     DevGuard g(b->device);
     const Layout& L = b->desc[slot].L;
     const unsigned blocks = (unsigned)((L.cells() + 255) / 256);
-    mixed_apply(b->d_desc, slot, L.cells(), b->stream);
+    // A finished problem is no longer touched by stages (its items skip), so
+    // its read-back runs on the download stream beside whatever is queued on
+    // the main stream; a running one is read in stream order.
+    const bool finished = b->h_ctl[slot].stop_req != 0;
+    cudaStream_t st = finished ? b->dstream : b->stream;
+    mixed_apply(b->d_desc, slot, L.cells(), st);
     if (values) {
         const size_t nvals = (size_t)L.cells() * NV;
-        if (b->stage_doubles < nvals) {
-            cudaFree(b->stage_buf);
-            b->stage_buf = nullptr;
-            b->stage_doubles = 0;
-            TB_CUDA(cudaMalloc(&b->stage_buf, nvals * sizeof(double)));
-            b->stage_doubles = nvals;
+        if (b->dstage_doubles < nvals) {
+            cudaFree(b->dstage);
+            b->dstage = nullptr;
+            b->dstage_doubles = 0;
+            TB_CUDA(cudaMalloc(&b->dstage, nvals * sizeof(double)));
+            b->dstage_doubles = nvals;
         }
-        k_b_gather<<<blocks, 256, 0, b->stream>>>(b->stage_buf, b->d_desc, slot);
+        k_b_gather<<<blocks, 256, 0, st>>>(b->dstage, b->d_desc, slot);
         TB_CUDA(cudaGetLastError());
-        TB_CUDA(cudaMemcpyAsync(values, b->stage_buf, nvals * sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+        TB_CUDA(cudaMemcpyAsync(values, b->dstage, nvals * sizeof(double), cudaMemcpyDeviceToHost, st));
     }
-    ts_status s = b->pull();
+    ts_status s = TS_OK;
+    if (finished) TB_CUDA(cudaStreamSynchronize(st));
+    else s = b->pull();
     if (s != TS_OK) return s;
     if (info) {
         const Ctl& c = b->h_ctl[slot];
@@ -641,12 +692,19 @@ ts_status ts_batch_remove(ts_batch* b, int32_t id) {
     auto it = b->id2slot.find(id);
     if (it == b->id2slot.end()) return fail(TS_ERR_NOT_FOUND, "unknown problem id");
     DevGuard g(b->device);
-    TB_CUDA(cudaStreamSynchronize(b->stream));
     const int slot = it->second;
+    // a running problem may still be read by queued stages: drain them first.
+    // A finished one is skipped by them, so its memory is free at once; its
+    // slot waits until the main stream has drained (the work lists queued
+    // there still name it).
+    if (!b->h_ctl[slot].stop_req) TB_CUDA(cudaStreamSynchronize(b->stream));
+    TB_CUDA(cudaStreamSynchronize(b->dstream));
     Slot& sl = b->slots[slot];
     b->done_cell_updates += (double)sl.cells * (double)b->h_ctl[slot].iteration;
     for (void* p : sl.mem) b->arena.give(p);
     sl = Slot();
+    sl.used = true;  // quarantined until the next drain
+    b->quarantine.push_back(slot);
     std::memset(&b->h_ctl[slot], 0, sizeof(Ctl));
     b->h_ctl[slot].stop_req = 1;
     TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &b->h_ctl[slot], sizeof(Ctl), cudaMemcpyHostToDevice, b->stream));
@@ -668,7 +726,7 @@ ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int
     TB_CUDA(cudaStreamSynchronize(b->stream));
     b->tune[nd] = Tune{tx, ty, ctas};
     for (int s = 0; s < b->capacity; ++s) {
-        if (!b->slots[s].used || b->desc[s].L.nd != nd) continue;
+        if (!b->slots[s].used || b->slots[s].id < 0 || b->desc[s].L.nd != nd) continue;
         b->place(s);
         TB_CUDA(cudaMemcpyAsync(b->d_desc + s, &b->desc[s], sizeof(ProbDesc), cudaMemcpyHostToDevice, b->stream));
     }
@@ -685,7 +743,7 @@ ts_status ts_batch_autotune(ts_batch* b, int32_t stages, int32_t* tx_out, int32_
     // dominant dimension by cells
     long long cells[3] = {0, 0, 0};
     for (int k = 0; k < b->capacity; ++k)
-        if (b->slots[k].used) cells[b->desc[k].L.nd] += b->slots[k].cells;
+        if (b->slots[k].used && b->slots[k].id >= 0) cells[b->desc[k].L.nd] += b->slots[k].cells;
     const int nd = cells[2] > cells[1] ? 2 : 1;
     if (cells[nd] == 0) return fail(TS_ERR_INVALID, "empty batch");
     // snapshot: the arena up to its high-water mark and the control words

@@ -76,7 +76,7 @@ struct ts_server {
     std::vector<double> lat_ms, wait_ms;
     int64_t submitted = 0, admitted = 0, completed = 0, rejected = 0;
     int64_t stages = 0, launches = 0;
-    double cell_updates = 0.0, busy_s = 0.0;
+    double cell_updates = 0.0, busy_s = 0.0, admit_s = 0.0, retire_s = 0.0;
     size_t in_use = 0;
     double in_cells = 0.0;
     ts_status worker_status = TS_OK;
@@ -114,18 +114,28 @@ struct ts_server {
         cv_done.notify_all();
     }
 
+    // One pass: admit (uploads overlap the chunk in flight), retire what the
+    // last wait found finished (read-backs overlap it too), wait for the
+    // chunk, launch the next one.
     void loop() {
         int chunk = 4;
-        std::vector<int32_t> fin(1024);
+        bool in_flight = false;
+        int32_t active = 0;
+        Clock::time_point launched = Clock::now();
+        std::vector<int32_t> fin(1024), to_retire;
         for (;;) {
             std::vector<Req> admit;
             {
                 std::unique_lock<std::mutex> lk(mu);
-                if (running.empty()) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
-                if (stop) return;
+                if (running.empty() && !in_flight) cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+                if (stop) {
+                    lk.unlock();
+                    if (in_flight) ts_batch_wait(batch, &active);
+                    return;
+                }
                 if (order == TS_SERVE_SHORTEST_FIRST)
                     std::stable_sort(queue.begin(), queue.end(),
-                                     [](const Req& a, const Req& b) { return a.get()->work < b.get()->work; });
+                                     [](const Req& x, const Req& y) { return x.get()->work < y.get()->work; });
                 size_t room = budget - in_use;
                 double cells = in_cells;
                 while (!queue.empty()) {
@@ -140,6 +150,8 @@ struct ts_server {
                     queue.pop_front();
                 }
             }
+            const Clock::time_point a0 = Clock::now();
+            int added = 0;
             for (size_t k = 0; k < admit.size(); ++k) {
                 const Req& r = admit[k];
                 int32_t bid = -1;
@@ -156,6 +168,7 @@ struct ts_server {
                     cv_done.notify_all();
                     continue;
                 }
+                ++added;
                 r->batch_id = bid;
                 r->t.admit_s = now();
                 if (!r->keep) std::vector<double>().swap(r->values);
@@ -165,51 +178,63 @@ struct ts_server {
                 ++admitted;
                 wait_ms.push_back(1e3 * (r->t.admit_s - r->t.submit_s));
             }
+            const Clock::time_point r0 = Clock::now();
+            ts_status s = TS_OK;
+            for (int32_t bid : to_retire) {
+                Req r;
+                {
+                    std::lock_guard<std::mutex> lk(mu);
+                    auto it = running.find(bid);
+                    if (it == running.end()) continue;
+                    r = it->second;
+                }
+                s = ts_batch_get(batch, bid, r->keep ? r->values.data() : nullptr, &r->info);
+                if (s == TS_OK) s = ts_batch_remove(batch, bid);
+                if (s != TS_OK) break;
+                std::lock_guard<std::mutex> lk(mu);
+                running.erase(bid);
+                in_use -= r->bytes;
+                in_cells -= r->cells;
+                retire(r, TS_OK, "");
+                cv_done.notify_all();
+            }
+            to_retire.clear();
+            if (s != TS_OK) { worker_failed(s); return; }
+            const Clock::time_point w0 = Clock::now();
             {
                 std::lock_guard<std::mutex> lk(mu);
-                if (running.empty()) continue;
+                admit_s += std::chrono::duration<double>(r0 - a0).count();
+                retire_s += std::chrono::duration<double>(w0 - r0).count();
             }
-            const Clock::time_point c0 = Clock::now();
-            int32_t active = 0;
-            ts_status s = ts_batch_run(batch, chunk, &active);
-            if (s != TS_OK) { worker_failed(s); return; }
-            const double el = std::chrono::duration<double>(Clock::now() - c0).count();
-            // next chunk: about chunk_ms of stages at the current rate
-            const double per_stage_ms = std::max(1e3 * el / chunk, 1e-3);
-            chunk = std::min(std::max((int)(chunk_ms / per_stage_ms), 1), 4096);
-            // retire finished solves
-            for (;;) {
-                int32_t n = 0;
-                if ((s = ts_batch_finished(batch, fin.data(), (int32_t)fin.size(), &n)) != TS_OK) break;
-                for (int32_t k = 0; k < n; ++k) {
-                    Req r;
-                    {
-                        std::lock_guard<std::mutex> lk(mu);
-                        auto it = running.find(fin[k]);
-                        if (it == running.end()) continue;
-                        r = it->second;
-                    }
-                    s = ts_batch_get(batch, fin[k], r->keep ? r->values.data() : nullptr, &r->info);
-                    if (s == TS_OK) s = ts_batch_remove(batch, fin[k]);
-                    if (s != TS_OK) break;
-                    std::lock_guard<std::mutex> lk(mu);
-                    running.erase(fin[k]);
-                    in_use -= r->bytes;
-                    in_cells -= r->cells;
-                    retire(r, TS_OK, "");
+            if (in_flight) {
+                if ((s = ts_batch_wait(batch, &active)) != TS_OK) { worker_failed(s); return; }
+                in_flight = false;
+                const double el = std::chrono::duration<double>(Clock::now() - launched).count();
+                // next chunk: about chunk_ms of stages at the current rate
+                const double per_stage_ms = std::max(1e3 * el / chunk, 1e-3);
+                chunk = std::min(std::max((int)(chunk_ms / per_stage_ms), 1), 4096);
+                for (;;) {
+                    int32_t n = 0;
+                    if ((s = ts_batch_finished(batch, fin.data(), (int32_t)fin.size(), &n)) != TS_OK) break;
+                    to_retire.insert(to_retire.end(), fin.begin(), fin.begin() + n);
+                    if (n < (int32_t)fin.size()) break;
                 }
-                if (s != TS_OK || n < (int32_t)fin.size()) break;
+                if (s != TS_OK) { worker_failed(s); return; }
+                double cu = 0.0;
+                int64_t st = 0, la = 0;
+                ts_batch_stats(batch, &cu, &st, &la);
+                std::lock_guard<std::mutex> lk(mu);
+                busy_s += el;
+                cell_updates = cu;
+                stages = st;
+                launches = la;
             }
-            if (s != TS_OK) { worker_failed(s); return; }
-            double cu = 0.0;
-            int64_t st = 0, la = 0;
-            ts_batch_stats(batch, &cu, &st, &la);
-            std::lock_guard<std::mutex> lk(mu);
-            busy_s += el;
-            cell_updates = cu;
-            stages = st;
-            launches = la;
-            cv_done.notify_all();
+            if (active > 0 || added > 0) {
+                launched = Clock::now();
+                if ((s = ts_batch_launch(batch, chunk)) != TS_OK) { worker_failed(s); return; }
+                in_flight = true;
+                active = std::max(active, added);
+            }
         }
     }
 };
@@ -332,6 +357,8 @@ ts_status ts_server_stats_get(ts_server* s, ts_server_stats* o) {
     o->launches = s->launches;
     o->cell_updates = s->cell_updates;
     o->busy_s = s->busy_s;
+    o->admit_s = s->admit_s;
+    o->retire_s = s->retire_s;
     o->latency_p50_ms = percentile(s->lat_ms, 50.0);
     o->latency_p99_ms = percentile(s->lat_ms, 99.0);
     o->latency_max_ms = s->lat_ms.empty() ? 0.0 : *std::max_element(s->lat_ms.begin(), s->lat_ms.end());
