@@ -218,6 +218,38 @@ def run_reference(args, rank, ws):
                 "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
+    if args.workload in ("shear2d", "batch2d"):
+        # the reference algorithm (oracle port, OpenMP over all host threads)
+        # on the same 2D grids: the 1024^2 shear layer, or one 512^2 quadrant
+        # problem of the batch, for a bounded number of steps
+        from oracle import oracle as O
+        from turbostructred_gb300 import capi, workloads
+        if args.workload == "shear2d":
+            case = capi.make_case(ndims=2, nx=1024, ny=1024, periodic=(1, 1, 1), recon=capi.RECON_LINEAR2_LIM,
+                                  solver=capi.RS_HLLC, cfl=0.4, max_iter=10**6, max_time=1e30)
+            ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7, [2.0, 1.0, 0.5, 2.5, 0.01])
+            steps, sample = 60, "60 RK steps of the 1024^2 shear layer"
+        else:
+            case = workloads.quadrant_case(512, capi.RS_ROE, 10**6)
+            ic = workloads.stream_state(case, [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03,
+                                               0.53, 0.0, 1.2, 0.3], 1)
+            steps, sample = 120, "120 RK steps of one 512^2 quadrant problem of the batch"
+        full = O.embed(case, ic)
+        full, _ = O.advance(case, full, 2, threads=threads)
+        t0 = time.perf_counter()
+        O.advance(case, full, steps, threads=threads)
+        secs = time.perf_counter() - t0
+        cells = case["nx"] * case["ny"]
+        rate = cells * steps / secs
+        line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
+                "steps": steps, "warmup": 2, "ms_per_step": 1e3 * secs / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+                "config": {"workload": args.workload, "sample": sample},
+                "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                                 "sample": sample},
+                "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
     rate, secs, sample = oracle_sample_rate(args.steps, args.warmup, threads)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
@@ -649,6 +681,7 @@ def run_batch2d(args, rank, ws, lr, dist):
         c = workloads.quadrant_case(side, capi.RS_ROE if k % 2 else capi.RS_HLLC, 10**6)
         b.add(c, workloads.stream_state(c, quad, k))
         cells += side * side
+    choice = b.autotune(args.tune_stages) if args.tune_stages > 0 else None
     b.step(args.warmup)
     torch.cuda.synchronize()
     sampler = ClockSampler(gpu_uuid(lr))
@@ -666,7 +699,8 @@ def run_batch2d(args, rank, ws, lr, dist):
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
                           "dtype": "f64 state / f32 flux", "data": "synthetic",
                           "config": {"workload": "batch of 24 2D quadrant problems (8 x 1024^2, 8 x 512^2, "
-                                                 "8 x 256^2), Linear2psLim(BJ), Roe/HLLC", "cells": cells},
+                                                 "8 x 256^2), Linear2psLim(BJ), Roe/HLLC", "cells": cells,
+                                     "tile": choice},
                           "clocks": clocks, "gpu_launches": s1["launches"] - s0["launches"]}), flush=True)
 
 

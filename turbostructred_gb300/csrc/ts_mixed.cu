@@ -1179,7 +1179,9 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
     int dev = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&mb.sms, cudaDevAttrMultiProcessorCount, dev);
-    const int tx = L.nd == 3 ? 32 : (L.nd == 2 ? 260 : 256);
+    // 2D: 132-thread rows (measured on the 1024^2 shear layer: 13.3e9 against
+    // 12.2e9 cell-updates/s for 260-thread rows)
+    const int tx = L.nd == 3 ? 32 : (L.nd == 2 ? 132 : 256);
     const int ty = L.nd == 3 ? 8 : 1;
     return mixed_set_tile(mb, tx, ty, 0, err);
 }
