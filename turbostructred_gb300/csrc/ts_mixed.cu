@@ -254,7 +254,10 @@ struct Tile {
     static constexpr int NRING = RX * RY;
     static constexpr int NA = (NBOX + NT - 1) / NT;        // box positions per thread
     static constexpr int NB = (NRING + NT - 1) / NT;       // ring positions per thread
-    static constexpr int WS = MARCH ? 3 : 1;               // working-state planes kept
+    // two-axis tiles march in two phases per plane (four working-state
+    // planes live), one-row tiles in three (three planes live)
+    static constexpr bool TWO_PHASE = HAS_Y && MARCH;
+    static constexpr int WS = MARCH ? (TWO_PHASE ? 4 : 3) : 1;  // working-state planes kept
     static constexpr int DS = MARCH ? 2 : 1;               // slope planes kept
     static constexpr int W_OFF = 0;
     static constexpr int D_OFF = W_OFF + WS * NV * NBOX;
@@ -270,6 +273,7 @@ struct Tile {
     static constexpr int WARPS = (NT + 31) / 32;
     static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : (24 + WARPS - 1) / WARPS);
 
+    static __device__ __forceinline__ int wslot(int p) { return TWO_PHASE ? (p & 3) : (p + 3) % 3; }
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
     static __device__ __forceinline__ int d(int s, int ax, int v, int ring) {
         return D_OFF + ((s * NAX + ax) * NV + v) * NRING + ring;
@@ -294,7 +298,6 @@ __device__ __forceinline__ constexpr int phys_axis() {
     return AX == 0 ? 0 : (AX == 1 ? 1 : (T::HAS_Y ? 2 : 1));
 }
 
-__device__ __forceinline__ int wslot(int p) { return (p + 3) % 3; }
 __device__ __forceinline__ int dslot(int p) { return (p + 2) & 1; }
 
 // One working-state position of a thread: where its source cell lives in a
@@ -380,7 +383,7 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
     const int sk = plane_of<T>(d, p, zs);
     const long long zoff = d.kbase + sk * d.kstr[2];
     const float cfz = dtf * __ldg(&d.kgeo[2][sk + d.kgoff[2]].ih);
-    const int slot = T::MARCH ? wslot(p) : 0;
+    const int slot = T::MARCH ? T::wslot(p) : 0;
     const bool own_plane = p >= z0 && p < z1;
 #pragma unroll
     for (int k = 0; k < T::NA; ++k) {
@@ -406,7 +409,11 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
                 un[v] = pf[k].u[v] + f32_to_f64(inc[v]);
                 __stcg(Uout + v * plane + c, un[v]);
             }
-            if (!(un[0] > 0.0)) health |= (un[0] == un[0]) ? TS_HEALTH_NEG_DENSITY : TS_HEALTH_NAN;
+            // rho > 0 tested on the bit pattern (no FP64 comparison): positive
+            // finite values and +inf are the integers 1 .. 0x7FF0000000000000
+            const long long b = __double_as_longlong(un[0]);
+            if (b <= 0 || b > 0x7FF0000000000000LL)
+                health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
             if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
         }
     }
@@ -423,7 +430,7 @@ template <class T>
 __device__ __forceinline__ Slots slots_of(int p) {
     Slots s;
     if (T::MARCH) {
-        s.wm = wslot(p - 1); s.w0 = wslot(p); s.wp = wslot(p + 1);
+        s.wm = T::wslot(p - 1); s.w0 = T::wslot(p); s.wp = T::wslot(p + 1);
         s.d0 = dslot(p); s.d1 = dslot(p + 1);
     } else {
         s.wm = s.w0 = s.wp = 0;
@@ -439,11 +446,19 @@ struct RingPos {
     int g0, g1;   // geometry indices along kernel axes 0 and 1
 };
 
+// Ring position of round k of this thread.  Second rounds run from the last
+// thread down: the first threads already have a second working-state
+// position, so the extra work of the two phases lands on different warps.
+template <class T>
+__device__ __forceinline__ int ring_index(int k) {
+    return k == 0 ? (int)threadIdx.x : k * T::NT + (T::NT - 1 - (int)threadIdx.x);
+}
+
 template <class T>
 __device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, int j0, RingPos (&rp)[T::NB]) {
 #pragma unroll
     for (int k = 0; k < T::NB; ++k) {
-        const int t = threadIdx.x + k * T::NT;
+        const int t = ring_index<T>(k);
         rp[k].box = -1;
         if (t >= T::NRING) continue;
         const int rx = t % T::RX, ry = t / T::RX;
@@ -490,7 +505,7 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
 #pragma unroll
     for (int k = 0; k < T::NB; ++k) {
         if (rp[k].box < 0) continue;
-        const int t = threadIdx.x + k * T::NT;
+        const int t = ring_index<T>(k);
         const int box = rp[k].box;
         AxisGeo g[3];
         g[0] = d.kgeo[0][rp[k].g0];
@@ -782,10 +797,12 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         const float4 own = src ? own_state<T>(sm, s) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
         residual<T>(d, sm, Rout, i0, j0, 0, s, own, srmax);
-    } else {
+    } else if constexpr (!T::TWO_PHASE) {
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
         // build the slopes of planes z0-1, z0 and the marching face z0-1/2.
+        // Each pass: store plane z+2, slopes of plane z+1, faces of plane z,
+        // residual of plane z (three barriers).
         issue<T>(d, Uin, Rin, z0 - 2, bp, pf);
         store<T>(d, sm, Uout, z0 - 2, z0, z1, dtf, bp, pf, health);
         issue<T>(d, Uin, Rin, z0 - 1, bp, pf);
@@ -803,6 +820,41 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             const float4 own = src && z >= z0 ? own_state<T>(sm, sf) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
             __syncthreads();
             if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, sf, own, srmax);
+        }
+    } else {
+        const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
+        // Planes z0-2 .. z1+1 are loaded.  Pass P has two phases:
+        //   A: store plane P+2, slopes of plane P, residual of plane P-2;
+        //   B: faces of plane P-1 (axes 0, 1) and the marching face P-1/P.
+        // Four working-state planes (P-1 .. P+2) and two slope planes are
+        // live, so the two phases need one barrier each.
+        issue<T>(d, Uin, Rin, z0 - 2, bp, pf);
+        store<T>(d, sm, Uout, z0 - 2, z0, z1, dtf, bp, pf, health);
+        issue<T>(d, Uin, Rin, z0 - 1, bp, pf);
+        store<T>(d, sm, Uout, z0 - 1, z0, z1, dtf, bp, pf, health);
+        issue<T>(d, Uin, Rin, z0, bp, pf);
+        store<T>(d, sm, Uout, z0, z0, z1, dtf, bp, pf, health);
+        issue<T>(d, Uin, Rin, z0 + 1, bp, pf);
+        __syncthreads();
+        float4 own = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+#pragma unroll 1
+        for (int P = z0 - 1; P <= z1 + 1; ++P) {
+            // plane P+2 was prefetched during the previous pass
+            if (P + 2 <= z1 + 1) {
+                store<T>(d, sm, Uout, P + 2, z0, z1, dtf, bp, pf, health);
+                if (P + 3 <= z1 + 1) issue<T>(d, Uin, Rin, P + 3, bp, pf);
+            }
+            if (!pwc && P <= z1) recon<T>(d, sm, P, kind, slots_of<T>(P), rp);
+            if (P - 2 >= z0) residual<T>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, srmax);
+            if (P > z1) break;
+            __syncthreads();
+            if (P < z0) continue;
+            const Slots sf = slots_of<T>(P - 1);
+            fluxes<T, SOLVER>(d, sm, i0, j0, P - 1, pwc, P - 1 >= z0, true, sf);
+            // the residual of plane P-1 runs in the next pass, after the
+            // store that reuses this working-state slot
+            if (src && P - 1 >= z0) own = own_state<T>(sm, sf);
+            __syncthreads();
         }
     }
 }
