@@ -128,7 +128,8 @@ __device__ __forceinline__ float pick3(int a, float x, float y, float z) { retur
 // ---------------------------------------------------------------------------
 
 // Roe-Pike flux (RoeSolverPerfectGasEOS.h:74-160) in the equivalent form
-// 1/2 [F(UL) + F(UR) + |A|(UL - UR)], |A| dU = a1 dU + Ac Qa + Bc Qb with
+// 1/2 [F(UL) + F(UR) + |A|(UL - UR)], returned without the factor 1/2
+// (flux_scale<SOLVER>), |A| dU = a1 dU + Ac Qa + Bc Qb with
 // Qa = (0, e_A, un), Qb = (1, u, H), Ac = Ea dR + Eb dD, Bc = Ea dD + Eb dR / c^2.
 template <int A>
 __device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
@@ -165,11 +166,12 @@ __device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], con
     const float Bc = Ea * dD + Eb * dR * (ic * ic);
     const float unl = pick3(A, ulx, uly, ulz), unr = pick3(A, urx, ury, urz);
     const float pn = pl + pr + Ac;
-    F[0] = 0.5f * (UL[0] * unl + UR[0] * unr + a1 * dr + Bc);
-    F[1] = 0.5f * (UL[1] * unl + UR[1] * unr + (A == 0 ? pn : 0.0f) + a1 * dmx + Bc * ux);
-    F[2] = 0.5f * (UL[2] * unl + UR[2] * unr + (A == 1 ? pn : 0.0f) + a1 * dmy + Bc * uy);
-    F[3] = 0.5f * (UL[3] * unl + UR[3] * unr + (A == 2 ? pn : 0.0f) + a1 * dmz + Bc * uz);
-    F[4] = 0.5f * (el * unl + er * unr + a1 * de + Ac * un + Bc * h);
+    // twice the flux: the factor 1/2 is applied with the face areas
+    F[0] = UL[0] * unl + UR[0] * unr + a1 * dr + Bc;
+    F[1] = UL[1] * unl + UR[1] * unr + (A == 0 ? pn : 0.0f) + a1 * dmx + Bc * ux;
+    F[2] = UL[2] * unl + UR[2] * unr + (A == 1 ? pn : 0.0f) + a1 * dmy + Bc * uy;
+    F[3] = UL[3] * unl + UR[3] * unr + (A == 2 ? pn : 0.0f) + a1 * dmz + Bc * uz;
+    F[4] = el * unl + er * unr + a1 * de + Ac * un + Bc * h;
     return lam;
 }
 
@@ -219,6 +221,10 @@ __device__ __forceinline__ float hllc32(const MixPhys& p, const float UL[NV], co
     }
     return fmaxf(fabsf(SL), fabsf(SR));
 }
+
+// Factor between the stored face flux and the flux.
+template <int SOLVER>
+__device__ __forceinline__ constexpr float flux_scale() { return SOLVER == TS_RS_HLLC ? 1.0f : 0.5f; }
 
 template <int SOLVER, int A>
 __device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
@@ -538,7 +544,23 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
             }
-            if (KIND == RK_LIM_BJ || KIND == RK_LIM_VK) {
+            if (KIND == RK_LIM_BJ) {
+                // Barth-Jespersen (Limiters.h:74-83): the smallest admissible
+                // ratio over the 2*nd face projections +-dd.  Branch-free: with
+                // dmax = 0 every dd is 0 and the ratio (0/0 or x/0) is dropped
+                // by fminf, so lim = 1 as in the reference.
+                float umax = w0, umin = w0, dmax = 0.0f;
+#pragma unroll
+                for (int ax = 0; ax < T::NAX; ++ax) {
+                    umax = fmaxf(umax, fmaxf(nm[ax], np[ax]));
+                    umin = fminf(umin, fminf(nm[ax], np[ax]));
+                    dmax = fmaxf(dmax, fabsf(dd[ax]));
+                }
+                const float lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
+#pragma unroll
+                for (int ax = 0; ax < T::NAX; ++ax) dd[ax] *= lim;
+            }
+            if (KIND == RK_LIM_VK) {
                 float umax = w0, umin = w0;
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) {
@@ -547,29 +569,20 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
                 }
                 float lim = 1.0f;
                 if (umax - umin > 0.0f) {
-                    if (KIND == RK_LIM_VK) {
-                        // Limiters.h:86-115, per face projection +-dd
-                        const float iun = 2.0f / (umax - umin);
+                    // Limiters.h:86-115, per face projection +-dd
+                    const float iun = 2.0f / (umax - umin);
 #pragma unroll
-                        for (int ax = 0; ax < T::NAX; ++ax) {
+                    for (int ax = 0; ax < T::NAX; ++ax) {
 #pragma unroll
-                            for (int sg = 0; sg < 2; ++sg) {
-                                const float d2 = sg ? -dd[ax] : dd[ax];
-                                if (d2 == 0.0f) continue;
-                                const float dm = ((d2 > 0.0f ? umax : umin) - w0) * iun;
-                                const float q = d2 * iun;
-                                const float r =
-                                    ((dm * dm + eps2) + 2.0f * q * dm) / (dm * dm + 2.0f * q * q + dm * q + eps2);
-                                lim = fminf(lim, r);
-                            }
+                        for (int sg = 0; sg < 2; ++sg) {
+                            const float d2 = sg ? -dd[ax] : dd[ax];
+                            if (d2 == 0.0f) continue;
+                            const float dm = ((d2 > 0.0f ? umax : umin) - w0) * iun;
+                            const float q = d2 * iun;
+                            const float r =
+                                ((dm * dm + eps2) + 2.0f * q * dm) / (dm * dm + 2.0f * q * q + dm * q + eps2);
+                            lim = fminf(lim, r);
                         }
-                    } else {
-                        // Barth-Jespersen (Limiters.h:74-83): the smallest admissible
-                        // ratio over the 2*nd face projections +-dd.
-                        float dmax = 0.0f;
-#pragma unroll
-                        for (int ax = 0; ax < T::NAX; ++ax) dmax = fmaxf(dmax, fabsf(dd[ax]));
-                        if (dmax > 0.0f) lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
                     }
                 }
 #pragma unroll
@@ -685,37 +698,65 @@ __device__ __forceinline__ float4 own_state(const float* sm, const Slots& s) {
                        sm[T::w(s.w0, 3, box)]);
 }
 
-// Residual and spectral radius of the owned cell of this thread in plane z.
+// Geometry of the thread's own cell along kernel axes 0 and 1 (fixed while
+// an item marches): sizes, the face area normal to the marching axis, the
+// inverse area, and the spectral-radius factors of the high boundary faces
+// (0 where the cell is not the last one along the axis).
+struct CellGeo {
+    float hx, hy, fsz, ixy, farx, fary;
+};
+
 template <class T>
+__device__ __forceinline__ CellGeo cell_geo(const ProbDesc& d, int i0, int j0) {
+    CellGeo c{1.0f, 1.0f, 1.0f, 1.0f, 0.0f, 0.0f};
+    int tx, ty;
+    if (!T::cell(threadIdx.x, tx, ty)) return c;
+    const int gi = i0 + tx, gj = j0 + ty;
+    if (gi >= d.kn[0] || gj >= d.kn[1]) return c;
+    const AxisGeo gx = d.kgeo[0][gi + d.kgoff[0]], gy = d.kgeo[1][gj + d.kgoff[1]];
+    c.hx = gx.h;
+    c.hy = gy.h;
+    c.fsz = gx.h * gy.h;
+    c.ixy = gx.ih * gy.ih;
+    if (gi == d.kn[0] - 1) c.farx = d.kgeo[0][d.kn[0] + d.kgoff[0]].ih * gy.ih;
+    if (T::HAS_Y && gj == d.kn[1] - 1) c.fary = gx.ih * d.kgeo[1][d.kn[1] + d.kgoff[1]].ih;
+    return c;
+}
+
+// Residual and spectral radius of the owned cell of this thread in plane z
+// (hz, ihz: size and inverse size of plane z).
+template <class T, int SOLVER>
 __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
-                                         int z, const Slots& s, float4 own, float& srmax) {
+                                         int z, const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
+                                         float& srmax) {
     int tx, ty;
     if (!T::cell(threadIdx.x, tx, ty)) return;
     const int gi = i0 + tx, gj = j0 + ty;
     if (gi >= d.kn[0] || gj >= d.kn[1]) return;
-    const AxisGeo gx = d.kgeo[0][gi + d.kgoff[0]], gy = d.kgeo[1][gj + d.kgoff[1]], gz = d.kgeo[2][z + d.kgoff[2]];
-    const float fsx = gy.h * gz.h, fsy = gx.h * gz.h, fsz = gx.h * gy.h;
-    const float iv = gx.ih * gy.ih * gz.ih;
+    const float fsx = cg.hy * hz, fsy = cg.hx * hz, fsz = cg.fsz;
+    const float iv = cg.ixy * ihz;
+    // face areas times the stored-flux factor
+    const float kx = flux_scale<SOLVER>() * fsx, ky = flux_scale<SOLVER>() * fsy, kz = flux_scale<SOLVER>() * fsz;
     float R[NV];
     const float lxl = sm[T::fx(5, ty, tx)], lxr = sm[T::fx(5, ty, tx + 1)];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * fsx;
+    for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * kx;
     float sr = fsx * (lxl + lxr);
-    if (gi == d.kn[0] - 1) srmax = fmaxf(srmax, fsx * lxr * d.kgeo[0][d.kn[0] + d.kgoff[0]].ih * gy.ih * gz.ih);
+    if (cg.farx != 0.0f) srmax = fmaxf(srmax, fsx * lxr * cg.farx * ihz);
     if (T::HAS_Y) {
 #pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * fsy;
+        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * ky;
         const float lyr = sm[T::fy(5, ty + 1, tx)];
         sr += fsy * (sm[T::fy(5, ty, tx)] + lyr);
-        if (gj == d.kn[1] - 1) srmax = fmaxf(srmax, fsy * lyr * gx.ih * d.kgeo[1][d.kn[1] + d.kgoff[1]].ih * gz.ih);
+        if (cg.fary != 0.0f) srmax = fmaxf(srmax, fsy * lyr * cg.fary * ihz);
     }
     if (T::MARCH) {
         const int dn = s.d0, up = s.d1;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * fsz;
+        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * kz;
         const float lzr = sm[T::fz(up, 5, ty, tx)];
         sr += fsz * (sm[T::fz(dn, 5, ty, tx)] + lzr);
-        if (z == d.kn[2] - 1) srmax = fmaxf(srmax, fsz * lzr * gx.ih * gy.ih * d.kgeo[2][d.kn[2] + d.kgoff[2]].ih);
+        if (z == d.kn[2] - 1) srmax = fmaxf(srmax, fsz * lzr * cg.ixy * d.kgeo[2][d.kn[2] + d.kgoff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
     // source terms after the face fluxes (kernel.h:941-989), on the working state
@@ -724,7 +765,7 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
         const float ro = own.x;
         const float iro = 1.0f / ro;
         const float vu = own.y * iro, vv = own.z * iro, vw = own.w * iro;
-        const float vol = gx.h * gy.h * gz.h;
+        const float vol = fsz * hz;
         if (mp.force) {
             R[1] += vol * mp.sigma[0];
             R[2] += vol * mp.sigma[1];
@@ -787,6 +828,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
     const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
     setup_box<T>(d, i0, j0, bp);
     if (!pwc) setup_ring<T>(d, i0, j0, rp);
+    const CellGeo cg = cell_geo<T>(d, i0, j0);
     if (!T::MARCH) {
         const Slots s = slots_of<T>(0);
         issue<T>(d, Uin, Rin, 0, bp, pf);
@@ -796,7 +838,8 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false, s);
         const float4 own = src ? own_state<T>(sm, s) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
-        residual<T>(d, sm, Rout, i0, j0, 0, s, own, srmax);
+        const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
+        residual<T, SOLVER>(d, sm, Rout, i0, j0, 0, s, own, cg, gz.h, gz.ih, srmax);
     } else if constexpr (!T::TWO_PHASE) {
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
@@ -819,7 +862,10 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true, sf);
             const float4 own = src && z >= z0 ? own_state<T>(sm, sf) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
             __syncthreads();
-            if (z >= z0) residual<T>(d, sm, Rout, i0, j0, z, sf, own, srmax);
+            if (z >= z0) {
+                const AxisGeo gz = d.kgeo[2][z + d.kgoff[2]];
+                residual<T, SOLVER>(d, sm, Rout, i0, j0, z, sf, own, cg, gz.h, gz.ih, srmax);
+            }
         }
     } else {
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
@@ -839,13 +885,20 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         float4 own = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
 #pragma unroll 1
         for (int P = z0 - 1; P <= z1 + 1; ++P) {
+            // geometry of the residual's plane first: its load overlaps the phase
+            float hz = 1.0f, ihz = 1.0f;
+            if (P - 2 >= z0) {
+                const AxisGeo gz = d.kgeo[2][P - 2 + d.kgoff[2]];
+                hz = gz.h;
+                ihz = gz.ih;
+            }
             // plane P+2 was prefetched during the previous pass
             if (P + 2 <= z1 + 1) {
                 store<T>(d, sm, Uout, P + 2, z0, z1, dtf, bp, pf, health);
                 if (P + 3 <= z1 + 1) issue<T>(d, Uin, Rin, P + 3, bp, pf);
             }
             if (!pwc && P <= z1) recon<T>(d, sm, P, kind, slots_of<T>(P), rp);
-            if (P - 2 >= z0) residual<T>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, srmax);
+            if (P - 2 >= z0) residual<T, SOLVER>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, cg, hz, ihz, srmax);
             if (P > z1) break;
             __syncthreads();
             if (P < z0) continue;
