@@ -609,34 +609,33 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int p, int k
 // tile (AX = 0), (fx, fy-1) and (fx, fy) (AX = 1), or (fx, fy) of planes z and
 // z+1 (AX = 2): face states, boundary image, Riemann flux and eigenvalue into
 // the face array.  s holds the slots of plane z.
-template <class T, int SOLVER, int AX>
-__device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
-                                     const Slots& s, bool pwc) {
+template <class T, int AX>
+__device__ __forceinline__ bool face_in(const ProbDesc& d, const float* sm, int fx, int fy, int gi, int gj, int z,
+                                        const Slots& s, bool pwc, float UL[NV], float UR[NV], int& out, int& vs) {
     constexpr int A = phys_axis<T, AX>();
     constexpr int SA = AX == 0 ? 0 : (AX == 1 ? 1 : T::AZ);
-    int bl, br, rl, rr, g, n, per, out, vs;
+    int bl, br, rl, rr, g, n, per;
     int wl = s.w0, wr = s.w0, dl = s.d0, dr = s.d0;
     if (AX == 0) {
-        if (gi > d.kn[0] || gj >= d.kn[1]) return;
+        if (gi > d.kn[0] || gj >= d.kn[1]) return false;
         bl = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
         rl = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
         g = gi; n = d.kn[0]; per = d.kper[0];
         out = T::fx(0, fy, fx); vs = T::TY * (T::TX + 1);
     } else if (AX == 1) {
-        if (gi >= d.kn[0] || gj > d.kn[1]) return;
+        if (gi >= d.kn[0] || gj > d.kn[1]) return false;
         bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
         rl = fy * T::RX + fx + 1; rr = rl + T::RX;
         g = gj; n = d.kn[1]; per = d.kper[1];
         out = T::fy(0, fy, fx); vs = (T::TY + 1) * T::TX;
     } else {
-        if (gi >= d.kn[0] || gj >= d.kn[1]) return;
+        if (gi >= d.kn[0] || gj >= d.kn[1]) return false;
         bl = br = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + HB;
         rl = rr = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx + 1;
         wr = s.wp; dr = s.d1;
         g = z + 1; n = d.kn[2]; per = d.kper[2];
         out = T::fz(s.d1, 0, fy, fx); vs = T::TY * T::TX;
     }
-    float UL[NV], UR[NV], F[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, SA, v, rl)]);
@@ -651,36 +650,68 @@ __device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int f
         for (int v = 0; v < NV; ++v) UR[v] = UL[v];
         bc32(d.mp, 2 * A + 1, A, UR);
     }
-    const float lam = flux32<SOLVER, A>(d.mp, UL, UR, F);
+    return true;
+}
+
+template <class T, int SOLVER, int AX>
+__device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
+                                     const Slots& s, bool pwc) {
+    float UL[NV], UR[NV], F[NV];
+    int out, vs;
+    if (!face_in<T, AX>(d, sm, fx, fy, gi, gj, z, s, pwc, UL, UR, out, vs)) return;
+    const float lam = flux32<SOLVER, phys_axis<T, AX>()>(d.mp, UL, UR, F);
 #pragma unroll
     for (int v = 0; v < NV; ++v) sm[out + v * vs] = F[v];
     sm[out + NV * vs] = lam;
 }
 
+// Faces on kernel axes 0 and 1 of one thread computed side by side (one
+// basic block, so the two Riemann solutions interleave).
+template <class T, int SOLVER>
+__device__ __forceinline__ void face_pair(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
+                                          const Slots& s, bool pwc) {
+    float UL0[NV], UR0[NV], UL1[NV], UR1[NV], F0[NV], F1[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) UL0[v] = UR0[v] = UL1[v] = UR1[v] = 1.0f;
+    int o0, v0, o1, v1;
+    const bool ok0 = face_in<T, 0>(d, sm, fx, fy, gi, gj, z, s, pwc, UL0, UR0, o0, v0);
+    const bool ok1 = face_in<T, 1>(d, sm, fx, fy, gi, gj, z, s, pwc, UL1, UR1, o1, v1);
+    const float l0 = flux32<SOLVER, phys_axis<T, 0>()>(d.mp, UL0, UR0, F0);
+    const float l1 = flux32<SOLVER, phys_axis<T, 1>()>(d.mp, UL1, UR1, F1);
+    if (ok0) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sm[o0 + v * v0] = F0[v];
+        sm[o0 + NV * v0] = l0;
+    }
+    if (ok1) {
+#pragma unroll
+        for (int v = 0; v < NV; ++v) sm[o1 + v * v1] = F1[v];
+        sm[o1 + NV * v1] = l1;
+    }
+}
+
 // The faces of plane z this thread computes: on kernel axis 0 the face left
-// of its cell, on axis 1 the face below it, on the marching axis the face
-// above it (between z and z+1).  The tile's far faces go to the first TY
-// threads (axis 0, face TX) and the next TX threads (axis 1, face TY) of a
-// two-axis tile, and to thread TX of a one-row tile.
+// of its cell, on axis 1 the face below it (the two side by side), on the
+// marching axis the face above it (between z and z+1).  The tile's far faces
+// go to different warps of a two-axis tile: axis 1 (face TY) to the first TX
+// threads, axis 0 (face TX) to the last TY threads; in a one-row tile thread
+// TX computes the far face.
 template <class T, int SOLVER>
 __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int j0, int z, bool pwc, bool do_xy,
                                        bool do_z, const Slots& s) {
     const int tid = threadIdx.x;
     const int tx = T::HAS_Y ? tid % T::TX : tid, ty = T::HAS_Y ? tid / T::TX : 0;
     if (do_xy) {
-        const int reps0 = (T::HAS_Y && tid < T::TY) ? 2 : 1;
-#pragma unroll 1
-        for (int r = 0; r < reps0; ++r) {
-            const int fx = r ? T::TX : tx, fy = r ? tid : ty;
-            if (T::HAS_Y || fx <= T::TX) face<T, SOLVER, 0>(d, sm, fx, fy, i0 + fx, j0 + fy, z, s, pwc);
-        }
-        if (T::HAS_Y) {
-            const int reps1 = (tid >= T::TY && tid < T::TY + T::TX) ? 2 : 1;
-#pragma unroll 1
-            for (int r = 0; r < reps1; ++r) {
-                const int fx = r ? tid - T::TY : tx, fy = r ? T::TY : ty;
-                face<T, SOLVER, 1>(d, sm, fx, fy, i0 + fx, j0 + fy, z, s, pwc);
+        if constexpr (T::HAS_Y) {
+            face_pair<T, SOLVER>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
+            // far faces: axis 1 on the first warp(s), axis 0 on the last threads
+            if (tid < T::TX) face<T, SOLVER, 1>(d, sm, tid, T::TY, i0 + tid, j0 + T::TY, z, s, pwc);
+            else if (tid >= T::NT - T::TY) {
+                const int fy = tid - (T::NT - T::TY);
+                face<T, SOLVER, 0>(d, sm, T::TX, fy, i0 + T::TX, j0 + fy, z, s, pwc);
             }
+        } else {
+            if (tx <= T::TX) face<T, SOLVER, 0>(d, sm, tx, 0, i0 + tx, j0, z, s, pwc);
         }
     }
     if (T::MARCH && do_z && (T::HAS_Y || tx < T::TX)) face<T, SOLVER, 2>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
