@@ -122,12 +122,15 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary, if any."""
+def profile_traffic(kernel, cells):
+    """DRAM bytes per launch of `kernel` over `cells` cells: the committed ncu
+    capture's bytes per cell (dram__bytes_read.sum + dram__bytes_write.sum over
+    the captured launch's cells) times the cell count, or None."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(kernel)
+            rec = json.load(f).get(kernel)
+        return float(rec["bytes_per_cell"]) * cells if rec else None
     except Exception:
         return None
 
@@ -330,7 +333,8 @@ def run_ours(args, rank, ws, lr, dist):
         alg_note = "80 B x cells per step, charged to the dominant kernel of the FP64 path"
     achieved = alg / (top_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(top), "kernel": top, "kernel_ms": top_ms,
+                "traffic": profile_traffic(top, cells) if precision == "mixed" else None, "kernel": top,
+                "kernel_ms": top_ms,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes": alg, "algorithmic_note": alg_note,
                 "step_kernels_ms": kernels}
