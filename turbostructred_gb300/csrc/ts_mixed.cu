@@ -273,11 +273,12 @@ struct Tile {
     static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TY * TX : 0);
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
     static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
-    // resident CTAs per SM the register allocation is sized for (about 24-32
-    // warps per SM for one-row tiles; two per SM for the shared-memory-heavy
-    // two-axis tiles)
+    // resident CTAs per SM the register allocation is sized for (about 24
+    // warps per SM for 1D tiles, 16 for marching one-row tiles, whose longer
+    // items hide latency with fewer warps and more registers; two CTAs per SM
+    // for the shared-memory-heavy two-axis tiles)
     static constexpr int WARPS = (NT + 31) / 32;
-    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : (24 + WARPS - 1) / WARPS);
+    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : ((MARCH ? 16 : 24) + WARPS - 1) / WARPS);
 
     static __device__ __forceinline__ int wslot(int p) { return TWO_PHASE ? (p & 3) : (p + 3) % 3; }
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
@@ -448,8 +449,9 @@ __device__ __forceinline__ Slots slots_of(int p) {
 // One reconstruction position of a thread for the current item: its ring
 // index, box index and geometry entries (fixed while the item marches).
 struct RingPos {
-    int box;      // box index of the cell; -1: nothing to do
-    int g0, g1;   // geometry indices along kernel axes 0 and 1
+    int box;        // box index of the cell; -1: nothing to do
+    int g0, g1;     // geometry indices along kernel axes 0 and 1
+    float ks0, ks1; // central-slope factors along kernel axes 0 and 1
 };
 
 // Ring position of round k of this thread.  Second rounds run from the last
@@ -481,6 +483,8 @@ __device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, int j0, Ri
         rp[k].box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
         rp[k].g0 = si + d.kgoff[0];
         rp[k].g1 = sj + d.kgoff[1];
+        rp[k].ks0 = d.kgeo[0][rp[k].g0].ks;
+        rp[k].ks1 = T::HAS_Y ? d.kgeo[1][rp[k].g1].ks : 0.0f;
     }
 }
 
@@ -514,8 +518,14 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
         const int t = ring_index<T>(k);
         const int box = rp[k].box;
         AxisGeo g[3];
-        g[0] = d.kgeo[0][rp[k].g0];
-        if (T::HAS_Y) g[1] = d.kgeo[1][rp[k].g1];
+        if (KIND == RK_LINEAR || KIND == RK_LIM_BJ) {
+            // central slopes need only ks, kept in registers for the item
+            g[0].ks = rp[k].ks0;
+            if (T::HAS_Y) g[1].ks = rp[k].ks1;
+        } else {
+            g[0] = d.kgeo[0][rp[k].g0];
+            if (T::HAS_Y) g[1] = d.kgeo[1][rp[k].g1];
+        }
         if (T::MARCH) g[T::AZ] = gz;
         float eps2 = 0.0f;
         if (KIND == RK_LIM_VK) {
