@@ -711,8 +711,9 @@ def run_batch2d(args, rank, ws, lr, dist):
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
-    p.add_argument("--steps", type=int, default=200)
-    p.add_argument("--warmup", type=int, default=5)
+    p.add_argument("--steps", type=int, default=None,
+                   help="timed steps (default 200; tubes: 3, a step being the whole batch solved to t_end)")
+    p.add_argument("--warmup", type=int, default=None, help="untimed warm-up steps (default 5; tubes: 3)")
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
     p.add_argument("--n", type=int, default=N_DEFAULT)
@@ -739,6 +740,10 @@ def main():
     p.add_argument("--order", choices=["fifo", "shortest"], default="shortest")
     p.add_argument("--max-cells", type=float, default=16e6)
     args = p.parse_args()
+    if args.steps is None:
+        args.steps = 3 if args.workload == "tubes" else 200
+    if args.warmup is None:
+        args.warmup = 3 if args.workload == "tubes" else 5
     if args.impl == "reference":
         rank = int(os.environ.get("RANK", "0"))
         run_reference(args, rank, int(os.environ.get("WORLD_SIZE", "1")))
