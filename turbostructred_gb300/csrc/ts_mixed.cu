@@ -451,7 +451,7 @@ __device__ __forceinline__ Slots slots_of(int p) {
 struct RingPos {
     int box;        // box index of the cell; -1: nothing to do
     int g0, g1;     // geometry indices along kernel axes 0 and 1
-    float ks0, ks1; // central-slope factors along kernel axes 0 and 1
+    float ks0, ks1; // central-slope factors along kernel axes 0 and 1 (marching tiles)
 };
 
 // Ring position of round k of this thread.  Second rounds run from the last
@@ -483,8 +483,10 @@ __device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, int j0, Ri
         rp[k].box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
         rp[k].g0 = si + d.kgoff[0];
         rp[k].g1 = sj + d.kgoff[1];
-        rp[k].ks0 = d.kgeo[0][rp[k].g0].ks;
-        rp[k].ks1 = T::HAS_Y ? d.kgeo[1][rp[k].g1].ks : 0.0f;
+        if (T::MARCH) {
+            rp[k].ks0 = d.kgeo[0][rp[k].g0].ks;
+            rp[k].ks1 = T::HAS_Y ? d.kgeo[1][rp[k].g1].ks : 0.0f;
+        }
     }
 }
 
@@ -518,8 +520,8 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
         const int t = ring_index<T>(k);
         const int box = rp[k].box;
         AxisGeo g[3];
-        if (KIND == RK_LINEAR || KIND == RK_LIM_BJ) {
-            // central slopes need only ks, kept in registers for the item
+        if (T::MARCH && (KIND == RK_LINEAR || KIND == RK_LIM_BJ)) {
+            // central slopes need only ks, kept in registers while the item marches
             g[0].ks = rp[k].ks0;
             if (T::HAS_Y) g[1].ks = rp[k].ks1;
         } else {
@@ -869,7 +871,6 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
     const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
     setup_box<T>(d, i0, j0, bp);
     if (!pwc) setup_ring<T>(d, i0, j0, rp);
-    const CellGeo cg = cell_geo<T>(d, i0, j0);
     if (!T::MARCH) {
         const Slots s = slots_of<T>(0);
         issue<T>(d, Uin, Rin, 0, bp, pf);
@@ -879,9 +880,12 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false, s);
         const float4 own = src ? own_state<T>(sm, s) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
+        // a single plane: the geometry is loaded where it is used
+        const CellGeo cg = cell_geo<T>(d, i0, j0);
         const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
         residual<T, SOLVER>(d, sm, Rout, i0, j0, 0, s, own, cg, gz.h, gz.ih, srmax);
     } else if constexpr (!T::TWO_PHASE) {
+        const CellGeo cg = cell_geo<T>(d, i0, j0);
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
         // build the slopes of planes z0-1, z0 and the marching face z0-1/2.
@@ -909,6 +913,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             }
         }
     } else {
+        const CellGeo cg = cell_geo<T>(d, i0, j0);
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded.  Pass P has two phases:
         //   A: store plane P+2, slopes of plane P, residual of plane P-2;
