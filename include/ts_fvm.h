@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define TS_FVM_ABI_VERSION 2
+#define TS_FVM_ABI_VERSION 3
 
 typedef enum ts_status {
     TS_OK = 0,
@@ -136,6 +136,15 @@ typedef struct ts_config {
     int32_t uniform_acceleration;  /* IsUnifromAccelerationRequared: R_mom += rho V g, R_E += V rho g.u */
     double sigma[3];               /* Sigma */
     double acceleration[3];        /* UniformAcceleration */
+    /* Viscous flow (ExplicitRungeKuttaFVM.h:81-874, :1161-1170): with
+       `viscous` set, velocity gradients (central in the interior, least
+       squares at non-periodic boundaries) give the stress-tensor face fluxes
+       subtracted from the convective ones.  `viscosity` (gas viscosity mu)
+       also enters the spectral radius of every step, viscous or not
+       (:1239-1248).  FP64 precision only (TS_ERR_UNSUPPORTED otherwise). */
+    int32_t viscous;               /* IsViscousFlow */
+    int32_t reserved3;
+    double viscosity;              /* Viscosity */
 } ts_config;
 
 /* StepInfo (kernel.h:31-39) plus a health word. */
@@ -176,7 +185,7 @@ ts_status ts_step(ts_handle* h, int32_t n_steps, ts_step_info* info);
    handle's stream around the whole run and around every kernel launch
    (launched one by one, not from a graph).  Per-kernel times are averages
    per launch; names identify the kernels of one step in launch order. */
-#define TS_MAX_KERNELS 12
+#define TS_MAX_KERNELS 16
 typedef struct ts_timing {
     double total_ms;
     int32_t n_kernels;        /* kernels per step */

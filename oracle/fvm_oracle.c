@@ -111,6 +111,10 @@ typedef struct {
     double* rgrad;
     double* rlim;
     double* eps2;              /* Venkatakrishnan eps^2 per cell (Limiters.h:93-96) */
+    const double* U;           /* the step's values (cell values for the viscous fluxes) */
+    /* velocity gradients per cell (gradientVelocityX/Y/Z, ExplicitRungeKuttaFVM.h:
+       81-134): vgrad[(cell * 3 + d) * 3 + e] = d(velocity d)/d(axis e) */
+    double* vgrad;
 } orc_ctx;
 
 static inline int cidx(const orc_ctx* w, int i, int j, int k) {
@@ -727,6 +731,215 @@ static double riemann(const orc_config* c, const double* UL, const double* UR, i
     return roe_flux(c, UL, UR, fn, flux);
 }
 
+
+/* ------------------------------------------------------------------------ */
+/* Viscous part, ExplicitRungeKuttaFVM.h:81-874                             */
+/* ------------------------------------------------------------------------ */
+
+/* Velocity component d of a cell's conserved values (VariablesTransition.h:18-36). */
+static inline double vel(const double* V, int d) { return V[1 + d] / V[0]; }
+
+static inline double* vgrad_of(orc_ctx* w, int cell, int d) { return w->vgrad + ((size_t)cell * 3 + d) * 3; }
+
+static inline double det3(double a00, double a01, double a02, double a10, double a11, double a12, double a20,
+                          double a21, double a22) {
+    return a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+}
+
+/* Least-squares gradient (GradientComputer::ExecuteByLeastSquares,
+   GradientComputer.h:20-52): the g minimising |A g - rhs| with rows
+   A_r = point - points_r (first nd components) and rhs_r = value - values_r.
+   The reference solves it with Eigen 3.2.5's JacobiSVD; this restatement
+   solves the normal equations (A^T A) g = A^T rhs by Cramer's rule (1x1 to
+   3x3, well conditioned for these stencils), so it agrees with the reference
+   to rounding, not bit for bit. */
+static void ls_gradient(int nd, int m, const double (*A)[3], const double* rhs, double* g) {
+    double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, b[3] = {0, 0, 0};
+    for (int r = 0; r < m; ++r)
+        for (int a = 0; a < nd; ++a) {
+            b[a] += A[r][a] * rhs[r];
+            for (int e = 0; e < nd; ++e) M[a][e] += A[r][a] * A[r][e];
+        }
+    g[0] = g[1] = g[2] = 0.0;
+    if (nd == 1) {
+        g[0] = b[0] / M[0][0];
+    } else if (nd == 2) {
+        const double det = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+        g[0] = (b[0] * M[1][1] - M[0][1] * b[1]) / det;
+        g[1] = (M[0][0] * b[1] - b[0] * M[1][0]) / det;
+    } else {
+        const double det = det3(M[0][0], M[0][1], M[0][2], M[1][0], M[1][1], M[1][2], M[2][0], M[2][1], M[2][2]);
+        g[0] = det3(b[0], M[0][1], M[0][2], b[1], M[1][1], M[1][2], b[2], M[2][1], M[2][2]) / det;
+        g[1] = det3(M[0][0], b[0], M[0][2], M[1][0], b[1], M[1][2], M[2][0], b[2], M[2][2]) / det;
+        g[2] = det3(M[0][0], M[0][1], b[0], M[1][0], M[1][1], b[1], M[2][0], M[2][1], b[2]) / det;
+    }
+}
+
+/* Ghost-cell gradients beyond one boundary cell (ComputeDummyCellGradients,
+   ExplicitRungeKuttaFVM.h:318-680): the least-squares gradient at the face
+   centre from the face value (BCGeneral::getFaceValues, BCGeneral.h:90-94:
+   the mean of the cell and its BC image) and the stencil of
+   Stencil::InternalBorderStencil (Stencil.h:28-63) plus the ghost cell,
+   extrapolated as 2 g_face - g_cell. */
+static void dummy_gradient(orc_ctx* w, const double* U, int a, int side, int i, int j, int k) {
+    const orc_config* c = w->c;
+    const int nd = c->ndims;
+    const double* X[3] = {w->x, w->y, w->z};
+    const double* H[3] = {w->hx, w->hy, w->hz};
+    int ix[3] = {i, j, k};
+    const int inner = cidx(w, i, j, k);
+    int gi[3] = {i, j, k};
+    gi[a] += side ? 1 : -1;
+    const int ghost = cidx(w, gi[0], gi[1], gi[2]);
+    double fc[3] = {w->x[i], w->y[j], w->z[k]};
+    fc[a] = side ? X[a][ix[a]] + 0.5 * H[a][ix[a]] : X[a][ix[a]] - 0.5 * H[a][ix[a]];
+    const double* Vin = U + (size_t)inner * NV;
+    vec3 n = {a == 0 ? (side ? 1.0 : -1.0) : 0.0, a == 1 ? (side ? 1.0 : -1.0) : 0.0,
+              a == 2 ? (side ? 1.0 : -1.0) : 0.0};
+    double du[NV], Vf[NV];
+    bc_dummy_values(c, 2 * a + side, Vin, n, du);
+    for (int v = 0; v < NV; ++v) Vf[v] = 0.5 * (Vin[v] + du[v]);
+    /* stencil: the cell, its neighbours along the other active axes, the ghost */
+    int st[7][3], m = 0;
+    st[m][0] = i; st[m][1] = j; st[m][2] = k; ++m;
+    for (int b = 0; b < nd; ++b) {
+        if (b == a) continue;
+        for (int sg = 1; sg >= -1; sg -= 2) {
+            st[m][0] = i; st[m][1] = j; st[m][2] = k;
+            st[m][b] += sg;
+            ++m;
+        }
+    }
+    st[m][0] = gi[0]; st[m][1] = gi[1]; st[m][2] = gi[2]; ++m;
+    double A[7][3], rhs[7], g[3];
+    for (int r = 0; r < m; ++r) {
+        A[r][0] = fc[0] - w->x[st[r][0]];
+        A[r][1] = fc[1] - w->y[st[r][1]];
+        A[r][2] = fc[2] - w->z[st[r][2]];
+    }
+    for (int d = 0; d < 3; ++d) {
+        const double value = Vf[1 + d] / Vf[0];
+        for (int r = 0; r < m; ++r) rhs[r] = value - vel(U + (size_t)cidx(w, st[r][0], st[r][1], st[r][2]) * NV, d);
+        ls_gradient(nd, m, (const double (*)[3])A, rhs, g);
+        double* gg = vgrad_of(w, ghost, d);
+        const double* gc = vgrad_of(w, inner, d);
+        for (int e = 0; e < 3; ++e) gg[e] = 2.0 * g[e] - gc[e];
+    }
+}
+
+/* ComputeVelocityGradients (ExplicitRungeKuttaFVM.h:81-134): central
+   differences inside (Kernel::ComputeGradientNonUniformStructured,
+   kernel.h:918-938), the periodic exchange of ExchangeGradients (:136-316) on
+   one rank, then the ghost gradients of non-periodic sides. */
+static void velocity_gradients(orc_ctx* w, const double* U) {
+    const orc_config* c = w->c;
+    const int nd = c->ndims;
+    for (int k = w->kmin; k <= w->kmax; ++k)
+        for (int j = w->jmin; j <= w->jmax; ++j)
+            for (int i = w->imin; i <= w->imax; ++i) {
+                const int id = cidx(w, i, j, k);
+                for (int d = 0; d < 3; ++d) {
+                    double* g = vgrad_of(w, id, d);
+                    const double dux = vel(U + (size_t)cidx(w, i + 1, j, k) * NV, d) -
+                                       vel(U + (size_t)cidx(w, i - 1, j, k) * NV, d);
+                    g[0] = dux / (w->x[i + 1] - w->x[i - 1]);
+                    g[1] = 0.0;
+                    g[2] = 0.0;
+                    if (nd > 1) {
+                        const double duy = vel(U + (size_t)cidx(w, i, j + 1, k) * NV, d) -
+                                           vel(U + (size_t)cidx(w, i, j - 1, k) * NV, d);
+                        g[1] = duy / (w->y[j + 1] - w->y[j - 1]);
+                    }
+                    if (nd > 2) {
+                        const double duz = vel(U + (size_t)cidx(w, i, j, k + 1) * NV, d) -
+                                           vel(U + (size_t)cidx(w, i, j, k - 1) * NV, d);
+                        g[2] = duz / (w->z[k + 1] - w->z[k - 1]);
+                    }
+                }
+            }
+    const int lo[3] = {w->imin, w->jmin, w->kmin}, hi[3] = {w->imax, w->jmax, w->kmax};
+    for (int a = 0; a < nd; ++a) {
+        /* transverse cells of the two boundary layers along a (interior range) */
+        const int b1 = a == 0 ? 1 : 0, b2 = a == 2 ? 1 : 2;
+        for (int p = lo[b1]; p <= hi[b1]; ++p)
+            for (int q = lo[b2]; q <= hi[b2]; ++q) {
+                int cl[3], ch[3];
+                cl[a] = lo[a]; ch[a] = hi[a];
+                cl[b1] = ch[b1] = p;
+                cl[b2] = ch[b2] = q;
+                if (c->periodic[a]) {
+                    int gl[3] = {cl[0], cl[1], cl[2]}, gh[3] = {ch[0], ch[1], ch[2]};
+                    gl[a] -= 1;
+                    gh[a] += 1;
+                    const int il = cidx(w, cl[0], cl[1], cl[2]), ih = cidx(w, ch[0], ch[1], ch[2]);
+                    const int jl = cidx(w, gl[0], gl[1], gl[2]), jh = cidx(w, gh[0], gh[1], gh[2]);
+                    memcpy(vgrad_of(w, jh, 0), vgrad_of(w, il, 0), sizeof(double) * 9);
+                    memcpy(vgrad_of(w, jl, 0), vgrad_of(w, ih, 0), sizeof(double) * 9);
+                }
+            }
+    }
+    for (int a = 0; a < nd; ++a) {
+        if (c->periodic[a]) continue;
+        const int b1 = a == 0 ? 1 : 0, b2 = a == 2 ? 1 : 2;
+        for (int p = lo[b1]; p <= hi[b1]; ++p)
+            for (int q = lo[b2]; q <= hi[b2]; ++q) {
+                int cl[3], ch[3];
+                cl[a] = lo[a]; ch[a] = hi[a];
+                cl[b1] = ch[b1] = p;
+                cl[b2] = ch[b2] = q;
+                dummy_gradient(w, U, a, 0, cl[0], cl[1], cl[2]);
+                dummy_gradient(w, U, a, 1, ch[0], ch[1], ch[2]);
+            }
+    }
+}
+
+/* Viscous flux of the face between cells cm and cp along axis a, s the index
+   of cp along a (ComputeViscousFluxes, ExplicitRungeKuttaFVM.h:683-874): face
+   velocity gradients from the two cells' gradients weighted by the cell
+   sizes, the normal derivatives by the two-point difference, the stress
+   tensor with second viscosity -2/3 mu, and the work of the stresses. */
+static void viscous_flux(orc_ctx* w, int a, int cm, int cp, int s, double* fv) {
+    const orc_config* c = w->c;
+    const double* X = a == 0 ? w->x : (a == 1 ? w->y : w->z);
+    const double* H = a == 0 ? w->hx : (a == 1 ? w->hy : w->hz);
+    const double* UL = w->U + (size_t)cm * NV;
+    const double* UR = w->U + (size_t)cp * NV;
+    const double dx = X[s] - X[s - 1];
+    const double l = H[s - 1] / dx;
+    const double r = H[s] / dx;
+    double D[3][3], uu[3];
+    for (int d = 0; d < 3; ++d) {
+        const double* gL = vgrad_of(w, cm, d);
+        const double* gR = vgrad_of(w, cp, d);
+        for (int e = 0; e < 3; ++e) D[d][e] = 0.5 * (r * gL[e] + l * gR[e]);
+        D[d][a] = (vel(UR, d) - vel(UL, d)) / dx;
+    }
+    for (int d = 0; d < 3; ++d) uu[d] = 0.5 * (l * vel(UR, d) + r * vel(UL, d));
+    const double mu = c->viscosity;
+    const double sv = (-2.0 / 3.0) * mu;
+    const double td = sv * (D[0][0] + D[1][1] + D[2][2]);
+    fv[0] = 0.0;
+    if (a == 0) {
+        const double txx = td + 2 * mu * D[0][0];
+        const double txy = mu * (D[0][1] + D[1][0]);
+        const double txz = mu * (D[0][2] + D[2][0]);
+        fv[1] = txx; fv[2] = txy; fv[3] = txz;
+        fv[4] = uu[0] * txx + uu[1] * txy + uu[2] * txz;
+    } else if (a == 1) {
+        const double tyy = td + 2 * mu * D[1][1];
+        const double txy = mu * (D[0][1] + D[1][0]);
+        const double tyz = mu * (D[1][2] + D[2][1]);
+        fv[1] = txy; fv[2] = tyy; fv[3] = tyz;
+        fv[4] = uu[0] * txy + uu[1] * tyy + uu[2] * tyz;
+    } else {
+        const double tzz = td + 2 * mu * D[2][2];
+        const double txz = mu * (D[0][2] + D[2][0]);
+        const double tyz = mu * (D[1][2] + D[2][1]);
+        fv[1] = txz; fv[2] = tyz; fv[3] = tzz;
+        fv[4] = uu[0] * txz + uu[1] * tyz + uu[2] * tzz;
+    }
+}
+
 /* ------------------------------------------------------------------------ */
 /* Residual, ExplicitRungeKuttaFVM.h:1150-1424                              */
 /* ------------------------------------------------------------------------ */
@@ -773,16 +986,19 @@ static void residual_line(orc_ctx* w, int a, int p, int q) {
             sample(w, cp, a, hr, UR);
         }
         double lam = riemann(c, UL, UR, a, fr);
-        for (int v = 0; v < NV; ++v) fr[v] -= 0.0; /* fvisc = 0 (inviscid) */
+        double fvisc[NV] = {0, 0, 0, 0, 0};
+        if (c->viscous) viscous_flux(w, a, cm, cp, s, fvisc);
+        for (int v = 0; v < NV; ++v) fr[v] -= fvisc[v];
         w->spectral[cp] += fS * lam;
         if (s > lo) {
             for (int v = 0; v < NV; ++v) w->resid[(size_t)cm * NV + v] -= (fr[v] - fl[v]) * fS;
             w->spectral[cm] += fS * lam;
-            /* viscous spectral-radius term with zero viscosity (:1239-1248) */
+            /* viscous spectral-radius term, added whatever IsViscousFlow is
+               (:1239-1248); Prandtl number 1 */
             double roFace = sqrt(UL[0] * UR[0]);
             double t1 = 4.0 / (3.0 * roFace), t2 = c->gamma / roFace;
             double vsr = (t1 < t2) ? t2 : t1;
-            vsr *= 0.0 / 1.0;
+            vsr *= c->viscosity / 1.0;
             vsr *= fS * fS;
             vsr /= w->vol[cm];
             w->spectral[cm] += vsr;
@@ -870,6 +1086,8 @@ static void iteration_step(orc_ctx* w, double* U, orc_step_info* info) {
                 for (int i = w->imin; i <= w->imax; ++i) reconstruct_cell(w, U, i, j, k);
     }
     exchange_recon(w);
+    w->U = U;
+    if (c->viscous) velocity_gradients(w, U);
     compute_residual(w);
     add_sources(w, U);
 
@@ -924,7 +1142,8 @@ int orc_advance(const orc_config* c, double* values, int n_steps, orc_step_info*
     w.rvals = calloc((size_t)w.ncells * NV, sizeof(double));
     w.rgrad = calloc((size_t)w.ncells * 3 * NV, sizeof(double));
     w.rlim = calloc((size_t)w.ncells * NV, sizeof(double));
-    if (!w.vol || !w.spectral || !w.resid || !w.rvals || !w.rgrad || !w.rlim) return 1;
+    if (c->viscous) w.vgrad = calloc((size_t)w.ncells * 9, sizeof(double));
+    if (!w.vol || !w.spectral || !w.resid || !w.rvals || !w.rgrad || !w.rlim || (c->viscous && !w.vgrad)) return 1;
     for (int k = 0; k < w.nza; ++k)
         for (int j = 0; j < w.nya; ++j)
             for (int i = 0; i < w.nxa; ++i) w.vol[cidx(&w, i, j, k)] = w.hx[i] * w.hy[j] * w.hz[k];
@@ -954,6 +1173,7 @@ int orc_advance(const orc_config* c, double* values, int n_steps, orc_step_info*
     }
     free(w.x); free(w.hx); free(w.y); free(w.hy); free(w.z); free(w.hz);
     free(w.vol); free(w.spectral); free(w.resid); free(w.rvals); free(w.rgrad); free(w.rlim); free(w.eps2);
+    free(w.vgrad);
     return 0;
 }
 

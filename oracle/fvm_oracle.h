@@ -58,6 +58,11 @@ typedef struct {
        with UniformAcceleration (KernelConfiguration.h:50-51,87-88). */
     int external_force, uniform_acceleration;
     double sigma[3], acceleration[3];
+    /* Viscous flow: IsViscousFlow and Viscosity (KernelConfiguration.h:43,49).
+       The viscosity enters the spectral radius even when viscous == 0
+       (ExplicitRungeKuttaFVM.h:1239-1248). */
+    int viscous;
+    double viscosity;
 } orc_config;
 
 typedef struct {

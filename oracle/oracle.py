@@ -57,6 +57,7 @@ class OrcConfig(C.Structure):
         ("threads", C.c_int),
         ("external_force", C.c_int), ("uniform_acceleration", C.c_int),
         ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
+        ("viscous", C.c_int), ("viscosity", C.c_double),
     ]
 
 
@@ -106,7 +107,7 @@ def make_case(**kw) -> dict:
                 gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
                 save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
-                external_force=None, uniform_acceleration=None)
+                external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0)
     case.update(kw)
     return case
 
@@ -137,6 +138,8 @@ def to_struct(case: dict, threads: int = 0) -> OrcConfig:
         setattr(c, flag, int(v is not None))
         for a in range(3):
             getattr(c, vec)[a] = v[a] if v is not None else 0.0
+    c.viscous = int(bool(case.get("viscous", False)))
+    c.viscosity = float(case.get("viscosity", 0.0))
     return c
 
 
@@ -223,6 +226,10 @@ def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, ste
         lines.append("external_force " + " ".join(repr(float(v)) for v in case["external_force"]))
     if case.get("uniform_acceleration") is not None:
         lines.append("uniform_acceleration " + " ".join(repr(float(v)) for v in case["uniform_acceleration"]))
+    if case.get("viscous"):
+        lines.append("viscous 1")
+    if case.get("viscosity", 0.0):
+        lines.append("viscosity " + repr(float(case["viscosity"])))
     lines += [f"ic_file {ic_path}", f"out_file {out_path}"]
     if toro:
         lines.append(f"toro {toro}")

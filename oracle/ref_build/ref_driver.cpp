@@ -26,6 +26,7 @@
 //   molar_mass x, gas_constant x   (KernelConfiguration MolarMass, UniversalGasConstant)
 //   external_force sx sy sz        (IsExternalForceRequared with Sigma)
 //   uniform_acceleration gx gy gz  (IsUnifromAccelerationRequared with UniformAcceleration)
+//   viscous 0|1, viscosity mu      (IsViscousFlow, Viscosity)
 #include "Methods/ExplicitRungeKuttaFVM.h"
 #include "Tests/1DTests/ToroTests.h"
 
@@ -132,6 +133,8 @@ DriverConfig parse(const char* path) {
             c.IsUnifromAccelerationRequared = true;
             c.UniformAcceleration = Vector(D(1), D(2), D(3));
         }
+        else if (k == "viscous") c.IsViscousFlow = I(1) != 0;
+        else if (k == "viscosity") c.Viscosity = D(1);
         else if (k == "molar_mass") c.MolarMass = D(1);
         else if (k == "gas_constant") c.UniversalGasConstant = D(1);
         else { std::fprintf(stderr, "unknown key %s\n", k.c_str()); std::exit(2); }

@@ -182,6 +182,13 @@ struct ts_handle {
             pb.eps2 = d;
         }
         if ((s = alloc(&pb.partial, (size_t)plain_partial_blocks(L))) != TS_OK) return s;
+        if (cfg.viscous) {
+            if ((s = alloc(&pb.VG, (size_t)9 * L.plane)) != TS_OK) return s;
+            TS_CUDA(cudaMemset(pb.VG, 0, (size_t)9 * L.plane * sizeof(double)));
+        }
+        if (cfg.viscosity != 0.0)
+            for (int a = 0; a < nd; ++a)
+                if ((s = alloc(&pb.VSR[a], L.plane)) != TS_OK) return s;
         pb.ctl = ctl_d;
         return TS_OK;
     }
@@ -413,6 +420,8 @@ ts_status ts_step_timed(ts_handle* h, int32_t n_steps, ts_step_info* info, ts_ti
         std::vector<cudaEvent_t>& ev;
         ~Cleanup() { for (auto& e : ev) if (e) cudaEventDestroy(e); }
     } cleanup{ev};
+    static_assert(kPlainMaxLaunches <= TS_MAX_KERNELS && kMixedMaxLaunches <= TS_MAX_KERNELS,
+                  "every launch of a step has a kernel slot");
     const char* names[TS_MAX_KERNELS] = {};
     int nl = 0;
     TS_CUDA(cudaEventRecord(ev[0], h->stream));

@@ -117,6 +117,11 @@ ts_status validate_config(const ts_config& c, std::string& err) {
         if (c.bc[s].type < TS_BC_WALL || c.bc[s].type > TS_BC_NATURAL) { err = "unknown boundary condition"; return TS_ERR_INVALID; }
     }
     if (c.precision != TS_PRECISION_FP64 && c.precision != TS_PRECISION_MIXED) { err = "unknown precision"; return TS_ERR_INVALID; }
+    if (!(c.viscosity >= 0.0) || !std::isfinite(c.viscosity)) { err = "viscosity must be finite and >= 0"; return TS_ERR_INVALID; }
+    if ((c.viscous || c.viscosity != 0.0) && c.precision != TS_PRECISION_FP64) {
+        // the viscosity enters the spectral radius even without viscous fluxes
+        err = "viscous flow (or a nonzero viscosity) runs on the FP64 path"; return TS_ERR_UNSUPPORTED;
+    }
     return TS_OK;
 }
 
@@ -168,6 +173,8 @@ Phys make_phys(const ts_config& c) {
         for (int a = 0; a < 3; ++a) p.bc.vel[s][a] = c.bc[s].velocity[a];
         p.bc.pstatic[s] = c.bc[s].pstatic;
     }
+    p.viscous = c.viscous != 0;
+    p.visc = c.viscosity;
     p.force = c.external_force != 0;
     p.accel = c.uniform_acceleration != 0;
     for (int a = 0; a < 3; ++a) {

@@ -62,6 +62,8 @@ struct Phys {
     BcSet bc;
     int force, accel;          // source terms on (kernel.h:941-989)
     double sigma[3], g[3];     // Sigma, UniformAcceleration
+    int viscous;               // IsViscousFlow: viscous face fluxes
+    double visc;               // Viscosity: also in the spectral radius
 };
 
 // Per-handle step control word in device memory (StepInfo, kernel.h:31-39).

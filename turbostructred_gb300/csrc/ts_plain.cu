@@ -462,6 +462,201 @@ __global__ void k_ghost(PlainBufs b, Phys ph) {
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Viscous part (ExplicitRungeKuttaFVM.h:81-874), FP64 like the rest of the path
+// ---------------------------------------------------------------------------
+
+// Velocity component d of cell c (VariablesTransition.h:18-36).
+__device__ __forceinline__ double velc(const PlainBufs& b, long long c, int d) {
+    return b.U[vidx(b.L, 1 + d) + c] / b.U[vidx(b.L, 0) + c];
+}
+
+__device__ __forceinline__ double vgrad(const PlainBufs& b, long long c, int d, int e) {
+    return b.VG[vidx(b.L, 3 * d + e) + c];
+}
+
+// Central-difference gradients of the three velocity components in every
+// interior cell (Kernel::ComputeGradientNonUniformStructured, kernel.h:918-938).
+__global__ void k_vgrad(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int j = blockIdx.y, k = blockIdx.z;
+    if (i >= L.nx) return;
+    const long long c = L.at(i, j, k);
+    const int nd = ph.nd;
+    for (int d = 0; d < 3; ++d) {
+        const double dux = velc(b, c + L.stride(0), d) - velc(b, c - L.stride(0), d);
+        const double gx = dux / (b.cx[0][i + 1 + L.gx] - b.cx[0][i - 1 + L.gx]);
+        double gy = 0.0, gz = 0.0;
+        if (nd > 1) {
+            const double duy = velc(b, c + L.stride(1), d) - velc(b, c - L.stride(1), d);
+            gy = duy / (b.cx[1][j + 1 + L.gy] - b.cx[1][j - 1 + L.gy]);
+        }
+        if (nd > 2) {
+            const double duz = velc(b, c + L.stride(2), d) - velc(b, c - L.stride(2), d);
+            gz = duz / (b.cx[2][k + 1 + L.gz] - b.cx[2][k - 1 + L.gz]);
+        }
+        b.VG[vidx(L, 3 * d) + c] = gx;
+        b.VG[vidx(L, 3 * d + 1) + c] = gy;
+        b.VG[vidx(L, 3 * d + 2) + c] = gz;
+    }
+}
+
+__device__ __forceinline__ double det3(double a00, double a01, double a02, double a10, double a11, double a12,
+                                       double a20, double a21, double a22) {
+    return a00 * (a11 * a22 - a12 * a21) - a01 * (a10 * a22 - a12 * a20) + a02 * (a10 * a21 - a11 * a20);
+}
+
+// Least-squares gradient of GradientComputer::ExecuteByLeastSquares
+// (GradientComputer.h:20-52) by the normal equations (A^T A) g = A^T rhs and
+// Cramer's rule; the reference uses Eigen's JacobiSVD, which agrees to
+// rounding.
+__device__ void ls_gradient(int nd, int m, const double (*A)[3], const double* rhs, double* g) {
+    double M[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}}, bb[3] = {0, 0, 0};
+    for (int r = 0; r < m; ++r)
+        for (int a = 0; a < nd; ++a) {
+            bb[a] += A[r][a] * rhs[r];
+            for (int e = 0; e < nd; ++e) M[a][e] += A[r][a] * A[r][e];
+        }
+    g[0] = g[1] = g[2] = 0.0;
+    if (nd == 1) {
+        g[0] = bb[0] / M[0][0];
+    } else if (nd == 2) {
+        const double det = M[0][0] * M[1][1] - M[0][1] * M[1][0];
+        g[0] = (bb[0] * M[1][1] - M[0][1] * bb[1]) / det;
+        g[1] = (M[0][0] * bb[1] - bb[0] * M[1][0]) / det;
+    } else {
+        const double det = det3(M[0][0], M[0][1], M[0][2], M[1][0], M[1][1], M[1][2], M[2][0], M[2][1], M[2][2]);
+        g[0] = det3(bb[0], M[0][1], M[0][2], bb[1], M[1][1], M[1][2], bb[2], M[2][1], M[2][2]) / det;
+        g[1] = det3(M[0][0], bb[0], M[0][2], M[1][0], bb[1], M[1][2], M[2][0], bb[2], M[2][2]) / det;
+        g[2] = det3(M[0][0], M[0][1], bb[0], M[1][0], M[1][1], bb[1], M[2][0], M[2][1], bb[2]) / det;
+    }
+}
+
+// Ghost gradients beyond boundary cell (i, j, k) on side `side` of axis A
+// (ComputeDummyCellGradients, ExplicitRungeKuttaFVM.h:318-680): least-squares
+// gradient at the face centre from the face value (mean of the cell and its
+// BC image, BCGeneral::getFaceValues) and the stencil of
+// Stencil::InternalBorderStencil plus the ghost cell; ghost = 2 g_face - g_cell.
+template <int A>
+__device__ void dummy_gradient(const PlainBufs& b, const Phys& ph, int side, int i, int j, int k) {
+    const Layout& L = b.L;
+    const int nd = ph.nd;
+    const int ix[3] = {i, j, k};
+    const int go[3] = {L.gx, L.gy, L.gz};
+    const long long inner = L.at(i, j, k);
+    const long long ghost = inner + (side ? L.stride(A) : -L.stride(A));
+    double fc[3] = {b.cx[0][i + L.gx], b.cx[1][j + L.gy], b.cx[2][k + L.gz]};
+    const double xa = b.cx[A][ix[A] + go[A]], ha = b.ch[A][ix[A] + go[A]];
+    fc[A] = side ? xa + 0.5 * ha : xa - 0.5 * ha;
+    double Vin[NV], du[NV], Vf[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Vin[v] = b.U[vidx(L, v) + inner];
+    bc_values(ph, 2 * A + side, A, side ? 1.0 : -1.0, Vin, du);
+#pragma unroll
+    for (int v = 0; v < NV; ++v) Vf[v] = 0.5 * (Vin[v] + du[v]);
+    // stencil: the cell, its neighbours along the other active axes (+ then -), the ghost
+    int st[7][3];
+    int m = 0;
+    st[m][0] = i; st[m][1] = j; st[m][2] = k; ++m;
+    for (int a = 0; a < nd; ++a) {
+        if (a == A) continue;
+        for (int sg = 1; sg >= -1; sg -= 2) {
+            st[m][0] = i; st[m][1] = j; st[m][2] = k;
+            st[m][a] += sg;
+            ++m;
+        }
+    }
+    st[m][0] = i; st[m][1] = j; st[m][2] = k;
+    st[m][A] += side ? 1 : -1;
+    ++m;
+    double Am[7][3], rhs[7], g[3];
+    for (int r = 0; r < m; ++r) {
+        Am[r][0] = fc[0] - b.cx[0][st[r][0] + L.gx];
+        Am[r][1] = fc[1] - b.cx[1][st[r][1] + L.gy];
+        Am[r][2] = fc[2] - b.cx[2][st[r][2] + L.gz];
+    }
+    for (int d = 0; d < 3; ++d) {
+        const double value = Vf[1 + d] / Vf[0];
+        for (int r = 0; r < m; ++r) rhs[r] = value - velc(b, L.at(st[r][0], st[r][1], st[r][2]), d);
+        ls_gradient(nd, m, Am, rhs, g);
+        for (int e = 0; e < 3; ++e) b.VG[vidx(L, 3 * d + e) + ghost] = 2.0 * g[e] - vgrad(b, inner, d, e);
+    }
+}
+
+// Gradients of the first ghost layer along axis A: the opposite interior
+// cell's on a periodic axis (ExchangeGradients on one rank,
+// ExplicitRungeKuttaFVM.h:136-316), least squares otherwise.
+template <int A>
+__global__ void k_vgrad_bc(PlainBufs b, Phys ph) {
+    if (b.ctl->stop_req) return;
+    const Layout& L = b.L;
+    const int n1 = (A == 0) ? L.ny : L.nx;
+    const int n2 = (A == 2) ? L.ny : L.nz;
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= n1 * n2) return;
+    const int p = t % n1, q = t / n1;
+    int i, j, k;
+    line_cell<A>(p, q, 0, i, j, k);
+    const long long c0 = L.at(i, j, k);
+    const long long st = L.stride(A);
+    const int n = L.n(A);
+    if (ph.periodic[A]) {
+        for (int pl = 0; pl < 9; ++pl) {
+            double* g = b.VG + vidx(L, pl) + c0;
+            g[(long long)n * st] = g[0];
+            g[-st] = g[(long long)(n - 1) * st];
+        }
+        return;
+    }
+    int ih = i, jh = j, kh = k;
+    if (A == 0) ih = n - 1; else if (A == 1) jh = n - 1; else kh = n - 1;
+    dummy_gradient<A>(b, ph, 0, i, j, k);
+    dummy_gradient<A>(b, ph, 1, ih, jh, kh);
+}
+
+// Viscous flux of the face along axis A between cells cl and cr, s the
+// index of cr along A (ComputeViscousFluxes, ExplicitRungeKuttaFVM.h:683-874).
+template <int A>
+__device__ void visc_flux(const PlainBufs& b, const Phys& ph, long long cl, long long cr, int s, double fv[NV]) {
+    const Layout& L = b.L;
+    const int g0 = (A == 0) ? L.gx : (A == 1 ? L.gy : L.gz);
+    const double dx = b.cx[A][s + g0] - b.cx[A][s - 1 + g0];
+    const double l = b.ch[A][s - 1 + g0] / dx;
+    const double r = b.ch[A][s + g0] / dx;
+    double D[3][3], uu[3];
+    for (int d = 0; d < 3; ++d) {
+        for (int e = 0; e < 3; ++e) D[d][e] = 0.5 * (r * vgrad(b, cl, d, e) + l * vgrad(b, cr, d, e));
+        D[d][A] = (velc(b, cr, d) - velc(b, cl, d)) / dx;
+    }
+    for (int d = 0; d < 3; ++d) uu[d] = 0.5 * (l * velc(b, cr, d) + r * velc(b, cl, d));
+    const double mu = ph.visc;
+    const double sv = (-2.0 / 3.0) * mu;
+    const double td = sv * (D[0][0] + D[1][1] + D[2][2]);
+    fv[0] = 0.0;
+    if (A == 0) {
+        const double txx = td + 2 * mu * D[0][0];
+        const double txy = mu * (D[0][1] + D[1][0]);
+        const double txz = mu * (D[0][2] + D[2][0]);
+        fv[1] = txx; fv[2] = txy; fv[3] = txz;
+        fv[4] = uu[0] * txx + uu[1] * txy + uu[2] * txz;
+    } else if (A == 1) {
+        const double tyy = td + 2 * mu * D[1][1];
+        const double txy = mu * (D[0][1] + D[1][0]);
+        const double tyz = mu * (D[1][2] + D[2][1]);
+        fv[1] = txy; fv[2] = tyy; fv[3] = tyz;
+        fv[4] = uu[0] * txy + uu[1] * tyy + uu[2] * tyz;
+    } else {
+        const double tzz = td + 2 * mu * D[2][2];
+        const double txz = mu * (D[0][2] + D[2][0]);
+        const double tyz = mu * (D[1][2] + D[2][1]);
+        fv[1] = txz; fv[2] = tyz; fv[3] = tzz;
+        fv[4] = uu[0] * txz + uu[1] * tyz + uu[2] * tzz;
+    }
+}
+
 // Venkatakrishnan l-function (Limiters.h:102-115).
 __device__ __forceinline__ double venkat(double um, double ui, double d2, double umax, double umin, double eps2) {
     const double un = 0.5 * (umax - umin);
@@ -551,6 +746,14 @@ __global__ void k_recon(PlainBufs b, Phys ph) {
     }
 }
 
+__device__ __forceinline__ double face_area(const PlainBufs& b, int nd, int a, int i, int j, int k) {
+    const Layout& L = b.L;
+    const double hx = b.ch[0][i + L.gx], hy = b.ch[1][j + L.gy], hz = b.ch[2][k + L.gz];
+    if (a == 0) return nd == 1 ? 1.0 : (nd == 2 ? hy : hy * hz);
+    if (a == 1) return nd == 2 ? hx : hx * hz;
+    return hx * hy;
+}
+
 // Face-centred sample of a cell's reconstruction (SampleSolution).
 __device__ __forceinline__ void sample(const PlainBufs& b, const Phys& ph, long long c, int a, double s,
                                        double out[NV]) {
@@ -606,9 +809,32 @@ __global__ void k_flux(PlainBufs b, Phys ph) {
     } else {
         lam = (ph.solver == TS_RS_HLLC) ? hllc_flux<A>(ph, UL, UR, F) : roe_flux<A>(ph, UL, UR, F);
     }
+    // viscous flux subtracted from the convective one (ExplicitRungeKuttaFVM.h:1220-1222);
+    // the cell values and gradients of the ghost cells serve the domain faces
+    if (ph.viscous) {
+        double fv[NV];
+        visc_flux<A>(b, ph, cf - st, cf, s, fv);
+#pragma unroll
+        for (int v = 0; v < NV; ++v) F[v] -= fv[v];
+    }
 #pragma unroll
     for (int v = 0; v < NV; ++v) b.F[A][vidx(L, v) + cf] = F[v];
     b.Lam[A][cf] = lam;
+    // viscous spectral-radius term of the face for its left cell (:1239-1248),
+    // Prandtl number 1, only for faces whose left cell is interior
+    if (ph.visc != 0.0 && s > 0) {
+        const double roFace = sqrt(UL[0] * UR[0]);
+        const double t1 = 4.0 / (3.0 * roFace), t2 = ph.gamma / roFace;
+        double vsr = (t1 < t2) ? t2 : t1;
+        vsr *= ph.visc / 1.0;
+        const double fS = face_area(b, ph.nd, A, i, j, k);
+        vsr *= fS * fS;
+        int il = i, jl = j, kl = k;
+        if (A == 0) il -= 1; else if (A == 1) jl -= 1; else kl -= 1;
+        const double Vl = b.ch[0][il + L.gx] * b.ch[1][jl + L.gy] * b.ch[2][kl + L.gz];
+        vsr /= Vl;
+        b.VSR[A][cf] = vsr;
+    }
 }
 
 __device__ __forceinline__ double warp_min(double v) {
@@ -617,13 +843,6 @@ __device__ __forceinline__ double warp_min(double v) {
     return v;
 }
 
-__device__ __forceinline__ double face_area(const PlainBufs& b, int nd, int a, int i, int j, int k) {
-    const Layout& L = b.L;
-    const double hx = b.ch[0][i + L.gx], hy = b.ch[1][j + L.gy], hz = b.ch[2][k + L.gz];
-    if (a == 0) return nd == 1 ? 1.0 : (nd == 2 ? hy : hy * hz);
-    if (a == 1) return nd == 2 ? hx : hx * hz;
-    return hx * hy;
-}
 
 // Spectral radius per cell in the reference's accumulation order (x-left,
 // x-right, y-left, ...), V/SR, block min by warp shuffles; the high-side
@@ -647,6 +866,7 @@ __global__ void k_dt(PlainBufs b, Phys ph) {
             const long long st = L.stride(a);
             sr += fS * b.Lam[a][c];
             sr += fS * b.Lam[a][c + st];
+            if (ph.visc != 0.0) sr += b.VSR[a][c + st];
             if (ix[a] == L.n(a) - 1) {
                 double hg[3] = {hx, hy, hz};
                 hg[a] = b.ch[a][L.n(a) + (a == 0 ? L.gx : (a == 1 ? L.gy : L.gz))];
@@ -813,6 +1033,14 @@ cudaError_t plain_step(const PlainBufs& b, const Phys& ph, cudaStream_t st, cuda
     mark("k_ghost_x");
     if (ph.nd > 1) { k_ghost<1><<<ghost_grid(1), blk, 0, st>>>(b, ph); mark("k_ghost_y"); }
     if (ph.nd > 2) { k_ghost<2><<<ghost_grid(2), blk, 0, st>>>(b, ph); mark("k_ghost_z"); }
+    if (ph.viscous) {
+        k_vgrad<<<cells, blk, 0, st>>>(b, ph);
+        mark("k_vgrad");
+        k_vgrad_bc<0><<<ghost_grid(0), blk, 0, st>>>(b, ph);
+        mark("k_vgrad_bc_x");
+        if (ph.nd > 1) { k_vgrad_bc<1><<<ghost_grid(1), blk, 0, st>>>(b, ph); mark("k_vgrad_bc_y"); }
+        if (ph.nd > 2) { k_vgrad_bc<2><<<ghost_grid(2), blk, 0, st>>>(b, ph); mark("k_vgrad_bc_z"); }
+    }
     if (ph.recon != TS_RECON_PIECEWISE_CONSTANT) { k_recon<<<cells, blk, 0, st>>>(b, ph); mark("k_recon"); }
     k_flux<0><<<dim3((L.nx + 1 + kPlainBlock - 1) / kPlainBlock, L.ny, L.nz), blk, 0, st>>>(b, ph);
     mark("k_flux_x");

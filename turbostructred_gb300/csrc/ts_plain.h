@@ -22,6 +22,9 @@ struct PlainBufs {
     const double* eps2;  // Venkatakrishnan eps^2 per cell (one plane) or null
     double* partial;     // per-block minima of V/SR
     Ctl* ctl;
+    double* VG;          // viscous flow: 9 planes, d(velocity d)/d(axis e) at plane 3d+e
+    double* VSR[3];      // viscosity > 0: 1 plane per axis, the face's viscous
+                         // spectral-radius term, stored at the face's right cell
 };
 
 int plain_partial_blocks(const Layout& L);
@@ -29,7 +32,7 @@ int plain_partial_blocks(const Layout& L);
 // Enqueues one step.  With `ev` non-null, records ev[0] before the first
 // launch and ev[i+1] after launch i (ev needs kPlainMaxLaunches+1 events);
 // *n_launch receives the launch count and names[i] the kernel names.
-constexpr int kPlainMaxLaunches = 10;
+constexpr int kPlainMaxLaunches = 14;
 cudaError_t plain_step(const PlainBufs& b, const Phys& ph, cudaStream_t st, cudaEvent_t* ev = nullptr,
                        int* n_launch = nullptr, const char** names = nullptr);
 
