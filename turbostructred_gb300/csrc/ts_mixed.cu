@@ -274,11 +274,11 @@ struct Tile {
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
     static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
     // resident CTAs per SM the register allocation is sized for (about 24
-    // warps per SM for 1D tiles, 16 for marching one-row tiles, whose longer
-    // items hide latency with fewer warps and more registers; two CTAs per SM
-    // for the shared-memory-heavy two-axis tiles)
+    // warps per SM for one-row tiles: sized for 16 warps, a single 1024^2
+    // problem ran 1.5 % faster but batches of problems 17 % slower; two CTAs
+    // per SM for the shared-memory-heavy two-axis tiles)
     static constexpr int WARPS = (NT + 31) / 32;
-    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : ((MARCH ? 16 : 24) + WARPS - 1) / WARPS);
+    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : (24 + WARPS - 1) / WARPS);
 
     static __device__ __forceinline__ int wslot(int p) { return TWO_PHASE ? (p & 3) : (p + 3) % 3; }
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
