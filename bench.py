@@ -60,15 +60,48 @@ def workload_config(n, precision, steps):
 
 
 def dist_init():
+    """(rank, world size, local rank, torch.distributed or None) from the
+    torchrun environment: one independent replica per GPU over NCCL (gloo on
+    hosts without CUDA, where only the host-side logic runs)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     if ws <= 1:
         return 0, 1, 0, None
     import torch
     import torch.distributed as dist
     lr = int(os.environ.get("LOCAL_RANK", "0"))
-    torch.cuda.set_device(lr)
-    dist.init_process_group("nccl")
+    if torch.cuda.is_available():
+        torch.cuda.set_device(lr)
+        dist.init_process_group("nccl")
+    else:
+        dist.init_process_group("gloo")
     return dist.get_rank(), ws, lr, dist
+
+
+def _reduce(x, dist, op):
+    if dist is None:
+        return float(x)
+    import torch
+    dev = f"cuda:{torch.cuda.current_device()}" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=op)
+    return float(t.item())
+
+
+def rank_max(x, dist):
+    """The largest x over the ranks (the slowest replica's time)."""
+    return _reduce(x, dist, dist.ReduceOp.MAX if dist is not None else None)
+
+
+def rank_sum(x, dist):
+    """The sum of x over the ranks (the units every replica processed)."""
+    return _reduce(x, dist, dist.ReduceOp.SUM if dist is not None else None)
+
+
+def replica_rate(units, seconds, dist):
+    """Whole-job rate of independent replicas: the units all ranks processed
+    divided by the slowest rank's time (the timed regions are bracketed by
+    barriers)."""
+    return rank_sum(units, dist) / rank_max(seconds, dist)
 
 
 class ClockSampler:
@@ -313,12 +346,8 @@ def run_ours(args, rank, ws, lr, dist):
     if dist is not None:
         dist.barrier()
     clocks = sampler.stop()
-    t_ms = timing["total_ms"]
-    if dist is not None:
-        t = torch.tensor([t_ms], device=f"cuda:{lr}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = ws * cells * args.steps / (t_ms / 1e3)
+    t_ms = rank_max(timing["total_ms"], dist)
+    value = replica_rate(cells * args.steps, t_ms / 1e3, dist)
 
     # roofline of the dominant kernel
     kernels = timing["kernels"]
@@ -384,7 +413,7 @@ def run_ours(args, rank, ws, lr, dist):
                 times.append(t1 - t0)
         tj = statistics.median(times)
         state_bytes = ic.size * 8
-        e2e = {"value": ws * cells * e2e_steps / tj, "unit": "cell-updates/s",
+        e2e = {"value": replica_rate(cells * e2e_steps, tj, dist), "unit": "cell-updates/s",
                "h2d_bytes_per_step": state_bytes / e2e_steps, "d2h_bytes_per_step": state_bytes / e2e_steps,
                "job": f"H2D of the {n}^3 initial state from pinned host memory, {e2e_steps} steps, D2H of the final state",
                "h2d_bytes_per_job": state_bytes, "d2h_bytes_per_job": state_bytes, "seconds_per_job": tj}
@@ -469,8 +498,9 @@ def run_tubes(args, rank, ws, lr, dist):
     clocks = sampler.stop()
     run_s = max(r["run_s"] for r in runs) if args.steps == 1 else statistics.median(r["run_s"] for r in runs)
     cu = tubes_cell_updates(runs[0]["infos"], probs)
-    value = ws * cu / run_s
+    value = replica_rate(cu, run_s, dist)
     e2e_s = statistics.median(r["add_s"] + r["run_s"] + r["get_s"] for r in runs)
+    e2e_value = replica_rate(cu, e2e_s, dist)
     health = sum(1 for inf in runs[0]["infos"] if inf["health"])
     iters = [inf["iteration"] for inf in runs[0]["infos"]]
     st = runs[0]["stats"]
@@ -497,7 +527,7 @@ def run_tubes(args, rank, ws, lr, dist):
                            "warmup_step": "the first 128 tubes solved to t_end",
                            "l2": "state resident in HBM; each stage touches every active tube once",
                            "tile": runs[0]["choice"]},
-                "e2e": {"value": ws * cu / e2e_s, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_in,
+                "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_in,
                         "d2h_bytes_per_step": bytes_in, "seconds_per_job": e2e_s},
                 "clocks": clocks, "gpu_launches": st["launches"],
                 "batch": {"stages": st["stages"], "launches": st["launches"], "cell_updates": cu,
@@ -565,8 +595,16 @@ def run_served(args, rank, ws, lr, dist, emit=True):
     clocks = sampler.stop()
     st = srv.stats()
     srv.close()
-    lat_ms = sorted(1e3 * (f - s) for s, a, f, it in lat)
-    wait_ms = sorted(1e3 * (a - s) for s, a, f, it in lat)
+    lat_ms = [1e3 * (f - s) for s, a, f, it in lat]
+    wait_ms = [1e3 * (a - s) for s, a, f, it in lat]
+    if dist is not None:
+        # every replica's requests count in the percentiles
+        parts = [None] * ws
+        dist.all_gather_object(parts, (lat_ms, wait_ms))
+        lat_ms = [x for p in parts for x in p[0]]
+        wait_ms = [x for p in parts for x in p[1]]
+    lat_ms.sort()
+    wait_ms.sort()
 
     def pct(v, p):
         import math
@@ -575,7 +613,7 @@ def run_served(args, rank, ws, lr, dist, emit=True):
     cu = st["cell_updates"] - st0["cell_updates"]
     first = min(s for s, a, f, it in lat)
     last = max(f for s, a, f, it in lat)
-    value = cu / (last - first)
+    value = replica_rate(cu, last - first, dist)
     bytes_io = sum(c["nx"] * c["ny"] * 40 for _, c, _, _ in reqs)
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": len(reqs),
@@ -638,8 +676,8 @@ def run_shear(args, rank, ws, lr, dist):
             clocks = sampler.stop() if sampler else None
             out[name] = dict(state=s.get_state(), info=info, ms=tm["total_ms"], kernels=tm["kernels"], clocks=clocks,
                              launches=tm["launches"])
-    t_ms = out["mixed"]["ms"]
-    value = ws * cells * args.shear_steps / (t_ms / 1e3)
+    t_ms = rank_max(out["mixed"]["ms"], dist)
+    value = replica_rate(cells * args.shear_steps, t_ms / 1e3, dist)
     kernels = out["mixed"]["kernels"]
     top = max(kernels, key=kernels.get)
     peak, peak_kind = measured_peak()
@@ -696,7 +734,7 @@ def run_batch2d(args, rank, ws, lr, dist):
     s1 = b.stats()
     clocks = sampler.stop()
     b.close()
-    value = ws * (s1["cell_updates"] - s0["cell_updates"]) / (t1 - t0)
+    value = replica_rate(s1["cell_updates"] - s0["cell_updates"], t1 - t0, dist)
     if rank == 0:
         print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (t1 - t0) / args.steps,
