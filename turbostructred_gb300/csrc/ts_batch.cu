@@ -134,6 +134,9 @@ struct Tune {
 const int kTiles1D[3] = {512, 256, 128};
 const int kTiles2D[3] = {260, 132, 68};
 constexpr int kRowsPerItem = 64;  // marching-axis rows per work item of a 2D problem
+// Work lists of at most this many items close each problem's step inside the
+// stage kernel; longer lists use the separate finish kernel.
+constexpr long long kFusedCloseItems = 1024;
 
 // The one-row tile of a problem with nx cells per row.  1D: the tile that
 // covers the row with the fewest warp-slots per cell, charging each column
@@ -172,6 +175,9 @@ struct ts_batch {
     cudaEvent_t fork = nullptr, join[kSide] = {};
     int* d_slots = nullptr;   // listed problems (closed by the finish kernel)
     int slots_cap = 0, n_listed = 0;
+    // short work lists close each problem's step in the stage kernel itself
+    // (the CTA finishing a problem's last item), saving the finish launch
+    bool fused_close = false;
     Arena arena;
     std::vector<Slot> slots;
     std::vector<ProbDesc> desc;
@@ -318,6 +324,9 @@ struct ts_batch {
         }
         for (auto& og : groups) cudaFree(og.d_items);
         groups.swap(ng);
+        long long total = 0;
+        for (auto& g : groups) total += g.n;
+        fused_close = total <= kFusedCloseItems;
         // the listed problems, for the stage's finish kernel
         std::vector<int> listed;
         for (auto& kv : bykey) listed.insert(listed.end(), kv.second.begin(), kv.second.end());
@@ -348,15 +357,17 @@ struct ts_batch {
                 st = side[(k - 1) % kSide];
                 if (k - 1 < kSide) cudaStreamWaitEvent(st, fork, 0);
             }
-            mixed_launch_batch(g.nd, g.tx, g.ty, g.solver, g.grid, d_desc, d_ctl, g.d_items, g.n, st);
+            mixed_launch_batch(g.nd, g.tx, g.ty, g.solver, g.grid, d_desc, d_ctl, g.d_items, g.n, st, fused_close);
             ++launches;
         }
         for (int k = 0; k < std::min(ng - 1, kSide); ++k) {
             cudaEventRecord(join[k], side[k]);
             cudaStreamWaitEvent(stream, join[k], 0);
         }
-        mixed_batch_finish(d_desc, d_slots, n_listed, stream);
-        ++launches;
+        if (!fused_close) {
+            mixed_batch_finish(d_desc, d_slots, n_listed, stream);
+            ++launches;
+        }
         ++stages;
     }
 
@@ -400,7 +411,7 @@ struct ts_batch {
                 }
                 TB_CUDA(cudaGraphLaunch(ex, stream));
                 stages += c;
-                launches += (long long)c * (long long)(groups.size() + 1);
+                launches += (long long)c * (long long)(groups.size() + (fused_close ? 0 : 1));
                 n -= c;
             }
         }

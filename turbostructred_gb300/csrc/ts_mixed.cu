@@ -1001,7 +1001,8 @@ template <class T, int SOLVER, bool BATCH>
 __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_constant__ ProbDesc one,
                                                     const ProbDesc* __restrict__ probs,
                                                     const Ctl* __restrict__ ctls,
-                                                    const int2* __restrict__ items, int n_items) {
+                                                    const int2* __restrict__ items, int n_items,
+                                                    int close_in_kernel) {
     extern __shared__ float sm[];
     __shared__ float wmax[32];
     __shared__ unsigned int whealth[32];
@@ -1043,7 +1044,8 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
             float srmax = 0.0f;
             unsigned int health = 0;
             process_item<T, SOLVER>(sd, pq.y, s_par, f64_to_f32(s_dt), sm, bp, pf, rp, srmax, health);
-            close_item<T, false>(sd, srmax, health, wmax, whealth);
+            if (close_in_kernel) close_item<T, true>(sd, srmax, health, wmax, whealth);
+            else close_item<T, false>(sd, srmax, health, wmax, whealth);
         }
     }
 }
@@ -1143,19 +1145,20 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
 void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const ProbDesc& h_desc, cudaStream_t st) {
     if (grid <= 0 || h_desc.nq <= 0) return;
     with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
-        k_mix_step<T, S, false><<<grid, T::NT, T::BYTES, st>>>(h_desc, nullptr, nullptr, nullptr, h_desc.nq);
+        k_mix_step<T, S, false><<<grid, T::NT, T::BYTES, st>>>(h_desc, nullptr, nullptr, nullptr, h_desc.nq, 0);
     });
 }
 
 bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const Ctl* d_ctls,
-                        const int2* d_items, int n_items, cudaStream_t st) {
+                        const int2* d_items, int n_items, cudaStream_t st, bool close_in_kernel) {
     if (nd == 3) return false;
     if (grid <= 0 || n_items <= 0) return true;
     ProbDesc none;
     std::memset(&none, 0, sizeof none);
     return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
         if constexpr (!T::HAS_Y)
-            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items);
+            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items,
+                                                                  close_in_kernel ? 1 : 0);
     });
 }
 

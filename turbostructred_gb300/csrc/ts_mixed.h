@@ -87,9 +87,12 @@ void mixed_launch_single(int nd, int tx, int ty, int solver, int grid, const Pro
 // One stage of a list of (problem, item) pairs of 1D or 2D problems sharing
 // the solver and tile (d_ctls[p] is problem p's control word); false when no
 // batched kernel exists for (nd, tile).  The stage is closed afterwards by
-// mixed_batch_finish over the listed problems.
+// mixed_batch_finish over the listed problems, or, with close_in_kernel, by
+// the CTA that completes each problem's last item (one launch per stage
+// instead of two; the returned per-item atomics cost more than the saved
+// launch when the list is long).
 bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const ProbDesc* d_probs, const Ctl* d_ctls,
-                        const int2* d_items, int n_items, cudaStream_t st);
+                        const int2* d_items, int n_items, cudaStream_t st, bool close_in_kernel = false);
 void mixed_batch_finish(const ProbDesc* d_probs, const int* d_slots, int n, cudaStream_t st);
 
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
