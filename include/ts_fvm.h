@@ -330,6 +330,14 @@ ts_status ts_batch_remove(ts_batch* b, int32_t id);
    and CTAs per SM of the persistent grid (0 = as many as fit). */
 ts_status ts_batch_set_tile(ts_batch* b, int32_t nd, int32_t tx, int32_t ty, int32_t ctas_per_sm);
 
+/* The batch's tail mode (on by default): once every unfinished problem is
+   1D, fits one thread-block cluster (at most 16 x 508 cells) and all of them
+   together fit the GPU at once, each launch advances every problem by up to
+   the requested number of stages in the cluster tail kernel, with the state
+   kept on chip between stages; results are identical to the stage-by-stage
+   path.  enable = 0 keeps the stage-by-stage path throughout. */
+ts_status ts_batch_set_tail(ts_batch* b, int32_t enable);
+
 /* Autotuner: times `stages` stages of the current batch for the per-problem
    policy and every compiled tile, each at several CTA counts, restoring the
    problems' states after each trial, and keeps the fastest; *tx (0: per

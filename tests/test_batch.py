@@ -261,3 +261,47 @@ def test_batch_admission_and_retirement_beside_queued_stages(tslib):
     for k in range(len(probs)):
         assert results[k][1]["iteration"] == alone[k][1]["iteration"]
         assert np.array_equal(results[k][0], alone[k][0]), k
+
+
+def tail_tubes():
+    """1D problems that end in the batch's tail mode: sizes up to 16 clusters'
+    worth of cells, PWC/limited/ENO2, Roe/HLLC, stiffened gas, periodic."""
+    from turbostructred_gb300 import capi
+    tube = [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
+    stiff = [0.5, 1.5, 0.2, 4.0, 0.8, -0.3, 0.5]
+    specs = [
+        (dict(ndims=1, nx=4096, periodic=(0, 1, 1), recon=3, solver=1, cfl=0.5, bc=[NAT] * 6), tube, 0.05),
+        (dict(ndims=1, nx=1531, periodic=(0, 1, 1), recon=0, solver=3, cfl=0.5, bc=[NAT] * 6), tube, 0.08),
+        (dict(ndims=1, nx=2000, periodic=(0, 1, 1), recon=3, solver=1, gamma=4.4, eos=1, p_inf=6.0, cfl=0.5,
+              bc=[NAT] * 6), stiff, 0.01),
+        (dict(ndims=1, nx=777, periodic=(1, 1, 1), recon=2, solver=3, cfl=0.4), tube, 0.05),
+        (dict(ndims=1, nx=8128, periodic=(0, 1, 1), recon=3, limiter=1, solver=1, cfl=0.5, bc=[SYM] * 6), tube,
+         0.004),
+        (dict(ndims=1, nx=508, periodic=(0, 1, 1), recon=0, solver=1, cfl=0.5, bc=[NAT] * 6), tube, 0.1),
+    ]
+    out = []
+    for n, (kw, params, t_end) in enumerate(specs):
+        case = capi.make_case(**dict(kw, max_time=t_end, max_iter=100000))
+        out.append((case, capi.fill_scenario(case, 0, 31 + n, params)))
+    return out
+
+
+def test_batch_tail_mode_equals_stage_path(tslib):
+    """The cluster tail kernel (state on chip, many stages per launch) gives
+    the stage-by-stage result bit for bit, in far fewer launches."""
+    from turbostructred_gb300 import capi
+    probs = tail_tubes()
+    res, launches = {}, {}
+    for tail in (True, False):
+        with capi.Batch(BUDGET) as b:
+            b.set_tail(tail)
+            ids = [b.add(c, v) for c, v in probs]
+            assert b.run() == 0
+            res[tail] = [b.get(i) for i in ids]
+            launches[tail] = b.stats()["launches"]
+    for (got, info), (ref, rinfo) in zip(res[True], res[False]):
+        assert info["iteration"] == rinfo["iteration"]
+        assert info["time"] == rinfo["time"] and info["dt"] == rinfo["dt"]
+        assert info["health"] == rinfo["health"] == 0
+        assert np.array_equal(got, ref)
+    assert launches[True] < launches[False] / 4

@@ -122,7 +122,7 @@ EXPORTS = [
     "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
     "ts_batch_create", "ts_batch_destroy", "ts_batch_add", "ts_batch_problem_bytes", "ts_batch_step",
     "ts_batch_run", "ts_batch_finished", "ts_batch_get", "ts_batch_remove", "ts_batch_set_tile",
-    "ts_batch_autotune", "ts_batch_stats", "ts_batch_launch", "ts_batch_wait",
+    "ts_batch_autotune", "ts_batch_stats", "ts_batch_launch", "ts_batch_wait", "ts_batch_set_tail",
     "ts_server_create", "ts_server_destroy", "ts_server_submit", "ts_server_wait", "ts_server_drain",
     "ts_server_stats_get",
     "ts_save_solution", "ts_load_solution", "ts_save_tecplot", "ts_wait_writes", "ts_write_solution_file",
@@ -173,6 +173,7 @@ def load(path: str = LIB_PATH):
     L.ts_batch_get.argtypes = [C.c_void_p, C.c_int32, P(C.c_double), P(StepInfo)]
     L.ts_batch_remove.argtypes = [C.c_void_p, C.c_int32]
     L.ts_batch_set_tile.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+    L.ts_batch_set_tail.argtypes = [C.c_void_p, C.c_int32]
     L.ts_batch_autotune.argtypes = [C.c_void_p, C.c_int32, P(C.c_int32), P(C.c_int32), P(C.c_int32)]
     L.ts_batch_stats.argtypes = [C.c_void_p, P(C.c_double), P(C.c_int64), P(C.c_int64)]
     L.ts_batch_launch.argtypes = [C.c_void_p, C.c_int32]
@@ -496,6 +497,9 @@ class Batch:
 
     def set_tile(self, nd: int, tx: int, ty: int = 1, ctas_per_sm: int = 0):
         check(self.lib.ts_batch_set_tile(self.b, nd, tx, ty, ctas_per_sm))
+
+    def set_tail(self, enable: bool):
+        check(self.lib.ts_batch_set_tail(self.b, int(bool(enable))))
 
     def autotune(self, stages: int = 8):
         tx, ty, ct = C.c_int32(), C.c_int32(), C.c_int32()

@@ -178,6 +178,12 @@ struct ts_batch {
     // short work lists close each problem's step in the stage kernel itself
     // (the CTA finishing a problem's last item), saving the finish launch
     bool fused_close = false;
+    // the last few long 1D problems run in the cluster tail kernel: many
+    // stages per launch, state on chip (one list per Riemann solver)
+    bool tail_enabled = true, tail_mode = false;
+    int tail_cluster = 0;
+    int* d_tail[2] = {nullptr, nullptr};
+    int tail_n[2] = {0, 0}, tail_cap[2] = {0, 0};
     Arena arena;
     std::vector<Slot> slots;
     std::vector<ProbDesc> desc;
@@ -212,6 +218,8 @@ struct ts_batch {
         drop_graphs();
         for (auto& g : groups) cudaFree(g.d_items);
         cudaFree(d_slots);
+        cudaFree(d_tail[0]);
+        cudaFree(d_tail[1]);
         for (int k = 0; k < kSide; ++k) {
             if (side[k]) cudaStreamDestroy(side[k]);
             if (join[k]) cudaEventDestroy(join[k]);
@@ -327,6 +335,8 @@ struct ts_batch {
         long long total = 0;
         for (auto& g : groups) total += g.n;
         fused_close = total <= kFusedCloseItems;
+        ts_status ts = plan_tail();
+        if (ts != TS_OK) return ts;
         // the listed problems, for the stage's finish kernel
         std::vector<int> listed;
         for (auto& kv : bykey) listed.insert(listed.end(), kv.second.begin(), kv.second.end());
@@ -342,6 +352,44 @@ struct ts_batch {
         TB_CUDA(cudaStreamSynchronize(stream));
         drop_graphs();
         dirty = false;
+        return TS_OK;
+    }
+
+    // Tail mode when every unfinished problem is 1D, fits one cluster, and
+    // all clusters together fit the GPU at once (one CTA per SM).
+    ts_status plan_tail() {
+        tail_mode = false;
+        tail_n[0] = tail_n[1] = 0;
+        if (!tail_enabled) return TS_OK;
+        const int cells = mixed_tail_cells();
+        std::vector<int> lists[2];
+        int cmax = 0, nact = 0;
+        for (int s = 0; s < capacity; ++s) {
+            if (!slots[s].used || h_ctl[s].stop_req) continue;
+            const ProbDesc& d = desc[s];
+            const int items = (d.kn[0] + cells - 1) / cells;
+            if (d.L.nd != 1 || items > kTailMaxCluster) return TS_OK;
+            cmax = std::max(cmax, items);
+            lists[d.mp.solver == TS_RS_HLLC ? 1 : 0].push_back(s);
+            ++nact;
+        }
+        if (nact == 0 || (long long)nact * cmax > sms) return TS_OK;
+        for (int k = 0; k < 2; ++k)
+            if (!lists[k].empty() && !mixed_tail_ready(k ? TS_RS_HLLC : TS_RS_ROE_PIKE, cmax)) return TS_OK;
+        for (int k = 0; k < 2; ++k) {
+            tail_n[k] = (int)lists[k].size();
+            if (!tail_n[k]) continue;
+            if (tail_n[k] > tail_cap[k]) {
+                cudaFree(d_tail[k]);
+                d_tail[k] = nullptr;
+                tail_cap[k] = std::max(64, tail_n[k]);
+                TB_CUDA(cudaMalloc(&d_tail[k], sizeof(int) * tail_cap[k]));
+            }
+            TB_CUDA(cudaMemcpyAsync(d_tail[k], lists[k].data(), sizeof(int) * tail_n[k], cudaMemcpyHostToDevice,
+                                    stream));
+        }
+        tail_cluster = cmax;
+        tail_mode = true;
         return TS_OK;
     }
 
@@ -382,6 +430,17 @@ struct ts_batch {
             stable = 0;
         }
         if (groups.empty()) return TS_OK;
+        if (tail_mode) {
+            // every tail problem advances up to n stages in one launch
+            for (int k = 0; k < 2; ++k) {
+                if (!tail_n[k]) continue;
+                TB_CUDA(mixed_launch_tail(k ? TS_RS_HLLC : TS_RS_ROE_PIKE, tail_cluster, tail_n[k], d_desc, d_tail[k],
+                                          n, stream));
+                ++launches;
+            }
+            stages += n;
+            return TS_OK;
+        }
         if (stable < 2) {
             ++stable;
             for (int k = 0; k < n; ++k) enqueue_stage();
@@ -726,6 +785,15 @@ ts_status ts_batch_remove(ts_batch* b, int32_t id) {
     b->h_ctl[slot].stop_req = 1;
     TB_CUDA(cudaMemcpyAsync(b->d_ctl + slot, &b->h_ctl[slot], sizeof(Ctl), cudaMemcpyHostToDevice, b->stream));
     b->id2slot.erase(it);
+    b->dirty = true;
+    return TS_OK;
+}
+
+ts_status ts_batch_set_tail(ts_batch* b, int32_t enable) {
+    if (!b) return fail(TS_ERR_INVALID, "NULL batch");
+    DevGuard g(b->device);
+    TB_CUDA(cudaStreamSynchronize(b->stream));
+    b->tail_enabled = enable != 0;
     b->dirty = true;
     return TS_OK;
 }

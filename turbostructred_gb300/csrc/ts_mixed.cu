@@ -41,6 +41,7 @@
 // conversions included), so FP64<->FP32 conversions are done with integer
 // bit operations and the only FP64 arithmetic per owned cell is the five
 // state additions.
+#include <cooperative_groups.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -766,21 +767,21 @@ __device__ __forceinline__ CellGeo cell_geo(const ProbDesc& d, int i0, int j0) {
     return c;
 }
 
-// Residual and spectral radius of the owned cell of this thread in plane z
-// (hz, ihz: size and inverse size of plane z).
+// Residual R and spectral radius of the owned cell of this thread in plane z
+// (hz, ihz: size and inverse size of plane z); false if the thread owns no
+// cell.
 template <class T, int SOLVER>
-__device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
-                                         int z, const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
-                                         float& srmax) {
+__device__ __forceinline__ bool residual_of(const ProbDesc& d, const float* sm, int i0, int j0, int z, const Slots& s,
+                                            float4 own, const CellGeo& cg, float hz, float ihz, float& srmax,
+                                            float R[NV]) {
     int tx, ty;
-    if (!T::cell(threadIdx.x, tx, ty)) return;
+    if (!T::cell(threadIdx.x, tx, ty)) return false;
     const int gi = i0 + tx, gj = j0 + ty;
-    if (gi >= d.kn[0] || gj >= d.kn[1]) return;
+    if (gi >= d.kn[0] || gj >= d.kn[1]) return false;
     const float fsx = cg.hy * hz, fsy = cg.hx * hz, fsz = cg.fsz;
     const float iv = cg.ixy * ihz;
     // face areas times the stored-flux factor
     const float kx = flux_scale<SOLVER>() * fsx, ky = flux_scale<SOLVER>() * fsy, kz = flux_scale<SOLVER>() * fsz;
-    float R[NV];
     const float lxl = sm[T::fx(5, ty, tx)], lxr = sm[T::fx(5, ty, tx + 1)];
 #pragma unroll
     for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * kx;
@@ -822,7 +823,19 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
             R[4] += ((ro * mp.g[0]) * vu + (ro * mp.g[1]) * vv + (ro * mp.g[2]) * vw) * vol;
         }
     }
-    const long long c = d.kbase + gi + gj * d.kstr[1] + z * d.kstr[2];
+    return true;
+}
+
+// The same, written to the pending-residual planes Rout.
+template <class T, int SOLVER>
+__device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
+                                         int z, const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
+                                         float& srmax) {
+    float R[NV];
+    if (!residual_of<T, SOLVER>(d, sm, i0, j0, z, s, own, cg, hz, ihz, srmax, R)) return;
+    int tx, ty;
+    T::cell(threadIdx.x, tx, ty);
+    const long long c = d.kbase + (i0 + tx) + (j0 + ty) * d.kstr[1] + z * d.kstr[2];
     const long long plane = d.L.plane;
 #pragma unroll
     for (int v = 0; v < NV; ++v) __stcg(Rout + v * plane + c, R[v]);
@@ -831,8 +844,7 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
 // dt of one problem from its CFL maximum, and the step's bookkeeping
 // (ComputeTimeStep :1427-1437, time += dt and iteration++ :1486-1487, and the
 // Kernel::Run snapshot/termination rules kernel.h:1763-1846).
-__device__ void finish_problem(Ctl* ctl, double cfl) {
-    const float m = __uint_as_float(*(volatile unsigned int*)&ctl->srmax_bits);
+__device__ __forceinline__ void finish_with(Ctl* ctl, float m, double cfl) {
     double dt = cfl / (double)m;
     if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
     if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
@@ -849,6 +861,10 @@ __device__ void finish_problem(Ctl* ctl, double cfl) {
         if ((ctl->save_slice > 0) && (ctl->next_slice == ctl->time)) ctl->next_slice += ctl->save_slice;
         if (ctl->iteration == ctl->max_iteration || ctl->time >= ctl->max_time) ctl->stop_req = 1;
     }
+}
+
+__device__ void finish_problem(Ctl* ctl, double cfl) {
+    finish_with(ctl, __uint_as_float(*(volatile unsigned int*)&ctl->srmax_bits), cfl);
 }
 
 // ---------------------------------------------------------------------------
@@ -1050,6 +1066,183 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
     }
 }
 
+
+// ---------------------------------------------------------------------------
+// Tail kernel: the last few long 1D problems of a batch, one thread-block
+// cluster per problem, many stages per launch
+// ---------------------------------------------------------------------------
+// Each CTA of the cluster owns 508 consecutive cells and keeps their FP64
+// state and FP32 pending residual in registers from stage to stage; halo
+// cells come from the neighbouring CTAs' shared memory (distributed shared
+// memory) and the CFL maximum is reduced into the first CTA's shared memory.
+// Per stage: the pending update and working copy of the own cells, a cluster
+// barrier, the halo pulls, slopes, faces and residual exactly as the batched
+// kernel computes them for the same cells, the cluster-wide maximum, a second
+// cluster barrier, and the step bookkeeping of finish_problem, which every
+// CTA repeats on its own copy of the control word (the same maximum gives
+// every CTA the same dt and the same stop decision, so all CTAs run the same
+// number of stages and barriers).
+using TailTile = Tile<512, 1, false>;
+
+template <int SOLVER>
+__global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict__ probs,
+                                                     const int* __restrict__ list, int budget) {
+    using T = TailTile;
+    namespace cg = cooperative_groups;
+    cg::cluster_group cluster = cg::this_cluster();
+    extern __shared__ float sm[];
+    float* rbuf = sm + T::TOTAL;            // residual of the own cells, NV planes of TX
+    __shared__ float wmax[32];
+    __shared__ unsigned int whealth[32];
+    __shared__ unsigned int red[2][2];      // per stage parity: max bits, health (first CTA's are used)
+    __shared__ Ctl sc;                      // this CTA's copy of the control word
+    __shared__ int s_stop;
+    const int tid = threadIdx.x;
+    const unsigned int rank = cluster.block_rank();
+    const ProbDesc& d = probs[list[blockIdx.x / cluster.num_blocks()]];
+    const MixPhys& mp = d.mp;
+    const int i0 = (int)rank * T::TX;
+    const long long plane = d.L.plane;
+    if (tid < 4) red[tid >> 1][tid & 1] = 0u;
+    if (tid == 0) {
+        sc = *d.ctl;
+        s_stop = sc.stop_req;
+    }
+    const int kind = recon_kind(mp);
+    const bool pwc = kind == 0;
+    const bool src = mp.force || mp.accel;
+    const bool stiff = mp.eos == TS_EOS_STIFFENED_GAS;
+    BoxPos bp[T::NA];
+    RingPos rp[T::NB];
+    setup_box<T>(d, i0, 0, bp);
+    if (!pwc) setup_ring<T>(d, i0, 0, rp);
+    const CellGeo cg0 = cell_geo<T>(d, i0, 0);
+    const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
+    const Slots sl = slots_of<T>(0);
+    const bool own = bp[0].off >= 0 && bp[0].own;
+    __syncthreads();
+    double u[NV];
+    float r[NV];
+    if (own) {
+        const int par = sc.parity;
+        const long long c = d.kbase + bp[0].off;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            u[v] = __ldcg(d.U[par] + v * plane + c);
+            r[v] = __ldcg(d.R[par] + v * plane + c);
+        }
+    }
+    cluster.sync();  // every CTA's reduction slots are zero before any remote update
+    for (int st = 0; st < budget; ++st) {
+        if (s_stop) break;
+        unsigned int health = 0;
+        // pending update of the own cell and its working copy (store())
+        if (own) {
+            const float cf = bp[0].cfxy * (f64_to_f32(sc.dt_apply) * gz.ih);
+            float inc[NV], w[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
+#pragma unroll
+            for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
+            w[4] = (stiff ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4])) + inc[4];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp[0].box)] = w[v];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) u[v] = u[v] + f32_to_f64(inc[v]);
+            const long long b = __double_as_longlong(u[0]);
+            if (b <= 0 || b > 0x7FF0000000000000LL)
+                health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
+            if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
+        }
+        cluster.sync();
+        // halo positions: the owner's working copy, then the boundary image
+        if (bp[0].off >= 0 && !own) {
+            const int si = bp[0].off;
+            const int orank = si / T::TX;
+            const float* owner = cluster.map_shared_rank(sm, orank);
+            const int opos = si - orank * T::TX + HB;
+            float w[NV];
+#pragma unroll
+            for (int v = 0; v < NV; ++v) w[v] = owner[T::w(0, v, opos)];
+            if (bp[0].xs >= 0) bc32(mp, bp[0].xs, 0, w);
+#pragma unroll
+            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp[0].box)] = w[v];
+        }
+        __syncthreads();
+        if (!pwc) { recon<T>(d, sm, 0, kind, sl, rp); __syncthreads(); }
+        fluxes<T, SOLVER>(d, sm, i0, 0, 0, pwc, true, false, sl);
+        const float4 ow = src ? own_state<T>(sm, sl) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+        __syncthreads();
+        float srmax = 0.0f, R[NV];
+        if (residual_of<T, SOLVER>(d, sm, i0, 0, 0, sl, ow, cg0, gz.h, gz.ih, srmax, R)) {
+#pragma unroll
+            for (int v = 0; v < NV; ++v) rbuf[v * T::TX + tid] = R[v];
+        }
+        // CTA maximum and health into the first CTA's slots
+        const int lane = tid & 31, wid = tid >> 5;
+        const unsigned int mbits = __reduce_max_sync(0xffffffffu, __float_as_uint(srmax));
+        const unsigned int hw = __reduce_or_sync(0xffffffffu, health);
+        if (lane == 0) { wmax[wid] = __uint_as_float(mbits); whealth[wid] = hw; }
+        __syncthreads();
+        if (tid == 0) {
+            float m = 0.0f;
+            unsigned int hh = 0;
+            for (int k = 0; k < T::NT / 32; ++k) { m = fmaxf(m, wmax[k]); hh |= whealth[k]; }
+            unsigned int* slot = cluster.map_shared_rank(&red[st & 1][0], 0);
+            if (m > 0.0f) atomicMax(slot, __float_as_uint(m));
+            if (hh) atomicOr(slot + 1, hh);
+        }
+        cluster.sync();
+        if (tid == 0) {
+            const unsigned int* slot = cluster.map_shared_rank(&red[st & 1][0], 0);
+            const float m = __uint_as_float(slot[0]);
+            const unsigned int hh = slot[1];
+            sc.health |= hh;
+            finish_with(&sc, m, mp.cfl);
+            // the first CTA clears the slots of the next stage (read by
+            // nobody since the previous stage's second barrier)
+            if (rank == 0) { red[(st + 1) & 1][0] = 0u; red[(st + 1) & 1][1] = 0u; }
+            // a non-physical state stops the loop; the host stops the problem
+            s_stop = sc.stop_req || hh != 0;
+        }
+        __syncthreads();
+        if (own) {
+            const int lx = bp[0].box - HB;
+#pragma unroll
+            for (int v = 0; v < NV; ++v) r[v] = rbuf[v * T::TX + lx];
+        }
+    }
+    // the state and pending residual back where the batched kernel expects
+    // them, and the control word
+    __syncthreads();
+    if (own) {
+        const int par = sc.parity;
+        const long long c = d.kbase + bp[0].off;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) {
+            d.U[par][v * plane + c] = u[v];
+            d.R[par][v * plane + c] = r[v];
+        }
+    }
+    if (rank == 0 && tid == 0) {
+        Ctl* g = d.ctl;
+        g->time = sc.time;
+        g->dt = sc.dt;
+        g->dt_min_raw = sc.dt_min_raw;
+        g->dt_apply = sc.dt_apply;
+        g->iteration = sc.iteration;
+        g->parity = sc.parity;
+        g->next_sol = sc.next_sol;
+        g->next_slice = sc.next_slice;
+        g->stop_req = sc.stop_req;
+        g->health = sc.health;
+        g->srmax_bits = 0u;
+        g->blocks_done = 0u;
+    }
+    // no CTA leaves while another may still read its shared memory
+    cluster.sync();
+}
+
 // U[parity] += dt R[parity] / V, R[parity] = 0 for problem p (materialise the
 // pending update with the fused kernel's own rounding: (1/h0 h1) (dt / h2)
 // over kernel axes).
@@ -1160,6 +1353,67 @@ bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const Prob
             k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items,
                                                                   close_in_kernel ? 1 : 0);
     });
+}
+
+int mixed_tail_cells() { return TailTile::TX; }
+
+namespace {
+template <int S>
+bool tail_ready_for(int cluster) {
+    const size_t bytes = TailTile::BYTES + sizeof(float) * NV * TailTile::TX;
+    if (cudaFuncSetAttribute(k_mix_tail<S>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) != cudaSuccess)
+        return false;
+    if (cluster > 8 &&
+        cudaFuncSetAttribute(k_mix_tail<S>, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess)
+        return false;
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cluster);
+    cfg.blockDim = dim3(TailTile::NT);
+    cfg.dynamicSmemBytes = bytes;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    int n = 0;
+    if (cudaOccupancyMaxActiveClusters(&n, k_mix_tail<S>, &cfg) != cudaSuccess) {
+        cudaGetLastError();
+        return false;
+    }
+    return n > 0;
+}
+
+template <int S>
+cudaError_t tail_launch(int cluster, int n_problems, const ProbDesc* d_probs, const int* d_list, int budget,
+                        cudaStream_t st) {
+    cudaLaunchConfig_t cfg = {};
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = cluster;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.gridDim = dim3(cluster * n_problems);
+    cfg.blockDim = dim3(TailTile::NT);
+    cfg.dynamicSmemBytes = TailTile::BYTES + sizeof(float) * NV * TailTile::TX;
+    cfg.stream = st;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k_mix_tail<S>, d_probs, d_list, budget);
+}
+}  // namespace
+
+bool mixed_tail_ready(int solver, int cluster) {
+    if (cluster < 1 || cluster > kTailMaxCluster) return false;
+    return solver == TS_RS_HLLC ? tail_ready_for<TS_RS_HLLC>(cluster) : tail_ready_for<TS_RS_ROE_PIKE>(cluster);
+}
+
+cudaError_t mixed_launch_tail(int solver, int cluster, int n_problems, const ProbDesc* d_probs, const int* d_list,
+                              int budget, cudaStream_t st) {
+    if (n_problems <= 0 || budget <= 0) return cudaSuccess;
+    return solver == TS_RS_HLLC ? tail_launch<TS_RS_HLLC>(cluster, n_problems, d_probs, d_list, budget, st)
+                                : tail_launch<TS_RS_ROE_PIKE>(cluster, n_problems, d_probs, d_list, budget, st);
 }
 
 void mixed_tile_cells(int nd, int tx, int ty, int* cx, int* cy) {

@@ -95,6 +95,17 @@ bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const Prob
                         const int2* d_items, int n_items, cudaStream_t st, bool close_in_kernel = false);
 void mixed_batch_finish(const ProbDesc* d_probs, const int* d_slots, int n, cudaStream_t st);
 
+// Tail of a batch: n_problems 1D problems (d_list: their descriptor indices),
+// each advanced by up to `budget` stages in one launch by a cluster of
+// `cluster` CTAs that own mixed_tail_cells() cells each and keep the state
+// on chip between stages (same arithmetic as the batched kernel).
+constexpr int kTailMaxCluster = 16;
+int mixed_tail_cells();
+// The tail kernel can run clusters of this size on this device.
+bool mixed_tail_ready(int solver, int cluster);
+cudaError_t mixed_launch_tail(int solver, int cluster, int n_problems, const ProbDesc* d_probs, const int* d_list,
+                              int budget, cudaStream_t st);
+
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
                      const DeviceAlloc& alloc, MixedBufs& mb, std::string& err);
 // Choose the tile shape (tx, ty) and the z chunking (0 = automatic), and
