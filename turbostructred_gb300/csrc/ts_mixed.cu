@@ -17,20 +17,25 @@
 // Work items.  A problem is cut into tile columns of TX x TY cells (x-y,
 // compile-time, one thread per tile cell) and, in 3D, z chunks; one item is
 // one (problem, column, chunk).  A CTA marches z through its item (2.5D
-// blocking), keeping a 3-plane ring of the FP32 working state with a 2-cell
-// halo, a 2-plane ring of limited half-slopes with a 1-cell halo and the
-// face fluxes in shared memory.  Every thread has fixed roles: up to two
-// working-state positions of the halo box (the next plane's loads are issued
-// into registers as soon as the current plane is stored, so their latency
-// hides behind the plane's compute), up to two reconstruction positions, the
-// x face left of its cell, the y face below, the z face above (the tile's far
-// faces go to the first TX + TY threads), and its cell's residual.  Items are
+// blocking), keeping a ring of the FP32 working state with a 2-cell halo
+// (four planes for 3D tiles, which run two phases per plane; three for the
+// one-row 1D/2D tiles, three phases), a 2-plane ring of limited half-slopes
+// with a 1-cell halo and the face fluxes in shared memory.  Every thread has
+// fixed roles: up to two working-state positions of the halo box (the next
+// plane's loads are issued into registers as soon as the current plane is
+// stored, so their latency hides behind the plane's compute), up to two
+// reconstruction positions (second rounds dealt from the last thread), the
+// x face left of its cell and the y face below (solved side by side), the z
+// face above (the tile's far faces go to the first and the last warp), and
+// its cell's residual.  Items are
 // indexed z-chunk-major and dealt round-robin to the persistent CTAs, so CTAs
 // running at the same time sweep neighbouring columns at the same z and share
 // halo rows through L2.  Each problem has its own control word: the CTA that
 // completes a problem's last item turns its CFL maximum into that problem's
 // dt, so many problems of different sizes advance with their own time steps
-// in one launch.
+// in one launch.  The last few long 1D problems of a batch run in the
+// cluster tail kernel (k_mix_tail) instead: state on chip, many stages per
+// launch.
 //
 // Ghost cells are virtual: a load outside the domain wraps on periodic axes
 // and mirrors plus applies the boundary condition (BCGeneral.h:186-268)
