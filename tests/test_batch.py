@@ -286,11 +286,16 @@ def tail_tubes():
     return out
 
 
-def test_batch_tail_mode_equals_stage_path(tslib):
+@pytest.mark.parametrize("limits", ["t_end", "max_iter_and_snapshots"])
+def test_batch_tail_mode_equals_stage_path(limits, tslib):
     """The cluster tail kernel (state on chip, many stages per launch) gives
-    the stage-by-stage result bit for bit, in far fewer launches."""
+    the stage-by-stage result bit for bit, in far fewer launches, with the
+    Run loop's end conditions and SaveSolutionTime's dt clipping."""
     from turbostructred_gb300 import capi
     probs = tail_tubes()
+    if limits != "t_end":
+        probs = [(dict(c, max_time=1e30, max_iter=37 + 11 * k, save_solution_time=c["max_time"] / 7), v)
+                 for k, (c, v) in enumerate(probs)]
     res, launches = {}, {}
     for tail in (True, False):
         with capi.Batch(BUDGET) as b:
