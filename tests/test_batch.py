@@ -17,6 +17,8 @@ pytestmark = pytest.mark.gpu
 RHO_L1 = 1e-5
 NAT = (5, 0.0, (0.0, 0.0, 0.0), 0.0)
 SYM = (1, 0.0, (0.0, 0.0, 0.0), 0.0)
+WALL = (0, 0.0, (0.0, 0.0, 0.0), 0.0)
+INLET = (3, 1.2, (0.4, 0.0, 0.0), 1.1)
 BUDGET = 256 << 20
 
 
@@ -278,6 +280,10 @@ def tail_tubes():
         (dict(ndims=1, nx=8128, periodic=(0, 1, 1), recon=3, limiter=1, solver=1, cfl=0.5, bc=[SYM] * 6), tube,
          0.004),
         (dict(ndims=1, nx=508, periodic=(0, 1, 1), recon=0, solver=1, cfl=0.5, bc=[NAT] * 6), tube, 0.1),
+        (dict(ndims=1, nx=1017, periodic=(0, 1, 1), recon=3, solver=3, cfl=0.45, external_force=(0.3, 0.0, 0.0),
+              uniform_acceleration=(-0.2, 0.0, 0.0), bc=[INLET, WALL] + [NAT] * 4), tube, 0.05),
+        (dict(ndims=1, nx=300, periodic=(0, 1, 1), recon=3, solver=1, cfl=0.5,
+              bc=[(2, 0.0, (0.2, 0.0, 0.0), 0.0), (4, 0.0, (0.0, 0.0, 0.0), 0.0)] + [NAT] * 4), tube, 0.08),
     ]
     out = []
     for n, (kw, params, t_end) in enumerate(specs):
