@@ -155,15 +155,16 @@ def measured_peak():
         return 6800.0, "fallback"
 
 
-def profile_traffic(kernel, cells):
-    """DRAM bytes per launch of `kernel` over `cells` cells: the committed ncu
-    capture's bytes per cell (dram__bytes_read.sum + dram__bytes_write.sum over
-    the captured launch's cells) times the cell count, or None."""
+def profile_traffic(workload, kernel, cells):
+    """DRAM bytes per launch of `kernel` over `cells` cells in `workload`: the
+    committed ncu capture's bytes per cell (dram__bytes_read.sum +
+    dram__bytes_write.sum over the captured launch's cells) times the cell
+    count, or None."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            rec = json.load(f).get(kernel)
-        return float(rec["bytes_per_cell"]) * cells if rec else None
+            rec = json.load(f).get(workload)
+        return float(rec["bytes_per_cell"]) * cells if rec and rec["kernel"] == kernel else None
     except Exception:
         return None
 
@@ -362,7 +363,7 @@ def run_ours(args, rank, ws, lr, dist):
         alg_note = "80 B x cells per step, charged to the dominant kernel of the FP64 path"
     achieved = alg / (top_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": profile_traffic(top, cells) if precision == "mixed" else None, "kernel": top,
+                "traffic": profile_traffic("blast3d", top, cells) if precision == "mixed" else None, "kernel": top,
                 "kernel_ms": top_ms,
                 "peak_source": f"{peak_kind} (MEASURED_PEAKS.json hbm_gbs)" if peak_kind == "measured" else peak_kind,
                 "algorithmic_bytes": alg, "algorithmic_note": alg_note,
@@ -693,7 +694,8 @@ def run_shear(args, rank, ws, lr, dist):
                            "l2": "state 84 MB per FP64 copy: below L2 (129 MB); the mixed step also moves "
                                  "the FP32 residual, 2 x 42 MB, so its working set spills"},
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                             "frac": achieved / peak, "traffic": None, "kernel": top, "kernel_ms": kernels[top],
+                             "frac": achieved / peak, "traffic": profile_traffic("shear2d", top, cells), "kernel": top,
+                             "kernel_ms": kernels[top],
                              "peak_source": peak_kind},
                 "fp64_value": cells * args.shear_steps / (out["fp64"]["ms"] / 1e3),
                 "mixed_over_fp64": out["fp64"]["ms"] / t_ms,
