@@ -744,6 +744,99 @@ def run_batch2d(args, rank, ws, lr, dist):
                           "clocks": clocks, "gpu_launches": s1["launches"] - s0["launches"]}), flush=True)
 
 
+def run_rows(args, rank, ws, lr, dist):
+    """The paths beyond the explicit step proper, each timed on the GPU with the
+    oracle port (the reference's algorithm, all host threads) beside it:
+    exact Godunov flux (FP64 path), source terms (mixed path), viscous flow
+    (FP64 path), and the solution-file and Tecplot writers."""
+    import numpy as np
+
+    from oracle import oracle as O
+    from turbostructred_gb300 import build, capi, workloads
+    if rank == 0 or dist is None:
+        build.build()
+    if dist is not None:
+        dist.barrier()
+    capi.load()
+    threads = os.cpu_count() or 1
+    nat = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
+    wall = (capi.BC_WALL, 0.0, (0.0, 0.0, 0.0), 0.0)
+    movw = (capi.BC_MOVING_WALL, 0.0, (0.3, 0.0, 0.0), 0.0)
+    quad = [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03, 0.53, 0.0, 1.2, 0.3]
+    heavy_top = [2.0, 0.0, 0.0, 2.5, 2.0, 0.0, 0.0, 2.5, 1.0, 0.0, 0.0, 2.5, 1.0, 0.0, 0.0, 2.5]
+    n = 512
+    rows = {
+        "godunov": ("exact Godunov flux, 2D quadrant problem 512^2, Linear2psLim(BJ), FP64 path",
+                    dict(ndims=2, nx=n, ny=n, periodic=(0, 0, 1), recon=capi.RECON_LINEAR2_LIM,
+                         solver=capi.RS_GODUNOV, cfl=0.4, bc=[nat] * 6), capi.PRECISION_FP64,
+                    capi.SCENARIO_QUADRANTS, quad, 20),
+        "sources": ("uniform acceleration (Rayleigh-Taylor set-up) 512^2, Linear2psLim(BJ)+Roe, mixed path",
+                    dict(ndims=2, nx=n, ny=n, periodic=(1, 0, 1), recon=capi.RECON_LINEAR2_LIM,
+                         solver=capi.RS_ROE, cfl=0.4, uniform_acceleration=(0.0, -1.0, 0.0),
+                         bc=[nat, nat, wall, wall, nat, nat]), capi.PRECISION_MIXED,
+                    capi.SCENARIO_QUADRANTS, heavy_top, 200),
+        "viscous": ("viscous channel 512^2 (periodic x, wall and moving wall), mu = 1e-3, Linear2psLim(BJ)+Roe, "
+                    "FP64 path", dict(ndims=2, nx=n, ny=n, periodic=(1, 0, 1), recon=capi.RECON_LINEAR2_LIM,
+                                      solver=capi.RS_ROE, cfl=0.4, viscous=True, viscosity=1e-3,
+                                      bc=[nat, nat, wall, movw, nat, nat]), capi.PRECISION_FP64,
+                    capi.SCENARIO_SHEAR_LAYER, [2.0, 1.0, 0.5, 2.5, 0.05], 20),
+    }
+    out = {}
+    for key, (desc, kw, prec, scen, params, steps) in rows.items():
+        case = capi.make_case(**dict(kw, max_iter=10**6, max_time=1e30))
+        ic = capi.fill_scenario(case, scen, 5, params)
+        with capi.Solver(case, prec, device=lr) as s:
+            s.set_state(ic)
+            s.step(3)
+            _, tm = s.step_timed(steps)
+        gpu_s = rank_max(tm["total_ms"] / 1e3, dist)
+        value = rank_sum(n * n * steps, dist) / gpu_s
+        cpu = None
+        if rank == 0 and not args.skip_cpu:
+            full = O.embed(case, ic)
+            t0 = time.perf_counter()
+            full, _ = O.advance(case, full, 2, threads=threads)
+            # a sample of about 3 s of host work
+            k = max(2, min(400, int(3.0 / max((time.perf_counter() - t0) / 2, 1e-6))))
+            t0 = time.perf_counter()
+            O.advance(case, full, k, threads=threads)
+            secs = time.perf_counter() - t0
+            cpu = {"value": n * n * k / secs, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                   "sample": f"{k} RK steps of the same {n}^2 case after 2 warm-up steps", "seconds": secs}
+        out[key] = {"workload": desc, "value": value, "unit": "cell-updates/s", "steps": steps,
+                    "ms_per_step": 1e3 * gpu_s / steps, "precision": "fp64" if prec == capi.PRECISION_FP64 else
+                    "mixed", "gpu_launches": tm["launches"], "cpu_baseline": cpu}
+    # solution files: Kernel::SaveSolution binary and the Tecplot text of a 128^3 state
+    io = {}
+    m = 128
+    case = workload_case(capi, m)
+    ic = capi.fill_scenario(case, capi.SCENARIO_BLAST, 3, BLAST)
+    with tempfile.TemporaryDirectory() as d, capi.Solver(case, capi.PRECISION_MIXED, device=lr) as s:
+        s.set_state(ic)
+        s.step(2)
+        s.synchronize()
+        for name, fn in (("save_solution", lambda p: s.save_solution(p)),
+                         ("save_tecplot", lambda p: (s.save_tecplot(p), s.wait_writes()))):
+            path = os.path.join(d, name)
+            t0 = time.perf_counter()
+            fn(path)
+            secs = time.perf_counter() - t0
+            io[name] = {"bytes": os.path.getsize(path), "seconds": secs,
+                        "MB_per_s": os.path.getsize(path) / secs / 1e6}
+    out["solution_files"] = {"workload": f"3D blast state {m}^3 written by ts_save_solution and ts_save_tecplot",
+                             **io}
+    if rank == 0:
+        line = {"metric": METRIC, "value": out["viscous"]["value"], "unit": "cell-updates/s", "n_gpus": ws,
+                "steps": out["viscous"]["steps"], "warmup": 3, "ms_per_step": out["viscous"]["ms_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded scenarios, no dataset)",
+                "config": {"workload": "the rows beyond the explicit step: exact Godunov flux, source terms, "
+                                       "viscous flow (value), solution files", "grid": [n, n]},
+                "rows": out,
+                "gpu_launches": sum(v["gpu_launches"] for k, v in out.items() if k != "solution_files")}
+        print(json.dumps(line), flush=True)
+
+
 def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
@@ -761,7 +854,8 @@ def main():
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
-    p.add_argument("--workload", choices=["blast3d", "tubes", "served", "shear2d", "batch2d"], default="blast3d")
+    p.add_argument("--workload", choices=["blast3d", "tubes", "served", "shear2d", "batch2d", "rows"],
+                   default="blast3d")
     p.add_argument("--shear-steps", type=int, default=1000)
     p.add_argument("--skip-served", action="store_true")
     p.add_argument("--served-sample-seconds", type=float, default=10.0)
@@ -786,7 +880,7 @@ def main():
         return
     rank, ws, lr, dist = dist_init()
     {"blast3d": run_ours, "tubes": run_tubes, "served": run_served, "shear2d": run_shear,
-     "batch2d": run_batch2d}[args.workload](
+     "batch2d": run_batch2d, "rows": run_rows}[args.workload](
         args, rank, ws, lr, dist)
     if dist is not None:
         dist.destroy_process_group()

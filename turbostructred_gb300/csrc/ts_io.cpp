@@ -10,7 +10,9 @@
 // Asynchronous Tecplot writes snapshot the state to host memory on the
 // calling thread and format/write it on a worker thread, so the device can
 // continue stepping; ts_wait_writes (and ts_destroy) join them.
+#include <algorithm>
 #include <cstdint>
+#include <cstdio>
 #include <cstring>
 #include <fstream>
 #include <map>
@@ -35,6 +37,34 @@ Dims dims_of(const ts_config& c) {
     return Dims{c.n_dims, c.nx, c.n_dims > 1 ? c.ny : 1, c.n_dims > 2 ? c.nz : 1};
 }
 
+// The text of `count` lines, line n produced by put(buf, n) (which returns the
+// line's length, at most 256 bytes), formatted by several threads into
+// per-range buffers and written in order: the same bytes as the reference's
+// line-by-line ofstream output (std::scientific with the default precision
+// is printf's "%.6e"; std::endl and '\n' write the same byte).
+template <class Put>
+void write_lines(std::ofstream& ofs, long long count, Put put) {
+    if (count <= 0) return;
+    const long long per = 1 << 16;
+    const int nt = (int)std::max<long long>(
+        1, std::min<long long>((count + per - 1) / per, std::max(1u, std::thread::hardware_concurrency())));
+    std::vector<std::string> parts(nt);
+    auto work = [&](int t) {
+        const long long b = count * t / nt, e = count * (t + 1) / nt;
+        std::string& out = parts[t];
+        out.reserve((size_t)(e - b) * 16);
+        char buf[256];
+        for (long long n = b; n < e; ++n) out.append(buf, (size_t)put(buf, n));
+    };
+    std::vector<std::thread> th;
+    for (int t = 1; t < nt; ++t) th.emplace_back(work, t);
+    work(0);
+    for (auto& x : th) x.join();
+    for (auto& p : parts) ofs.write(p.data(), (std::streamsize)p.size());
+}
+
+inline int put_e(char* buf, double x) { return std::snprintf(buf, 256, "%.6e\n", x); }
+
 // Interior values are x fastest, then y, then z, 5 doubles per cell.
 ts_status write_tecplot(const ts_config& c, const double* U, double time, double molar_mass, double gas_constant,
                         const std::string& path, std::string& err) {
@@ -58,8 +88,8 @@ ts_status write_tecplot(const ts_config& c, const double* U, double time, double
         ofs << "\"" << "w" << "\" ";
         ofs << "\"" << "P" << "\" ";
         ofs << "\"" << "e" << "\" ";
-        ofs << std::endl;
-        for (int i = 0; i < d.nx; ++i) {
+        ofs << '\n';
+        write_lines(ofs, d.nx, [&](char* buf, long long i) {
             const double x = g.x[i + 1];
             const double ro = cellv(i, 0);
             const double u = cellv(i, 1) / ro;
@@ -67,15 +97,8 @@ ts_status write_tecplot(const ts_config& c, const double* U, double time, double
             const double w = cellv(i, 3) / ro;
             const double e = cellv(i, 4) / ro - 0.5 * (u * u + v * v + w * w);
             const double P = (gamma - 1.0) * ro * e;
-            ofs << x << " ";
-            ofs << ro << " ";
-            ofs << u << " ";
-            ofs << v << " ";
-            ofs << w << " ";
-            ofs << P << " ";
-            ofs << e << " ";
-            ofs << std::endl;
-        }
+            return std::snprintf(buf, 256, "%.6e %.6e %.6e %.6e %.6e %.6e %.6e \n", x, ro, u, v, w, P, e);
+        });
         ofs.close();
         return ofs ? TS_OK : (err = "write failed: " + path, TS_ERR_INVALID);
     }
@@ -95,10 +118,15 @@ ts_status write_tecplot(const ts_config& c, const double* U, double time, double
         for (int k = 0; k < 6; ++k) ofs << ", CELLCENTERED";
         ofs << ", CELLCENTERED)";
         ofs << std::endl;
-        for (int j = 1; j <= d.ny + 1; ++j)
-            for (int i = 1; i <= d.nx + 1; ++i) { ofs << g.x[i] - 0.5 * g.hx[i]; ofs << std::endl; }
-        for (int j = 1; j <= d.ny + 1; ++j)
-            for (int i = 1; i <= d.nx + 1; ++i) { ofs << g.y[j] - 0.5 * g.hy[j]; ofs << std::endl; }
+        const long long nxn = d.nx + 1, nyn = d.ny + 1;
+        write_lines(ofs, nxn * nyn, [&](char* buf, long long n) {
+            const long long i = n % nxn + 1;
+            return put_e(buf, g.x[i] - 0.5 * g.hx[i]);
+        });
+        write_lines(ofs, nxn * nyn, [&](char* buf, long long n) {
+            const long long j = n / nxn + 1;
+            return put_e(buf, g.y[j] - 0.5 * g.hy[j]);
+        });
         for (long long n = 0; n < ncell; ++n) {
             rho[n] = cellv(n, 0);
             u[n] = cellv(n, 1) / rho[n];
@@ -124,15 +152,20 @@ ts_status write_tecplot(const ts_config& c, const double* U, double time, double
         for (int k = 0; k < 6; ++k) ofs << ", CELLCENTERED";
         ofs << ", CELLCENTERED)";
         ofs << std::endl;
-        for (int k = 1; k <= d.nz + 1; ++k)
-            for (int j = 1; j <= d.ny + 1; ++j)
-                for (int i = 1; i <= d.nx + 1; ++i) { ofs << g.x[i] - 0.5 * g.hx[i]; ofs << std::endl; }
-        for (int k = 1; k <= d.nz + 1; ++k)
-            for (int j = 1; j <= d.ny + 1; ++j)
-                for (int i = 1; i <= d.nx + 1; ++i) { ofs << g.y[j] - 0.5 * g.hy[j]; ofs << std::endl; }
-        for (int k = 1; k <= d.nz + 1; ++k)
-            for (int j = 1; j <= d.ny + 1; ++j)
-                for (int i = 1; i <= d.nx + 1; ++i) { ofs << g.z[k] - 0.5 * g.hz[k]; ofs << std::endl; }
+        const long long nxn = d.nx + 1, nyn = d.ny + 1, nzn = d.nz + 1;
+        const long long nn = nxn * nyn * nzn;
+        write_lines(ofs, nn, [&](char* buf, long long n) {
+            const long long i = n % nxn + 1;
+            return put_e(buf, g.x[i] - 0.5 * g.hx[i]);
+        });
+        write_lines(ofs, nn, [&](char* buf, long long n) {
+            const long long j = (n / nxn) % nyn + 1;
+            return put_e(buf, g.y[j] - 0.5 * g.hy[j]);
+        });
+        write_lines(ofs, nn, [&](char* buf, long long n) {
+            const long long k = n / (nxn * nyn) + 1;
+            return put_e(buf, g.z[k] - 0.5 * g.hz[k]);
+        });
         for (long long n = 0; n < ncell; ++n) {
             rho[n] = cellv(n, 0);
             const double mx = cellv(n, 1), my = cellv(n, 2), mz = cellv(n, 3);
@@ -147,31 +180,24 @@ ts_status write_tecplot(const ts_config& c, const double* U, double time, double
         }
     }
     for (const std::vector<double>* a : {&rho, &u, &v, &w, &P, &e, &T})
-        for (double r : *a) ofs << r << '\n';
+        write_lines(ofs, ncell, [&](char* buf, long long n) { return put_e(buf, (*a)[n]); });
     if (d.nd == 2) {
-        for (int j = 0; j < d.ny; ++j) {
-            int bl = (d.nx + 1) * j + 1;  // Tecplot node numbers start at 1
-            for (int i = 0; i < d.nx; ++i) {
-                const int br = bl + 1, ul = bl + (d.nx + 1), ur = ul + 1;
-                ofs << bl << ' ' << ul << ' ' << ur << ' ' << br;
-                ofs << std::endl;
-                bl++;
-            }
-        }
+        // cell (i, j): its four nodes, Tecplot node numbers starting at 1
+        write_lines(ofs, (long long)d.nx * d.ny, [&](char* buf, long long n) {
+            const int i = (int)(n % d.nx), j = (int)(n / d.nx);
+            const int bl = (d.nx + 1) * j + 1 + i;
+            const int br = bl + 1, ul = bl + (d.nx + 1), ur = ul + 1;
+            return std::snprintf(buf, 256, "%d %d %d %d\n", bl, ul, ur, br);
+        });
     } else {
         const int nxy = (d.nx + 1) * (d.ny + 1);
-        for (int k = 0; k < d.nz; ++k)
-            for (int j = 0; j < d.ny; ++j) {
-                int fbl = nxy * k + (d.nx + 1) * j + 1;
-                for (int i = 0; i < d.nx; ++i) {
-                    const int fbr = fbl + 1, ful = fbl + (d.nx + 1), fur = ful + 1;
-                    const int bbl = fbl + nxy, bbr = bbl + 1, bul = bbl + (d.nx + 1), bur = bul + 1;
-                    ofs << bbr << ' ' << bur << ' ' << bul << ' ' << bbl << ' ' << fbr << ' ' << fur << ' ' << ful
-                        << ' ' << fbl;
-                    ofs << std::endl;
-                    fbl++;
-                }
-            }
+        write_lines(ofs, ncell, [&](char* buf, long long n) {
+            const int i = (int)(n % d.nx), j = (int)((n / d.nx) % d.ny), k = (int)(n / ((long long)d.nx * d.ny));
+            const int fbl = nxy * k + (d.nx + 1) * j + 1 + i;
+            const int fbr = fbl + 1, ful = fbl + (d.nx + 1), fur = ful + 1;
+            const int bbl = fbl + nxy, bbr = bbl + 1, bul = bbl + (d.nx + 1), bur = bul + 1;
+            return std::snprintf(buf, 256, "%d %d %d %d %d %d %d %d\n", bbr, bur, bul, bbl, fbr, fur, ful, fbl);
+        });
     }
     ofs.close();
     if (!ofs) { err = "write failed: " + path; return TS_ERR_INVALID; }
