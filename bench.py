@@ -255,10 +255,11 @@ def run_reference(args, rank, ws):
                 "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
-    if args.workload in ("shear2d", "batch2d"):
+    if args.workload in ("shear2d", "batch2d", "rows"):
         # the reference algorithm (oracle port, OpenMP over all host threads)
-        # on the same 2D grids: the 1024^2 shear layer, or one 512^2 quadrant
-        # problem of the batch, for a bounded number of steps
+        # on the same 2D grids: the 1024^2 shear layer, one 512^2 quadrant
+        # problem of the batch, or the 512^2 viscous channel of the rows
+        # line, for a bounded number of steps
         from oracle import oracle as O
         from turbostructred_gb300 import capi, workloads
         if args.workload == "shear2d":
@@ -266,6 +267,15 @@ def run_reference(args, rank, ws):
                                   solver=capi.RS_HLLC, cfl=0.4, max_iter=10**6, max_time=1e30)
             ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7, [2.0, 1.0, 0.5, 2.5, 0.01])
             steps, sample = 60, "60 RK steps of the 1024^2 shear layer"
+        elif args.workload == "rows":
+            nat = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
+            wall = (capi.BC_WALL, 0.0, (0.0, 0.0, 0.0), 0.0)
+            movw = (capi.BC_MOVING_WALL, 0.0, (0.3, 0.0, 0.0), 0.0)
+            case = capi.make_case(ndims=2, nx=512, ny=512, periodic=(1, 0, 1), recon=capi.RECON_LINEAR2_LIM,
+                                  solver=capi.RS_ROE, cfl=0.4, viscous=True, viscosity=1e-3, max_iter=10**6,
+                                  max_time=1e30, bc=[nat, nat, wall, movw, nat, nat])
+            ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 5, [2.0, 1.0, 0.5, 2.5, 0.05])
+            steps, sample = 200, "200 RK steps of the 512^2 viscous channel"
         else:
             case = workloads.quadrant_case(512, capi.RS_ROE, 10**6)
             ic = workloads.stream_state(case, [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03,
