@@ -316,3 +316,28 @@ def test_batch_tail_mode_equals_stage_path(limits, tslib):
         assert info["health"] == rinfo["health"] == 0
         assert np.array_equal(got, ref)
     assert launches[True] < launches[False] / 4
+
+
+def test_c4_full_batch_sampled_against_fp64_oracle(tslib, oracle_mod):
+    """The 4096-tube workload at full size: every tube finishes (or is stopped
+    unhealthy), and sampled small tubes agree with the FP64 oracle run to the
+    same end time within the mixed-precision bar."""
+    from oracle import oracle as O
+    from turbostructred_gb300 import capi, workloads
+    probs = workloads.tubes(4096, seed=4096)
+    budget = int(1.5 * sum(capi.batch_problem_bytes(c) for c, _ in probs)) + (64 << 20)
+    with capi.Batch(budget) as b:
+        ids = [b.add(c, v) for c, v in probs]
+        assert b.run() == 0
+        res = [b.get(i) for i in ids]
+    healthy = [k for k, (_, info) in enumerate(res) if info["health"] == 0]
+    assert len(healthy) >= 4000
+    sample = [k for k in healthy if probs[k][0]["nx"] < 200][::7][:8]
+    assert len(sample) >= 4
+    for k in sample:
+        case, ic = probs[k]
+        got, info = res[k]
+        ref, rinfo = oracle_mod.advance(case, O.embed(case, ic), -1)
+        assert info["iteration"] == rinfo["iteration"], k
+        ref_i = ref[0, 0, 1:-1].reshape(got.shape)
+        assert l1(got, ref_i, 0) <= RHO_L1, (k, l1(got, ref_i, 0))
