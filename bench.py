@@ -115,7 +115,7 @@ class ClockSampler:
         self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
         try:
             self.p = subprocess.Popen(["nvidia-smi", "--query-gpu=" + self.Q, "--format=csv,noheader,nounits",
-                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+                                       "-lms", "100"], stdout=self.f, stderr=subprocess.DEVNULL)
         except OSError:
             self.p = None
 
@@ -851,7 +851,8 @@ def main():
     p = argparse.ArgumentParser()
     p.add_argument("--gpus", type=int, default=1)
     p.add_argument("--steps", type=int, default=None,
-                   help="timed steps (default 200; tubes: 3, a step being the whole batch solved to t_end)")
+                   help="timed steps (default 500 for blast3d, 200 otherwise; tubes: 3, a step being the whole "
+                        "batch solved to t_end)")
     p.add_argument("--warmup", type=int, default=None, help="untimed warm-up steps (default 5; tubes: 3)")
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
     p.add_argument("--precision", choices=["auto", "mixed", "fp64"], default="auto")
@@ -881,7 +882,8 @@ def main():
     p.add_argument("--max-cells", type=float, default=16e6)
     args = p.parse_args()
     if args.steps is None:
-        args.steps = 3 if args.workload == "tubes" else 200
+        # the 3D blast's timed region spans ~0.7 s (several clock samples)
+        args.steps = 3 if args.workload == "tubes" else (500 if args.workload == "blast3d" else 200)
     if args.warmup is None:
         args.warmup = 3 if args.workload == "tubes" else 5
     if args.impl == "reference":
