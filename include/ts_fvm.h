@@ -155,7 +155,8 @@ typedef struct ts_step_info {
     double dt;
     double next_solution_time;
     double next_slice_time;
-    double residual[5];  /* volume-weighted L1 residual norms (kernel.h:326) */
+    double residual[5];  /* volume-weighted L1 residual norms (kernel.h:326); the FP64
+                            path forms them every step, the mixed path reports zeros */
 } ts_step_info;
 
 typedef struct ts_handle ts_handle;
