@@ -18,10 +18,15 @@ Lines printed (rank 0, one JSON line):
                              the final state) timed on the host
                     roofline, cpu_baseline (oracle port on this host's cores),
                     clocks, fp64 plain-path rate and mixed-vs-FP64 errors
+                    workloads: the other configurations measured in the same
+                    run (2D shear layer 1024^2, the 4096 batched tubes, a
+                    10 s sample of the served stream), each with its own
+                    e2e, roofline, CPU baseline and mixed-vs-FP64 error
   --impl reference  the reference algorithm's CPU implementation (the
-                    oracle port, all host threads) on a bounded sample of the
-                    same workload: each step is one RK step over a
-                    256x256x16 slab of the blast.
+                    oracle port, all host threads) on the same workload: each
+                    step is one RK step over the whole 256^3 blast, whose
+                    initial state the oracle builds itself (the product
+                    library is not loaded).
 With torchrun (N>1) every rank advances its own replica (weak scaling).
 """
 from __future__ import annotations
@@ -52,10 +57,12 @@ def workload_case(capi, n, nz=None, periodic_z=False):
                           eps=0.0, max_iter=200, max_time=1e30, bc=[sym] * 6)
 
 
-def workload_config(n, precision, steps):
+def workload_config(n):
+    """The workload, identical on both arms (the arithmetic of each arm is in
+    its `dtype` and `precision` keys)."""
     return {"workload": f"3D ideal-gas blast {n}^3, Symmetry walls, Linear2psLim(BJ)+Roe, RK1, CFL 0.4",
-            "grid": [n, n, n], "cells": n ** 3, "steps_timed": steps, "precision": precision,
-            "state": "FP64 SoA in HBM (687 MB per copy at 256^3)",
+            "grid": [n, n, n], "cells": n ** 3, "seed": SEED,
+            "state": f"FP64, {n}^3 cells ({n ** 3 * 40 / 1e6:.0f} MB per copy)",
             "l2": "inputs larger than L2 (129 MB); no flush needed", "parallelism": "replicas"}
 
 
@@ -169,27 +176,24 @@ def profile_traffic(workload, kernel, cells):
         return None
 
 
-def oracle_sample_rate(steps, warmup, threads, nz=16, n=N_DEFAULT):
-    """The reference algorithm on the CPU (oracle port, OpenMP): cell-updates/s
-    of RK steps over a 256 x 256 x nz slab through the blast centre."""
-    import numpy as np
-
+def oracle_sample_rate(steps, warmup, threads, n=N_DEFAULT):
+    """The reference algorithm on the CPU (oracle port, OpenMP over `threads`
+    host threads): cell-updates/s of RK steps over the whole n^3 blast with
+    Symmetry walls, the same workload as the GPU arm; the oracle builds the
+    initial state itself (its restatement of the scenario, bit-identical to
+    the library's)."""
     from oracle import oracle as O
-    from turbostructred_gb300 import capi
-    case = workload_case(capi, n, nz=nz, periodic_z=True)
-    full_case = workload_case(capi, n)
-    ic = capi.fill_scenario(full_case, capi.SCENARIO_BLAST, SEED, BLAST)
-    k0 = n // 2 - nz // 2
-    sub = np.ascontiguousarray(ic[k0:k0 + nz])
-    full = O.embed(case, sub)
-    ocase = dict(case)
+    from turbostructred_gb300 import capi  # the plain-Python case description only
+    case = workload_case(capi, n)
+    ic = O.fill_scenario(case, O.SCENARIO_BLAST, SEED, BLAST, threads=threads)
+    full = O.embed(case, ic)
+    del ic
     if warmup:
-        full, _ = O.advance(ocase, full, warmup, threads=threads)
+        full, _ = O.advance(case, full, warmup, threads=threads)
     t0 = time.perf_counter()
-    full, info = O.advance(ocase, full, steps, threads=threads)
+    full, info = O.advance(case, full, steps, threads=threads)
     dt = time.perf_counter() - t0
-    cells = n * n * nz
-    return cells * steps / dt, dt, f"{steps} RK step(s) over a {n}x{n}x{nz} slab of the {n}^3 blast (planes {k0}-{k0 + nz - 1}), z periodic"
+    return n ** 3 * steps / dt, dt, f"{steps} RK step(s) over the whole {n}^3 blast (Symmetry walls) after {warmup} warm-up step(s)"
 
 
 def _cpu_job(job):
@@ -218,8 +222,9 @@ def cpu_pool_rate(jobs, procs):
 
 
 def tubes_cpu_sample(every=8, cap=4000, seed=4096):
+    from oracle import oracle as O
     from turbostructred_gb300 import workloads
-    probs = workloads.tubes(4096, seed=seed)
+    probs = workloads.tubes(4096, seed=seed, fill=O.fill_scenario)
     jobs = []
     for k in range(0, len(probs), every):
         c, ic = probs[k]
@@ -231,9 +236,10 @@ def tubes_cpu_sample(every=8, cap=4000, seed=4096):
 
 
 def served_cpu_sample(n_req=48, steps=16, seed=200):
+    from oracle import oracle as O
     from turbostructred_gb300 import workloads
     reqs = workloads.stream(200.0, 60.0, seed=seed)[:n_req]
-    jobs = [(c, workloads.stream_state(c, p, s), steps) for _, c, p, s in reqs]
+    jobs = [(c, workloads.stream_state(c, p, s, fill=O.fill_scenario), steps) for _, c, p, s in reqs]
     desc = (f"the first {n_req} requests of the stream, {steps} RK steps each (of 500), one process per host "
             "core, oracle port")
     return jobs, desc
@@ -265,7 +271,7 @@ def run_reference(args, rank, ws):
         if args.workload == "shear2d":
             case = capi.make_case(ndims=2, nx=1024, ny=1024, periodic=(1, 1, 1), recon=capi.RECON_LINEAR2_LIM,
                                   solver=capi.RS_HLLC, cfl=0.4, max_iter=10**6, max_time=1e30)
-            ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7, [2.0, 1.0, 0.5, 2.5, 0.01])
+            ic = O.fill_scenario(case, O.SCENARIO_SHEAR_LAYER, 7, [2.0, 1.0, 0.5, 2.5, 0.01])
             steps, sample = 60, "60 RK steps of the 1024^2 shear layer"
         elif args.workload == "rows":
             nat = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
@@ -274,12 +280,12 @@ def run_reference(args, rank, ws):
             case = capi.make_case(ndims=2, nx=512, ny=512, periodic=(1, 0, 1), recon=capi.RECON_LINEAR2_LIM,
                                   solver=capi.RS_ROE, cfl=0.4, viscous=True, viscosity=1e-3, max_iter=10**6,
                                   max_time=1e30, bc=[nat, nat, wall, movw, nat, nat])
-            ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 5, [2.0, 1.0, 0.5, 2.5, 0.05])
+            ic = O.fill_scenario(case, O.SCENARIO_SHEAR_LAYER, 5, [2.0, 1.0, 0.5, 2.5, 0.05])
             steps, sample = 200, "200 RK steps of the 512^2 viscous channel"
         else:
             case = workloads.quadrant_case(512, capi.RS_ROE, 10**6)
             ic = workloads.stream_state(case, [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03,
-                                               0.53, 0.0, 1.2, 0.3], 1)
+                                               0.53, 0.0, 1.2, 0.3], 1, fill=O.fill_scenario)
             steps, sample = 120, "120 RK steps of one 512^2 quadrant problem of the batch"
         full = O.embed(case, ic)
         full, _ = O.advance(case, full, 2, threads=threads)
@@ -297,11 +303,12 @@ def run_reference(args, rank, ws):
                 "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line), flush=True)
         return
-    rate, secs, sample = oracle_sample_rate(args.steps, args.warmup, threads)
+    rate, secs, sample = oracle_sample_rate(args.steps, args.warmup, threads, n=args.n)
     line = {"impl": "reference", "metric": METRIC, "value": rate, "unit": "cell-updates/s", "n_gpus": ws,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-            "data": "synthetic", "config": workload_config(args.n, "fp64", args.steps),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "precision": "fp64",
+            "data": "synthetic (seeded blast initial state built by the oracle, no dataset)",
+            "config": workload_config(args.n),
             "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                              "sample": sample},
             "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -429,43 +436,71 @@ def run_ours(args, rank, ws, lr, dist):
     cpu = None
     if rank == 0 and ws == 1 and not args.skip_cpu:
         threads = os.cpu_count() or 1
-        rate, secs, sample = oracle_sample_rate(args.cpu_steps, 1, threads, nz=args.cpu_nz, n=n)
+        rate, secs, sample = oracle_sample_rate(args.cpu_steps, 1, threads, n=n)
         cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port", "sample": sample,
                "seconds": secs}
+
+    # the other configurations, measured in the same run (one GPU only: under
+    # torchrun each replica would repeat them)
+    workloads = None
+    if ws == 1 and not args.skip_workloads:
+        workloads = other_workloads(args, rank, lr)
 
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
                 "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
                 "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 flux" if precision == "mixed" else "f64",
+                "precision": precision,
                 "data": "synthetic (seeded blast initial state, no dataset)",
-                "config": workload_config(n, precision, args.steps), "e2e": e2e, "roofline": roofline,
+                "config": workload_config(n), "e2e": e2e, "roofline": roofline,
                 "cpu_baseline": cpu, "clocks": clocks, "gpu_launches": timing["launches"] * ws,
                 "step_info": {"iteration": info["iteration"], "time": info["time"], "dt": info["dt"],
                               "health": info["health"]}}
         line.update(extra)
-        if ws == 1 and not args.skip_served:
-            import copy
-            a2 = copy.copy(args)
-            a2.seconds = args.served_sample_seconds
-            a2.skip_cpu = True
-            sv = run_served(a2, rank, ws, lr, None, emit=False)
-            line["served"] = {"p50_ms": sv["latency_ms"]["p50"], "p99_ms": sv["latency_ms"]["p99"],
-                              "cell_updates_per_s": sv["value"], "requests": sv["config"]["requests"],
-                              "sample": f"the first {a2.seconds:g} s of the {args.rate:g} req/s stream "
-                                        "(python bench.py --workload served runs the full 60 s)",
-                              "offered_cell_updates_per_s": sv["offered_cell_updates_per_s"],
-                              "admission": sv["config"]["admission"],
-                              "admission_wait_ms": sv["admission_wait_ms"], "clocks": sv["clocks"]}
+        if workloads is not None:
+            line["workloads"] = workloads
         print(json.dumps(line), flush=True)
+
+
+def other_workloads(args, rank, lr):
+    """The 2D shear layer (C2), the batched tubes (C4) and a sample of the
+    served stream (C5), each through its own bench function with its
+    defaults, summarised for the default bench line."""
+    import copy
+
+    def sub(**kw):
+        a = copy.copy(args)
+        a.steps, a.warmup = None, None
+        for k, v in kw.items():
+            setattr(a, k, v)
+        return a
+
+    keep = ("workload", "value", "unit", "steps", "warmup", "ms_per_step", "e2e", "roofline", "cpu_baseline",
+            "mixed_error_vs_fp64", "fp64_value", "mixed_over_fp64", "clocks", "gpu_launches", "config", "batch",
+            "latency_ms", "admission_wait_ms", "offered_cell_updates_per_s", "step_info")
+    out = {}
+    for key, fn, a in (("shear2d_1024", run_shear, sub(steps=args.shear_steps, warmup=5)),
+                       ("tubes_4096", run_tubes, sub(steps=3, warmup=3)),
+                       ("served_stream", run_served, sub(seconds=args.served_sample_seconds, warmup=0))):
+        line = fn(a, rank, 1, lr, None, emit=False)
+        if line is not None:
+            out[key] = {k: line[k] for k in keep if k in line}
+    if "served_stream" in out:
+        out["served_stream"]["sample"] = (f"the first {args.served_sample_seconds:g} s of the {args.rate:g} req/s "
+                                          "stream (python bench.py --workload served runs the full 60 s)")
+    return out
 
 
 def tubes_cell_updates(infos, probs):
     return float(sum(c["nx"] * inf["iteration"] for (c, _), inf in zip(probs, infos)))
 
 
-def run_tubes(args, rank, ws, lr, dist):
+def run_tubes(args, rank, ws, lr, dist, emit=True):
     """Batched 1D tubes: one step = the whole batch solved to t_end."""
     import torch
+
+    steps = args.steps or 3
+    warmup = 3 if args.warmup is None else args.warmup
 
     from turbostructred_gb300 import build, capi, workloads
     if rank == 0 or dist is None:
@@ -495,15 +530,15 @@ def run_tubes(args, rank, ws, lr, dist):
         return dict(add_s=t1 - t0, run_s=t3 - t2, get_s=t4 - t3, stats=st, choice=choice,
                     infos=[o[1] for o in outs], states=outs)
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         solve(probs[:128], False)
     uuid = gpu_uuid(lr)
     sampler = ClockSampler(uuid)
     if dist is not None:
         dist.barrier()
-    runs = [solve(probs, args.tune_stages > 0) for _ in range(args.steps)]
+    runs = [solve(probs, args.tune_stages > 0) for _ in range(steps)]
     clocks = sampler.stop()
-    run_s = max(r["run_s"] for r in runs) if args.steps == 1 else statistics.median(r["run_s"] for r in runs)
+    run_s = max(r["run_s"] for r in runs) if steps == 1 else statistics.median(r["run_s"] for r in runs)
     cu = tubes_cell_updates(runs[0]["infos"], probs)
     value = replica_rate(cu, run_s, dist)
     e2e_s = statistics.median(r["add_s"] + r["run_s"] + r["get_s"] for r in runs)
@@ -524,9 +559,12 @@ def run_tubes(args, rank, ws, lr, dist):
             errs.append(rel_errors(got, ref))
     err = {k: max(e[k] for e in errs) for k in errs[0]} if errs else None
     bytes_in = sum(v.size * 8 for _, v in probs)
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL_UPDATE * cu / run_s / 1e9
+    line = None
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.steps,
-                "warmup": args.warmup, "ms_per_step": 1e3 * run_s, "higher_is_better": True, "scaling": "weak",
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": steps,
+                "warmup": warmup, "ms_per_step": 1e3 * run_s, "higher_is_better": True, "scaling": "weak",
                 "vs_baseline": None, "dtype": "f64 state / f32 flux", "data": "synthetic (seeded tubes, no dataset)",
                 "config": {"workload": f"{len(probs)} batched 1D shock tubes to t_end 0.1 (sizes 64-4096 "
                                        "log-uniform, half stiffened gas, PWC/Linear2psLim mixed, Roe, CFL 0.5)",
@@ -536,6 +574,14 @@ def run_tubes(args, rank, ws, lr, dist):
                            "tile": runs[0]["choice"]},
                 "e2e": {"value": e2e_value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_in,
                         "d2h_bytes_per_step": bytes_in, "seconds_per_job": e2e_s},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": profile_traffic("tubes", "k_mix_step", cu),
+                             "kernel": "k_mix_step (batched, one-row 1D tiles) and k_mix_tail",
+                             "kernel_ms": None, "algorithmic_bytes": BYTES_PER_CELL_UPDATE * cu,
+                             "basis": "80 B x the batch's cell-updates over the whole solve's wall time (stage "
+                                      "kernels, finish kernels, the cluster tail kernel and launch gaps): a lower "
+                                      "bound of the kernels' own rate",
+                             "peak_source": peak_kind},
                 "clocks": clocks, "gpu_launches": st["launches"],
                 "batch": {"stages": st["stages"], "launches": st["launches"], "cell_updates": cu,
                           "max_iterations": max(iters), "unhealthy": health, "add_s": runs[0]["add_s"],
@@ -547,7 +593,9 @@ def run_tubes(args, rank, ws, lr, dist):
             rate, secs = cpu_pool_rate(jobs, procs)
             line["cpu_baseline"] = {"value": rate, "unit": "cell-updates/s", "cores": procs, "kind": "port",
                                     "sample": sample, "seconds": secs}
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
+    return line
 
 
 def run_served(args, rank, ws, lr, dist, emit=True):
@@ -622,6 +670,8 @@ def run_served(args, rank, ws, lr, dist, emit=True):
     last = max(f for s, a, f, it in lat)
     value = replica_rate(cu, last - first, dist)
     bytes_io = sum(c["nx"] * c["ny"] * 40 for _, c, _, _ in reqs)
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL_UPDATE * cu / (last - first) / 1e9
     if rank == 0:
         line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": len(reqs),
                 "warmup": len(workloads.SIDES), "ms_per_step": 1e3 * (last - first) / max(1, len(reqs)),
@@ -638,6 +688,14 @@ def run_served(args, rank, ws, lr, dist, emit=True):
                         "d2h_bytes_per_step": bytes_io / max(1, len(reqs)),
                         "note": "latency and throughput are end to end: host submit (copy of the initial state) "
                                 "to the final state back in host memory"},
+                "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                             "frac": achieved / peak, "traffic": profile_traffic("batch2d", "k_mix_step", cu),
+                             "kernel": "k_mix_step (batched, one-row 2D tiles)", "kernel_ms": None,
+                             "algorithmic_bytes": BYTES_PER_CELL_UPDATE * cu,
+                             "basis": "80 B x the served cell-updates over the wall time from the first "
+                                      "submission to the last result (includes uploads, read-backs and idle "
+                                      "gaps): a lower bound of the kernel's own rate",
+                             "peak_source": peak_kind},
                 "server": {k: st[k] for k in ("submitted", "completed", "rejected", "stages", "launches", "busy_s",
                                               "admit_s", "retire_s")},
                 "offered_cell_updates_per_s": sum(c["nx"] * c["ny"] * args.served_steps for _, c, _, _ in reqs)
@@ -654,12 +712,57 @@ def run_served(args, rank, ws, lr, dist, emit=True):
         return line
 
 
-def run_shear(args, rank, ws, lr, dist):
+SHEAR = [2.0, 1.0, 0.5, 2.5, 0.01]  # rho_in, rho_out, u, p, noise
+
+
+def shear_case(capi, n, steps):
+    return capi.make_case(ndims=2, nx=n, ny=n, periodic=(1, 1, 1), recon=capi.RECON_LINEAR2_LIM, limiter=capi.LIM_BJ,
+                          solver=capi.RS_HLLC, cfl=0.4, max_iter=steps, max_time=1e30)
+
+
+def shear_cpu_rate(threads, steps=60, n=1024):
+    """The oracle port (all host threads) on the same shear layer, inputs built
+    by the oracle: (rate, seconds, sample)."""
+    from oracle import oracle as O
+    from turbostructred_gb300 import capi  # plain-Python case description only
+    case = shear_case(capi, n, 10**6)
+    full = O.embed(case, O.fill_scenario(case, O.SCENARIO_SHEAR_LAYER, 7, SHEAR, threads=threads))
+    full, _ = O.advance(case, full, 2, threads=threads)
+    t0 = time.perf_counter()
+    O.advance(case, full, steps, threads=threads)
+    secs = time.perf_counter() - t0
+    return n * n * steps / secs, secs, f"{steps} RK steps of the {n}^2 shear layer after 2 warm-up steps"
+
+
+def e2e_jobs(capi, solver, ic, steps, jobs=2):
+    """Median host time of jobs through the C ABI with host buffers: H2D of
+    the initial state from pinned memory, `steps` steps, D2H of the final
+    state (the first job is a warm-up)."""
+    import ctypes as C
+
+    import torch
+    host_in = torch.from_numpy(ic.reshape(-1)).pin_memory()
+    host_out = torch.empty(ic.size, dtype=torch.float64).pin_memory()
+    lib = capi.load()
+    P = C.POINTER(C.c_double)
+    times = []
+    for job in range(jobs + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        capi.check(lib.ts_set_state(solver.h, C.cast(host_in.data_ptr(), P), capi.LAYOUT_INTERIOR))
+        solver.set_info(iteration=0, time=0.0, dt=0.0)
+        solver.step(steps)
+        capi.check(lib.ts_get_state(solver.h, C.cast(host_out.data_ptr(), P), capi.LAYOUT_INTERIOR))
+        t1 = time.perf_counter()
+        if job > 0:
+            times.append(t1 - t0)
+    return statistics.median(times), ic.size * 8
+
+
+def run_shear(args, rank, ws, lr, dist, emit=True):
     """2D shear layer 1024^2, periodic, Linear2psLim(BJ) + HLLC, 1000 steps:
     the mixed path timed, the plain FP64 path beside it, and the mixed-vs-FP64
     error after the same 1000 steps."""
-    import numpy as np
-
     from turbostructred_gb300 import build, capi
     if rank == 0 or dist is None:
         build.build()
@@ -667,48 +770,69 @@ def run_shear(args, rank, ws, lr, dist):
         dist.barrier()
     capi.load()
     n = 1024
-    case = capi.make_case(ndims=2, nx=n, ny=n, periodic=(1, 1, 1), recon=capi.RECON_LINEAR2_LIM, limiter=capi.LIM_BJ,
-                          solver=capi.RS_HLLC, cfl=0.4, max_iter=args.shear_steps, max_time=1e30)
-    ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7 + rank, [2.0, 1.0, 0.5, 2.5, 0.01])
+    steps = args.steps or args.shear_steps
+    warmup = 5 if args.warmup is None else args.warmup
+    case = shear_case(capi, n, steps)
+    ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7 + rank, SHEAR)
     cells = n * n
     out = {}
     for prec, name in ((capi.PRECISION_MIXED, "mixed"), (capi.PRECISION_FP64, "fp64")):
         with capi.Solver(case, prec, device=lr) as s:
             s.set_state(ic)
-            s.step(args.warmup)
+            s.step(warmup)
             s.set_state(ic)
             s.set_info(iteration=0, time=0.0, dt=0.0)
             sampler = ClockSampler(gpu_uuid(lr)) if name == "mixed" else None
-            info, tm = s.step_timed(args.shear_steps)
+            info, tm = s.step_timed(steps)
             clocks = sampler.stop() if sampler else None
             out[name] = dict(state=s.get_state(), info=info, ms=tm["total_ms"], kernels=tm["kernels"], clocks=clocks,
                              launches=tm["launches"])
+            if name == "mixed" and not args.skip_e2e:
+                out["e2e"] = e2e_jobs(capi, s, ic, steps)
     t_ms = rank_max(out["mixed"]["ms"], dist)
-    value = replica_rate(cells * args.shear_steps, t_ms / 1e3, dist)
+    value = replica_rate(cells * steps, t_ms / 1e3, dist)
     kernels = out["mixed"]["kernels"]
     top = max(kernels, key=kernels.get)
     peak, peak_kind = measured_peak()
     achieved = BYTES_PER_CELL_UPDATE * cells / (kernels[top] / 1e3) / 1e9
     err = rel_errors(out["mixed"]["state"], out["fp64"]["state"])
+    e2e = None
+    if "e2e" in out:
+        tj, nbytes = out["e2e"]
+        e2e = {"value": replica_rate(cells * steps, tj, dist), "unit": "cell-updates/s",
+               "h2d_bytes_per_step": nbytes / steps, "d2h_bytes_per_step": nbytes / steps,
+               "job": f"H2D of the {n}^2 initial state from pinned host memory, {steps} steps, D2H of the final state",
+               "seconds_per_job": tj}
+    cpu = None
+    if rank == 0 and ws == 1 and not args.skip_cpu:
+        threads = os.cpu_count() or 1
+        rate, secs, sample = shear_cpu_rate(threads)
+        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port", "sample": sample,
+               "seconds": secs}
+    line = None
     if rank == 0:
-        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": args.shear_steps,
-                "warmup": args.warmup, "ms_per_step": t_ms / args.shear_steps, "higher_is_better": True,
-                "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 flux",
+        line = {"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": steps,
+                "warmup": warmup, "ms_per_step": t_ms / steps, "higher_is_better": True,
+                "scaling": "weak", "vs_baseline": None, "dtype": "f64 state / f32 flux", "precision": "mixed",
                 "data": "synthetic (seeded shear layer, no dataset)",
                 "config": {"workload": "2D ideal-gas shear layer 1024^2, periodic, Linear2psLim(BJ)+HLLC, "
-                                       f"{args.shear_steps} RK steps, CFL 0.4", "cells": cells,
+                                       f"{steps} RK steps, CFL 0.4", "cells": cells,
                            "l2": "state 84 MB per FP64 copy: below L2 (129 MB); the mixed step also moves "
                                  "the FP32 residual, 2 x 42 MB, so its working set spills"},
+                "e2e": e2e,
                 "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                              "frac": achieved / peak, "traffic": profile_traffic("shear2d", top, cells), "kernel": top,
-                             "kernel_ms": kernels[top],
+                             "kernel_ms": kernels[top], "algorithmic_bytes": BYTES_PER_CELL_UPDATE * cells,
                              "peak_source": peak_kind},
-                "fp64_value": cells * args.shear_steps / (out["fp64"]["ms"] / 1e3),
+                "cpu_baseline": cpu,
+                "fp64_value": cells * steps / (out["fp64"]["ms"] / 1e3),
                 "mixed_over_fp64": out["fp64"]["ms"] / t_ms,
-                "mixed_error_vs_fp64": dict(steps=args.shear_steps, **err),
+                "mixed_error_vs_fp64": dict(steps=steps, **err),
                 "clocks": out["mixed"]["clocks"], "gpu_launches": out["mixed"]["launches"],
                 "step_info": {k: out["mixed"]["info"][k] for k in ("iteration", "time", "dt", "health")}}
-        print(json.dumps(line), flush=True)
+        if emit:
+            print(json.dumps(line), flush=True)
+    return line
 
 
 def run_batch2d(args, rank, ws, lr, dist):
@@ -860,15 +984,15 @@ def main():
     p.add_argument("--fp64-steps", type=int, default=5)
     p.add_argument("--err-steps", type=int, default=50)
     p.add_argument("--e2e-jobs", type=int, default=2)
-    p.add_argument("--cpu-steps", type=int, default=24)
-    p.add_argument("--cpu-nz", type=int, default=128)
+    p.add_argument("--cpu-steps", type=int, default=10)
     p.add_argument("--skip-fp64", action="store_true")
     p.add_argument("--skip-e2e", action="store_true")
     p.add_argument("--skip-cpu", action="store_true")
     p.add_argument("--workload", choices=["blast3d", "tubes", "served", "shear2d", "batch2d", "rows"],
                    default="blast3d")
     p.add_argument("--shear-steps", type=int, default=1000)
-    p.add_argument("--skip-served", action="store_true")
+    p.add_argument("--skip-workloads", action="store_true",
+                   help="default line: leave out the shear-layer, tubes and served-stream measurements")
     p.add_argument("--served-sample-seconds", type=float, default=10.0)
     p.add_argument("--tubes", type=int, default=4096)
     p.add_argument("--tune-stages", type=int, default=8)

@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define TS_FVM_ABI_VERSION 3
+#define TS_FVM_ABI_VERSION 4
 
 typedef enum ts_status {
     TS_OK = 0,
@@ -143,7 +143,10 @@ typedef struct ts_config {
        also enters the spectral radius of every step, viscous or not
        (:1239-1248).  FP64 precision only (TS_ERR_UNSUPPORTED otherwise). */
     int32_t viscous;               /* IsViscousFlow */
-    int32_t reserved3;
+    /* Mixed precision only: also form the volume-weighted L1 residual norms
+       of every step (kernel.h:326) as FP64 sums of V |R| over the FP32
+       residual.  The FP64 path always forms them. */
+    int32_t residual_norms;
     double viscosity;              /* Viscosity */
 } ts_config;
 
@@ -155,8 +158,9 @@ typedef struct ts_step_info {
     double dt;
     double next_solution_time;
     double next_slice_time;
-    double residual[5];  /* volume-weighted L1 residual norms (kernel.h:326); the FP64
-                            path forms them every step, the mixed path reports zeros */
+    double residual[5];  /* volume-weighted L1 residual norms sum V |R| of the last step
+                            (kernel.h:326); the FP64 path forms them every step, the
+                            mixed path when ts_config.residual_norms is set (else zeros) */
 } ts_step_info;
 
 typedef struct ts_handle ts_handle;
@@ -431,16 +435,27 @@ ts_status ts_server_stats_get(ts_server* s, ts_server_stats* out);
      cfg       problem set-up; precision must be TS_PRECISION_MIXED.
      state_in  device pointer, TS_LAYOUT_INTERIOR doubles (caller-owned).
      state_out device pointer, same layout (may equal state_in).
-     stream    a cudaStream_t, or NULL for the legacy default stream.
+     stream    a cudaStream_t, or NULL for the legacy default stream.  Every
+               upload, clear and kernel of the call is queued on it, so the
+               call is ordered after work already queued there.
      info      optional; its time, iteration and snapshot times are the
-               starting point and it receives the step info at the end.
+               starting point and it receives the step info at the end.  A
+               fresh run (info NULL, or iteration 0 at time 0, e.g. a
+               zero-filled struct) starts the snapshot schedule at
+               cfg->save_solution_time / save_slice_time as ts_create does;
+               otherwise next_solution_time / next_slice_time are taken
+               from info, so a continued run passes back what it received.
+               residual[] receives the norms when cfg->residual_norms is set
+               (formed in FP64 from the FP32 residual), else zeros.
    Every call works in one file-scope scratch array of TS_NOALLOC_MAX_PLANE
    elements per variable plane (about 38 MB, resident on every GPU that has
    loaded this library, until the process exits): grids whose padded planes
    exceed it are rejected with TS_ERR_INVALID.  The first call on a device
    looks up that array's device address, so make it before any stream
-   capture.  All calls share the array and leave their data in it; calls that
-   overlap on the GPU (other streams, other host threads) race on it. */
+   capture.  Each call waits on the host for its own work on `stream` to
+   finish before it returns (it reads the step count and time back).  All
+   calls share the array and leave their data in it; calls that overlap on
+   the GPU (other streams, other host threads) race on it. */
 #define TS_NOALLOC_MAX_PLANE 262144
 ts_status ts_advance_noalloc(const ts_config* cfg, const double* state_in, double* state_out, int32_t n_steps,
                              void* stream, ts_step_info* info);

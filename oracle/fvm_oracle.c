@@ -1261,3 +1261,80 @@ int orc_exact_riemann(double g, double pinf, double rl, double ul, double pl, do
     }
     return it;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Synthetic initial states of the benchmark scenarios                      */
+/* ------------------------------------------------------------------------ */
+/* The benchmark inputs are this project's own seeded scenarios (the reference
+   has no benchmark inputs).  Restated here so the CPU legs of the bench build
+   their inputs without the product library; tests/test_capi_host.py checks
+   this restatement bit for bit against ts_fill_scenario.  The scenarios are
+   point-sampled at the cell centres, as Kernel::SetInitialConditions does
+   (kernel.h:125-146), with a counter-based hash of (seed, i, j, k). */
+
+double orc_hash_uniform(unsigned long long seed, long long i, long long j, long long k) {
+    unsigned long long z = seed * 0x9E3779B97F4A7C15ULL + (unsigned long long)i * 0xBF58476D1CE4E5B9ULL +
+                           (unsigned long long)j * 0x94D049BB133111EBULL + (unsigned long long)k * 0xD6E8FEB86659FD39ULL;
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ULL;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBULL;
+    z ^= z >> 31;
+    return (double)(z >> 11) * 0x1.0p-53;
+}
+
+int orc_fill_scenario(const orc_config* c, int scenario, unsigned long long seed, const double* prm, int n_params,
+                      double* values) {
+    static const int need[4] = {7, 5, 5, 16};
+    if (scenario < 0 || scenario > 3 || n_params < need[scenario]) return 1;
+    int nxa, nya, nza;
+    orc_dims(c, &nxa, &nya, &nza);
+    double* x = (double*)malloc(sizeof(double) * (size_t)nxa);
+    double* hx = (double*)malloc(sizeof(double) * (size_t)nxa);
+    double* y = (double*)malloc(sizeof(double) * (size_t)nya);
+    double* hy = (double*)malloc(sizeof(double) * (size_t)nya);
+    double* z = (double*)malloc(sizeof(double) * (size_t)nza);
+    double* hz = (double*)malloc(sizeof(double) * (size_t)nza);
+    if (!x || !hx || !y || !hy || !z || !hz) return 2;
+    orc_grid(c, x, hx, y, hy, z, hz);
+    const int nd = c->ndims;
+    const int nx = c->nx, ny = nd > 1 ? c->ny : 1, nz = nd > 2 ? c->nz : 1;
+    const double gm1 = c->gamma - 1.0;
+    const double pshift = c->eos == ORC_EOS_STIFFENED ? c->gamma * c->p_inf : 0.0;
+#pragma omp parallel for schedule(static) if (c->threads != 1)
+    for (int k = 0; k < nz; ++k)
+        for (int j = 0; j < ny; ++j)
+            for (int i = 0; i < nx; ++i) {
+                double* o = values + 5 * (((size_t)k * ny + j) * nx + i);
+                const double xc = x[i + 1];
+                const double yc = nd > 1 ? y[j + 1] : 0.0;
+                const double zc = nd > 2 ? z[k + 1] : 0.0;
+                double rho = 1.0, u = 0.0, v = 0.0, w = 0.0, p = 1.0;
+                if (scenario == 0) {          /* shock tube: x0, rhoL, uL, pL, rhoR, uR, pR */
+                    if (xc > prm[0]) { rho = prm[4]; u = prm[5]; p = prm[6]; }
+                    else { rho = prm[1]; u = prm[2]; p = prm[3]; }
+                } else if (scenario == 1) {   /* shear layer: rho_in, rho_out, u, p, noise */
+                    const int inner = fabs(yc - 0.5 * c->length[1]) < 0.25 * c->length[1];
+                    rho = inner ? prm[0] : prm[1];
+                    u = inner ? prm[2] : -prm[2];
+                    p = prm[3];
+                    v = prm[4] * (2.0 * orc_hash_uniform(seed, i, j, k) - 1.0);
+                } else if (scenario == 2) {   /* blast: rho, p_out, p_in, radius, noise */
+                    const double dx = xc - 0.5 * c->length[0];
+                    const double dy = nd > 1 ? yc - 0.5 * c->length[1] : 0.0;
+                    const double dz = nd > 2 ? zc - 0.5 * c->length[2] : 0.0;
+                    rho = prm[0] * (1.0 + prm[4] * (2.0 * orc_hash_uniform(seed, i, j, k) - 1.0));
+                    p = (dx * dx + dy * dy + dz * dz < prm[3] * prm[3]) ? prm[2] : prm[1];
+                } else {                      /* quadrants: 4 x (rho, u, v, p) for ++, -+, --, +- */
+                    const int right = xc > 0.5 * c->length[0];
+                    const int top = nd > 1 ? yc > 0.5 * c->length[1] : 1;
+                    const int q = top ? (right ? 0 : 1) : (right ? 3 : 2);
+                    rho = prm[4 * q + 0]; u = prm[4 * q + 1]; v = prm[4 * q + 2]; p = prm[4 * q + 3];
+                }
+                o[0] = rho;
+                o[1] = rho * u;
+                o[2] = rho * v;
+                o[3] = rho * w;
+                o[4] = (p + pshift) / gm1 + 0.5 * rho * (u * u + v * v + w * w);
+            }
+    free(x); free(hx); free(y); free(hy); free(z); free(hz);
+    return 0;
+}

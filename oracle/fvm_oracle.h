@@ -95,6 +95,14 @@ int orc_exact_riemann(double gamma, double p_inf, double rl, double ul, double p
    Godunov flux's inner solve); returns 1 when converged. */
 int orc_godunov_pstar(double gamma, double rl, double ul, double pl, double rr, double ur, double pr, double* ps);
 
+/* The benchmark scenarios' initial states (interior cells, x fastest, 5
+   doubles per cell) and their hash RNG: uniform double in [0,1) of
+   (seed, i, j, k).  Scenario 0 shock tube, 1 shear layer, 2 blast,
+   3 quadrants; parameters as ts_fill_scenario.  Returns 0 on success. */
+double orc_hash_uniform(unsigned long long seed, long long i, long long j, long long k);
+int orc_fill_scenario(const orc_config* c, int scenario, unsigned long long seed, const double* params, int n_params,
+                      double* values);
+
 #ifdef __cplusplus
 }
 #endif

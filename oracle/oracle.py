@@ -96,6 +96,11 @@ def lib():
         L.orc_grid.argtypes = [C.POINTER(OrcConfig)] + [C.POINTER(C.c_double)] * 6
         L.orc_exact_riemann.argtypes = [C.c_double] * 9 + [C.POINTER(C.c_double)] * 3
         L.orc_exact_riemann.restype = C.c_int
+        L.orc_fill_scenario.argtypes = [C.POINTER(OrcConfig), C.c_int, C.c_ulonglong, C.POINTER(C.c_double), C.c_int,
+                                        C.POINTER(C.c_double)]
+        L.orc_fill_scenario.restype = C.c_int
+        L.orc_hash_uniform.argtypes = [C.c_ulonglong, C.c_longlong, C.c_longlong, C.c_longlong]
+        L.orc_hash_uniform.restype = C.c_double
         _lib = L
     return _lib
 
@@ -189,6 +194,25 @@ def advance(case: dict, full: np.ndarray, n_steps: int = -1, info: dict | None =
     out = dict(iteration=si.iteration, time=si.time, dt=si.dt, next_solution_time=si.next_solution_time,
                next_slice_time=si.next_slice_time, residual=list(si.residual))
     return vals, out
+
+
+SCENARIO_SHOCK_TUBE, SCENARIO_SHEAR_LAYER, SCENARIO_BLAST, SCENARIO_QUADRANTS = 0, 1, 2, 3
+
+
+def fill_scenario(case: dict, scenario: int, seed: int, params, threads: int = 0) -> np.ndarray:
+    """The seeded initial state of a benchmark scenario, interior cells as
+    (nz, ny, nx, 5): the same values the product's ts_fill_scenario writes."""
+    nx = case["nx"]
+    ny = case["ny"] if case["ndims"] > 1 else 1
+    nz = case["nz"] if case["ndims"] > 2 else 1
+    out = np.empty((nz, ny, nx, 5))
+    p = np.ascontiguousarray(params, dtype=np.float64)
+    cfg = to_struct(case, threads)
+    rc = lib().orc_fill_scenario(C.byref(cfg), scenario, seed, p.ctypes.data_as(C.POINTER(C.c_double)), len(p),
+                                 out.ctypes.data_as(C.POINTER(C.c_double)))
+    if rc != 0:
+        raise RuntimeError(f"orc_fill_scenario failed rc={rc}")
+    return out
 
 
 def exact_riemann(gamma, p_inf, left, right, s):

@@ -103,3 +103,23 @@ def test_state_sizes(tslib):
     cfg, keep = capi.to_config(capi.make_case(ndims=3, nx=4, ny=5, nz=6))
     assert tslib.ts_state_doubles(C.byref(cfg), 0) == 4 * 5 * 6 * 5
     assert tslib.ts_state_doubles(C.byref(cfg), 1) == 6 * 7 * 8 * 5
+
+
+@pytest.mark.parametrize("nd,scenario,params", [
+    (3, 2, [1.0, 0.1, 10.0, 0.1, 0.01]),
+    (2, 1, [2.0, 1.0, 0.5, 2.5, 0.01]),
+    (1, 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]),
+    (2, 3, [1.5, 0.0, 0.0, 1.5, 0.53, 1.2, 0.0, 0.3, 0.14, 1.2, 1.2, 0.03, 0.53, 0.0, 1.2, 0.3]),
+])
+def test_oracle_scenarios_equal_the_library_scenarios(nd, scenario, params, tslib, oracle_mod):
+    """The CPU legs of the bench build their inputs with the oracle's
+    restatement of the scenarios; it must give the product's bytes."""
+    from turbostructred_gb300 import capi
+    stiff = scenario == 0
+    case = capi.make_case(ndims=nd, nx=41, ny=27, nz=19, gamma=4.4 if stiff else 1.4,
+                          eos=capi.EOS_STIFFENED if stiff else capi.EOS_IDEAL, p_inf=6.0 if stiff else 0.0,
+                          blocks={0: [(0.0, 1.03, 41)]})
+    a = capi.fill_scenario(case, scenario, 2024, params)
+    b = oracle_mod.fill_scenario(case, scenario, 2024, params)
+    assert a.shape == b.shape
+    assert np.array_equal(a, b)

@@ -170,3 +170,57 @@ def test_mixed_c3_full_size_matches_fp64(tslib):
     assert abs(res[1][1]["time"] - res[0][1]["time"]) <= 1e-5 * res[0][1]["time"]
     m0 = ic[..., 0].sum()
     assert abs(res[1][0][..., 0].sum() - m0) <= 1e-9 * m0
+
+
+def test_mixed_c2_full_size_matches_fp64(tslib):
+    """C2 at full size: the 1024^2 periodic shear layer (Linear2psLim BJ +
+    HLLC), mixed vs the plain FP64 path after 200 steps: density L1 <= 1e-5,
+    momentum and energy L1 <= 1e-4, the same time, and exact conservation of
+    mass on the periodic domain to FP64 rounding."""
+    from turbostructred_gb300 import capi
+    case = capi.make_case(ndims=2, nx=1024, ny=1024, periodic=(1, 1, 1), recon=3, limiter=0, solver=3, cfl=0.4,
+                          max_iter=10**6, max_time=1e30)
+    ic = capi.fill_scenario(case, capi.SCENARIO_SHEAR_LAYER, 7, [2.0, 1.0, 0.5, 2.5, 0.01])
+    res = {}
+    for prec in (0, 1):
+        with capi.Solver(case, precision=prec) as s:
+            s.set_state(ic)
+            info = s.step(200)
+            res[prec] = (s.get_state(), info)
+    e = errors(res[1][0], res[0][0])
+    assert e["rho"] <= RHO_L1, e
+    assert e["mom"] <= MOM_E_L1 and e["E"] <= MOM_E_L1, e
+    assert abs(res[1][1]["time"] - res[0][1]["time"]) <= 1e-5 * res[0][1]["time"]
+    assert res[1][1]["health"] == 0
+    m0 = ic[..., 0].sum()
+    assert abs(res[1][0][..., 0].sum() - m0) <= 1e-10 * m0
+
+
+@pytest.mark.parametrize("nd", [1, 2, 3])
+def test_mixed_residual_norms_match_fp64(nd, tslib):
+    """With residual_norms set, the mixed path forms the reference's residual
+    norms sum V |R| per variable (kernel.h:326) in FP64 from its FP32
+    residual; they agree with the FP64 path's norms of the same step to the
+    FP32 residual's accuracy (relative 1e-4).  Without the flag they are 0."""
+    from oracle import oracle as O
+    from turbostructred_gb300 import capi
+    if nd == 3:
+        case = O.make_case(ndims=3, nx=48, ny=40, nz=36, periodic=(0, 0, 1), recon=3, solver=1, cfl=0.4,
+                           bc=[SYM] * 6)
+        scen, params = 2, [1.0, 0.1, 10.0, 0.2, 0.01]
+    elif nd == 2:
+        case = O.make_case(ndims=2, nx=200, ny=160, periodic=(1, 1, 1), recon=3, solver=3, cfl=0.4)
+        scen, params = 1, [2.0, 1.0, 0.5, 2.5, 0.01]
+    else:
+        case = O.make_case(ndims=1, nx=1500, periodic=(0, 1, 1), recon=3, cfl=0.5, bc=[NAT] * 6)
+        scen, params = 0, [0.5, 1.0, 0.0, 1.0, 0.125, 0.0, 0.1]
+    full = _full(case, scen, 11, params)
+    norms = {}
+    for prec, flag in ((0, False), (1, True), (1, False)):
+        with capi.Solver(capi.make_case(**dict(case, residual_norms=flag)), precision=prec) as s:
+            s.set_state(full, capi.LAYOUT_WITH_GHOSTS)
+            norms[(prec, flag)] = [np.array(s.step(1)["residual"]), np.array(s.step(6)["residual"])]
+    for ref, got in zip(norms[(0, False)], norms[(1, True)]):
+        live = ref > 1e-12 * ref.max()
+        assert np.all(np.abs(got[live] - ref[live]) <= 1e-4 * ref[live]), (got, ref)
+    assert all(np.all(x == 0.0) for x in norms[(1, False)])

@@ -18,7 +18,7 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libtsfvm.so")
 
-ABI_VERSION = 3
+ABI_VERSION = 4
 
 # enum values (include/ts_fvm.h)
 RECON_PWC, RECON_LINEAR2, RECON_ENO2, RECON_LINEAR2_LIM = 0, 1, 2, 3
@@ -63,7 +63,7 @@ class Config(C.Structure):
         ("bc", BcConfig * 6), ("precision", C.c_int32), ("device", C.c_int32),
         ("external_force", C.c_int32), ("uniform_acceleration", C.c_int32),
         ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
-        ("viscous", C.c_int32), ("reserved3", C.c_int32), ("viscosity", C.c_double),
+        ("viscous", C.c_int32), ("residual_norms", C.c_int32), ("viscosity", C.c_double),
     ]
 
 
@@ -224,7 +224,8 @@ def make_case(**kw) -> dict:
                 gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
                 save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
-                external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0)
+                external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0,
+                residual_norms=False)
     case.update(kw)
     return case
 
@@ -267,6 +268,7 @@ def to_config(case: dict, precision: int = PRECISION_FP64, device: int = 0):
             getattr(c, vec)[a] = v[a] if v is not None else 0.0
     c.viscous = int(bool(case.get("viscous", False)))
     c.viscosity = float(case.get("viscosity", 0.0))
+    c.residual_norms = int(bool(case.get("residual_norms", False)))
     return c, keep
 
 

@@ -255,8 +255,10 @@ struct ts_batch {
         std::memset(nh, 0, sizeof(Ctl) * cap);
         TB_CUDA(cudaStreamSynchronize(stream));
         if (capacity) {
-            TB_CUDA(cudaMemcpy(nc, d_ctl, sizeof(Ctl) * capacity, cudaMemcpyDeviceToDevice));
+            TB_CUDA(cudaMemcpyAsync(nc, d_ctl, sizeof(Ctl) * capacity, cudaMemcpyDeviceToDevice, stream));
             std::memcpy(nh, h_ctl, sizeof(Ctl) * capacity);
+            // the old control words are freed below: the copy out of them first
+            TB_CUDA(cudaStreamSynchronize(stream));
         }
         cudaFree(d_desc);
         cudaFree(d_ctl);
@@ -272,7 +274,7 @@ struct ts_batch {
             if (!slots[s].used) continue;
             desc[s].ctl = d_ctl + s;
         }
-        TB_CUDA(cudaMemcpy(d_desc, desc.data(), sizeof(ProbDesc) * cap, cudaMemcpyHostToDevice));
+        TB_CUDA(cudaMemcpyAsync(d_desc, desc.data(), sizeof(ProbDesc) * cap, cudaMemcpyHostToDevice, stream));
         dirty = true;
         return TS_OK;
     }
@@ -368,7 +370,8 @@ struct ts_batch {
             if (!slots[s].used || h_ctl[s].stop_req) continue;
             const ProbDesc& d = desc[s];
             const int items = (d.kn[0] + cells - 1) / cells;
-            if (d.L.nd != 1 || items > kTailMaxCluster) return TS_OK;
+            // the tail kernel forms no residual norms
+            if (d.L.nd != 1 || items > kTailMaxCluster || d.mp.norms) return TS_OK;
             cmax = std::max(cmax, items);
             lists[d.mp.solver == TS_RS_HLLC ? 1 : 0].push_back(s);
             ++nact;
@@ -605,7 +608,7 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
     auto undo = [&]() { for (void* p : sl.mem) b->arena.give(p); sl = Slot(); };
     ProbDesc& d = b->desc[slot];
     std::memset(&d, 0, sizeof d);
-    if ((s = mixed_problem(*cfg, L, ph, grid, b->d_ctl + slot, take, d, err)) != TS_OK) {
+    if ((s = mixed_problem(*cfg, L, ph, grid, b->d_ctl + slot, take, d, err, b->ustream)) != TS_OK) {
         undo();
         return err.empty() ? s : fail(s, err);
     }
@@ -758,7 +761,7 @@ ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* in
         info->dt = c.dt;
         info->next_solution_time = c.next_sol;
         info->next_slice_time = c.next_slice;
-        for (int v = 0; v < NV; ++v) info->residual[v] = 0.0;
+        for (int v = 0; v < NV; ++v) info->residual[v] = c.res[v];  // zeros unless residual_norms
     }
     return TS_OK;
 }

@@ -134,8 +134,9 @@ struct ts_handle {
         if (s != TS_OK) return s;
         s = alloc(&dh, h.size());
         if (s != TS_OK) return s;
-        TS_CUDA(cudaMemcpy(dx, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice));
-        TS_CUDA(cudaMemcpy(dh, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice));
+        // on the handle's stream (pageable sources are staged before return)
+        TS_CUDA(cudaMemcpyAsync(dx, x.data(), x.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
+        TS_CUDA(cudaMemcpyAsync(dh, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, stream));
         *cx = dx;
         *chh = dh;
         return TS_OK;
@@ -148,7 +149,7 @@ struct ts_handle {
         ts_status s;
         pb.L = L;
         if ((s = alloc(&pb.U, NV * L.plane)) != TS_OK) return s;
-        TS_CUDA(cudaMemset(pb.U, 0, NV * L.plane * sizeof(double)));
+        TS_CUDA(cudaMemsetAsync(pb.U, 0, NV * L.plane * sizeof(double), stream));
         if (linear && (s = alloc(&pb.G, (size_t)nd * NV * L.plane)) != TS_OK) return s;
         if (limited && (s = alloc(&pb.Lim, NV * L.plane)) != TS_OK) return s;
         for (int a = 0; a < nd; ++a) {
@@ -178,13 +179,13 @@ struct ts_handle {
                     }
             double* d;
             if ((s = alloc(&d, L.plane)) != TS_OK) return s;
-            TS_CUDA(cudaMemcpy(d, e.data(), L.plane * sizeof(double), cudaMemcpyHostToDevice));
+            TS_CUDA(cudaMemcpyAsync(d, e.data(), L.plane * sizeof(double), cudaMemcpyHostToDevice, stream));
             pb.eps2 = d;
         }
         if ((s = alloc(&pb.partial, (size_t)plain_partial_blocks(L))) != TS_OK) return s;
         if (cfg.viscous) {
             if ((s = alloc(&pb.VG, (size_t)9 * L.plane)) != TS_OK) return s;
-            TS_CUDA(cudaMemset(pb.VG, 0, (size_t)9 * L.plane * sizeof(double)));
+            TS_CUDA(cudaMemsetAsync(pb.VG, 0, (size_t)9 * L.plane * sizeof(double), stream));
         }
         if (cfg.viscosity != 0.0)
             for (int a = 0; a < nd; ++a)
@@ -310,7 +311,7 @@ ts_status ts_create(const ts_config* cfg, ts_handle** out) {
     if (cfg->precision == TS_PRECISION_MIXED) {
         s = mixed_init(h->cfg, h->L, h->ph, h->grid, h->ctl_d,
                        [&](size_t bytes, void** p) { return h->alloc(reinterpret_cast<char**>(p), bytes); },
-                       h->mb, err);
+                       h->mb, err, h->stream);
         if (s != TS_OK) return fail(s, err.empty() ? std::string(ts_last_error()) : err);
     } else {
         if ((s = h->init_plain()) != TS_OK) return s;
@@ -504,7 +505,7 @@ ts_status ts_set_tile(ts_handle* h, int32_t tx, int32_t ty, int32_t z_chunks) {
     DeviceGuard g(h->device);
     TS_CUDA(cudaStreamSynchronize(h->stream));
     std::string err;
-    ts_status s = mixed_set_tile(h->mb, tx, ty, z_chunks, err);
+    ts_status s = mixed_set_tile(h->mb, tx, ty, z_chunks, err, h->stream);
     if (s != TS_OK) return fail(s, err);
     for (auto& kv : h->graphs) cudaGraphExecDestroy(kv.second);  // launch shape changed
     h->graphs.clear();

@@ -86,6 +86,7 @@ struct Ctl {
     double dt_apply;           // dt of the residual still waiting to be applied
     int parity;                // which of the two state/residual buffers is current
     unsigned int srmax_bits;   // running max of SR/V as FP32 bits (positive floats order as uints)
+    double res_acc[5];         // residual norms of the stage in flight (moved to res when it closes)
 };
 
 // Host copy of the grid in the reference's layout (one ghost per active

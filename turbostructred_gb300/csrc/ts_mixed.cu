@@ -56,6 +56,7 @@
 #include <string>
 #include <vector>
 
+#include "ts_flux32.cuh"
 #include "ts_mixed.h"
 
 namespace ts {
@@ -63,180 +64,7 @@ namespace {
 
 constexpr int HB = 2;  // halo of the working-state box
 
-// ---------------------------------------------------------------------------
-// FP64 <-> FP32 on the integer pipe
-// ---------------------------------------------------------------------------
-// Truncating FP64 -> FP32 for finite values with |x| < 2^128; |x| < 2^-126
-// gives a signed zero.  Four integer operations instead of a conversion on
-// the FP64 pipe.
-__device__ __forceinline__ float f64_to_f32(double d) {
-    const unsigned int hi = (unsigned int)__double2hiint(d);
-    const unsigned int lo = (unsigned int)__double2loint(d);
-    const unsigned int sign = hi & 0x80000000u;
-    const unsigned int t = __funnelshift_l(lo, hi - 0x38000000u, 3);
-    const unsigned int e = (hi >> 20) & 0x7FFu;
-    return __uint_as_float(e < 897u ? sign : ((t & 0x7FFFFFFFu) | sign));
-}
-
-// Exact FP32 -> FP64 for normal numbers and zeros (FP32 runs flush-to-zero).
-__device__ __forceinline__ double f32_to_f64(float f) {
-    const unsigned int b = __float_as_uint(f);
-    const unsigned int a = b & 0x7FFFFFFFu;
-    const unsigned int hi = (a ? (a >> 3) + 0x38000000u : 0u) | (b & 0x80000000u);
-    return __hiloint2double((int)hi, (int)(b << 29));
-}
-
-__device__ __forceinline__ void resolve(int idx, int n, int periodic, int side_lo, int& src, int& side) {
-    side = -1;
-    src = idx;
-    if (idx < 0) {
-        if (periodic) src = idx + n;
-        else { src = -1 - idx; side = side_lo; }
-    } else if (idx >= n) {
-        if (periodic) src = idx - n;
-        else { src = 2 * n - 1 - idx; side = side_lo + 1; }
-    }
-}
-
-// Boundary-condition image of a state (shifted energy) across `side`.
-__device__ __forceinline__ void bc32(const MixPhys& p, int side, int A, float w[NV]) {
-    const int t = p.bc_type[side];
-    if (t == TS_BC_SYMMETRY) {
-        w[1 + A] = -w[1 + A];
-    } else if (t == TS_BC_WALL) {
-        w[1] = -w[1]; w[2] = -w[2]; w[3] = -w[3];
-    } else if (t == TS_BC_MOVING_WALL) {
-        const float r = w[0], ir = 1.0f / r;
-        const float vx = w[1] * ir, vy = w[2] * ir, vz = w[3] * ir;
-        const float dx = 2.0f * p.bc_vel[side][0] - vx, dy = 2.0f * p.bc_vel[side][1] - vy,
-                    dz = 2.0f * p.bc_vel[side][2] - vz;
-        w[1] = r * dx; w[2] = r * dy; w[3] = r * dz;
-        w[4] = w[4] + 0.5f * r * ((dx * dx + dy * dy + dz * dz) - (vx * vx + vy * vy + vz * vz));
-    } else if (t == TS_BC_SUBSONIC_INLET) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) w[v] = p.bc_state[side][v];
-    }
-}
-
-
-__device__ __forceinline__ float harten32(float z, float e) {
-    z = fabsf(z);
-    return (z < e) ? ((z * z) / e + e) * 0.5f : z;
-}
-
-__device__ __forceinline__ float pick3(int a, float x, float y, float z) { return a == 0 ? x : (a == 1 ? y : z); }
-
-// ---------------------------------------------------------------------------
-// FP32 Riemann solvers along axis A (a compile-time argument: the normal
-// components fold into register choices).  States carry the shifted energy
-// E' = E - einf, so p = (g-1)(E' - rho |u|^2 / 2) for both equations of state
-// without cancellation; E = E' + einf where the total energy enters.
-// ---------------------------------------------------------------------------
-
-// Roe-Pike flux (RoeSolverPerfectGasEOS.h:74-160) in the equivalent form
-// 1/2 [F(UL) + F(UR) + |A|(UL - UR)], returned without the factor 1/2
-// (flux_scale<SOLVER>), |A| dU = a1 dU + Ac Qa + Bc Qb with
-// Qa = (0, e_A, un), Qb = (1, u, H), Ac = Ea dR + Eb dD, Bc = Ea dD + Eb dR / c^2.
-template <int A>
-__device__ __forceinline__ float roe32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
-    const float gm1 = p.gm1;
-    const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
-    const float ulx = UL[1] * rl, uly = UL[2] * rl, ulz = UL[3] * rl;
-    const float urx = UR[1] * rr, ury = UR[2] * rr, urz = UR[3] * rr;
-    const float pl = gm1 * (UL[4] - 0.5f * UL[0] * (ulx * ulx + uly * uly + ulz * ulz));
-    const float pr = gm1 * (UR[4] - 0.5f * UR[0] * (urx * urx + ury * ury + urz * urz));
-    const float el = UL[4] + p.einf + pl, er = UR[4] + p.einf + pr;  // E + p
-    const float sl = UL[0] * rsqrtf(UL[0]), sr = UR[0] * rsqrtf(UR[0]);
-    const float inv = 1.0f / (sl + sr);
-    const float ql = sl * inv, qr = sr * inv;
-    const float ux = ql * ulx + qr * urx, uy = ql * uly + qr * ury, uz = ql * ulz + qr * urz;
-    const float h = ql * (el * rl) + qr * (er * rr);
-    const float q2 = ux * ux + uy * uy + uz * uz;
-    const float c2 = gm1 * (h - 0.5f * q2);
-    const float ic = rsqrtf(c2);
-    const float c = c2 * ic;
-    const float un = pick3(A, ux, uy, uz);
-    const float lam = fabsf(un) + c;
-    float a1 = fabsf(un), a3 = fabsf(un + c), a4 = fabsf(un - c);
-    if (p.eps > 0.0f) {
-        const float he = p.eps * lam;
-        a1 = harten32(un, he); a3 = harten32(un + c, he); a4 = harten32(un - c, he);
-    }
-    const float Ea = (a3 - a4) * 0.5f * ic;
-    const float Eb = (a3 + a4) * 0.5f - a1;
-    const float dr = UL[0] - UR[0], dmx = UL[1] - UR[1], dmy = UL[2] - UR[2], dmz = UL[3] - UR[3];
-    const float de = UL[4] - UR[4];
-    const float dR = 0.5f * gm1 * q2 * dr - gm1 * (ux * dmx + uy * dmy + uz * dmz - de);
-    const float dD = pick3(A, dmx, dmy, dmz) - dr * un;
-    const float Ac = Ea * dR + Eb * dD;
-    const float Bc = Ea * dD + Eb * dR * (ic * ic);
-    const float unl = pick3(A, ulx, uly, ulz), unr = pick3(A, urx, ury, urz);
-    const float pn = pl + pr + Ac;
-    // twice the flux: the factor 1/2 is applied with the face areas
-    F[0] = UL[0] * unl + UR[0] * unr + a1 * dr + Bc;
-    F[1] = UL[1] * unl + UR[1] * unr + (A == 0 ? pn : 0.0f) + a1 * dmx + Bc * ux;
-    F[2] = UL[2] * unl + UR[2] * unr + (A == 1 ? pn : 0.0f) + a1 * dmy + Bc * uy;
-    F[3] = UL[3] * unl + UR[3] * unr + (A == 2 ? pn : 0.0f) + a1 * dmz + Bc * uz;
-    F[4] = el * unl + er * unr + a1 * de + Ac * un + Bc * h;
-    return lam;
-}
-
-// HLLC (Toro ch. 10.4), Einfeldt-type speeds from Roe averages.
-template <int A>
-__device__ __forceinline__ float hllc32(const MixPhys& p, const float UL[NV], const float UR[NV],
-                                        float F[NV]) {
-    const float g = p.gamma, gm1 = p.gm1;
-    const float rl = 1.0f / UL[0], rr = 1.0f / UR[0];
-    const float vlx = UL[1] * rl, vly = UL[2] * rl, vlz = UL[3] * rl;
-    const float vrx = UR[1] * rr, vry = UR[2] * rr, vrz = UR[3] * rr;
-    const float pl = gm1 * (UL[4] - 0.5f * UL[0] * (vlx * vlx + vly * vly + vlz * vlz));
-    const float pr = gm1 * (UR[4] - 0.5f * UR[0] * (vrx * vrx + vry * vry + vrz * vrz));
-    const float El = UL[4] + p.einf, Er = UR[4] + p.einf;
-    const float cl = sqrtf(g * (pl + p.pinf) * rl), cr = sqrtf(g * (pr + p.pinf) * rr);
-    const float sl = UL[0] * rsqrtf(UL[0]), sr = UR[0] * rsqrtf(UR[0]);
-    const float inv = 1.0f / (sl + sr);
-    const float wl = sl * inv, wr = sr * inv;
-    const float ul = pick3(A, vlx, vly, vlz), ur = pick3(A, vrx, vry, vrz);
-    const float ut = wl * ul + wr * ur;
-    const float vtx = wl * vlx + wr * vrx, vty = wl * vly + wr * vry, vtz = wl * vlz + wr * vrz;
-    const float ht = wl * ((El + pl) * rl) + wr * ((Er + pr) * rr);
-    const float ct = sqrtf(gm1 * (ht - 0.5f * (vtx * vtx + vty * vty + vtz * vtz)));
-    const float SL = fminf(ul - cl, ut - ct);
-    const float SR = fmaxf(ur + cr, ut + ct);
-    const float ml = UL[0] * (SL - ul), mr = UR[0] * (SR - ur);
-    const float ss = (pr - pl + ul * ml - ur * mr) / (ml - mr);
-    // F_L if 0 <= S_L, F_R if S_R <= 0, else the star state on the side of S*
-    const bool supl = SL >= 0.0f, supr = SR <= 0.0f;
-    const bool left = supl || (!supr && ss >= 0.0f);
-    const float* U = left ? UL : UR;
-    const float vx = left ? vlx : vrx, vy = left ? vly : vry, vz = left ? vlz : vrz;
-    const float uk = left ? ul : ur, pk = left ? pl : pr, Ek = left ? El : Er, rk = left ? rl : rr;
-    const float Sk = left ? SL : SR, mk = left ? ml : mr;
-    F[0] = U[0] * uk;
-    F[1] = U[1] * uk + (A == 0 ? pk : 0.0f);
-    F[2] = U[2] * uk + (A == 1 ? pk : 0.0f);
-    F[3] = U[3] * uk + (A == 2 ? pk : 0.0f);
-    F[4] = (Ek + pk) * uk;
-    if (!supl && !supr) {
-        const float coef = mk / (Sk - ss);
-        F[0] += Sk * (coef - U[0]);
-        F[1] += Sk * (coef * (A == 0 ? ss : vx) - U[1]);
-        F[2] += Sk * (coef * (A == 1 ? ss : vy) - U[2]);
-        F[3] += Sk * (coef * (A == 2 ? ss : vz) - U[3]);
-        F[4] += Sk * (coef * (Ek * rk + (ss - uk) * (ss + pk / mk)) - Ek);
-    }
-    return fmaxf(fabsf(SL), fabsf(SR));
-}
-
-// Factor between the stored face flux and the flux.
-template <int SOLVER>
-__device__ __forceinline__ constexpr float flux_scale() { return SOLVER == TS_RS_HLLC ? 1.0f : 0.5f; }
-
-template <int SOLVER, int A>
-__device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], const float UR[NV], float F[NV]) {
-    if (SOLVER == TS_RS_HLLC) return hllc32<A>(p, UL, UR, F);
-    return roe32<A>(p, UL, UR, F);
-}
+using namespace mix32;
 
 // ---------------------------------------------------------------------------
 // Compile-time tile geometry and shared-memory layout (floats)
@@ -835,15 +663,36 @@ __device__ __forceinline__ bool residual_of(const ProbDesc& d, const float* sm, 
 template <class T, int SOLVER>
 __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
                                          int z, const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
-                                         float& srmax) {
+                                         float& srmax, float (&nrm)[NV]) {
     float R[NV];
     if (!residual_of<T, SOLVER>(d, sm, i0, j0, z, s, own, cg, hz, ihz, srmax, R)) return;
+    if (d.mp.norms) {
+        const float vol = cg.fsz * hz;
+#pragma unroll
+        for (int v = 0; v < NV; ++v) nrm[v] += vol * fabsf(R[v]);
+    }
     int tx, ty;
     T::cell(threadIdx.x, tx, ty);
     const long long c = d.kbase + (i0 + tx) + (j0 + ty) * d.kstr[1] + z * d.kstr[2];
     const long long plane = d.L.plane;
 #pragma unroll
     for (int v = 0; v < NV; ++v) __stcg(Rout + v * plane + c, R[v]);
+}
+
+// The residual norms of a warp's cells (FP32 per thread) added in FP64 to the
+// stage's accumulator: one atomic per variable per warp.  `live` lanes of
+// the warp take part (`mask`); values from lanes beyond them are discarded.
+__device__ __forceinline__ void add_norms(Ctl* ctl, const float (&nrm)[NV], unsigned int mask, int lane, int live) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double x = (double)nrm[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(mask, x, o);
+            if (lane + o < live) x += y;
+        }
+        if (lane == 0 && x != 0.0) atomicAdd(&ctl->res_acc[v], x);
+    }
 }
 
 // dt of one problem from its CFL maximum, and the step's bookkeeping
@@ -854,6 +703,12 @@ __device__ __forceinline__ void finish_with(Ctl* ctl, float m, double cfl) {
     if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
     if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
     ctl->dt_min_raw = 1.0 / (double)m;
+    // the stage's residual norms (zeros when they are not formed)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        ctl->res[v] = ctl->res_acc[v];
+        ctl->res_acc[v] = 0.0;
+    }
     ctl->dt = dt;
     ctl->dt_apply = dt;
     ctl->time += dt;
@@ -880,7 +735,7 @@ __device__ void finish_problem(Ctl* ctl, double cfl) {
 template <class T, int SOLVER>
 __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, float dtf, float* sm,
                                              BoxPos (&bp)[T::NA], Prefetch (&pf)[T::NA], RingPos (&rp)[T::NB],
-                                             float& srmax, unsigned int& health) {
+                                             float& srmax, unsigned int& health, float (&nrm)[NV]) {
     const double* __restrict__ Uin = d.U[par];
     double* __restrict__ Uout = d.U[par ^ 1];
     const float* __restrict__ Rin = d.R[par];
@@ -904,7 +759,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
         // a single plane: the geometry is loaded where it is used
         const CellGeo cg = cell_geo<T>(d, i0, j0);
         const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
-        residual<T, SOLVER>(d, sm, Rout, i0, j0, 0, s, own, cg, gz.h, gz.ih, srmax);
+        residual<T, SOLVER>(d, sm, Rout, i0, j0, 0, s, own, cg, gz.h, gz.ih, srmax, nrm);
     } else if constexpr (!T::TWO_PHASE) {
         const CellGeo cg = cell_geo<T>(d, i0, j0);
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
@@ -930,7 +785,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             __syncthreads();
             if (z >= z0) {
                 const AxisGeo gz = d.kgeo[2][z + d.kgoff[2]];
-                residual<T, SOLVER>(d, sm, Rout, i0, j0, z, sf, own, cg, gz.h, gz.ih, srmax);
+                residual<T, SOLVER>(d, sm, Rout, i0, j0, z, sf, own, cg, gz.h, gz.ih, srmax, nrm);
             }
         }
     } else {
@@ -965,7 +820,7 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
                 if (P + 3 <= z1 + 1) issue<T>(d, Uin, Rin, P + 3, bp, pf);
             }
             if (!pwc && P <= z1) recon<T>(d, sm, P, kind, slots_of<T>(P), rp);
-            if (P - 2 >= z0) residual<T, SOLVER>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, cg, hz, ihz, srmax);
+            if (P - 2 >= z0) residual<T, SOLVER>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, cg, hz, ihz, srmax, nrm);
             if (P > z1) break;
             __syncthreads();
             if (P < z0) continue;
@@ -984,12 +839,13 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
 // otherwise (batches) a separate kernel closes every listed problem's step
 // after the stage, and items only post their maxima (no returned atomics).
 template <class T, bool COUNT>
-__device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsigned int health, float* wmax,
-                                           unsigned int* whealth) {
+__device__ __forceinline__ void close_item(const ProbDesc& d, float srmax, unsigned int health, float (&nrm)[NV],
+                                           float* wmax, unsigned int* whealth) {
     const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
     // the last warp of a block whose size is not a multiple of 32 is partial
     const int live = min(32, T::NT - (threadIdx.x & ~31));
     const unsigned int mask = live == 32 ? 0xffffffffu : ((1u << live) - 1u);
+    if (d.mp.norms) add_norms(d.ctl, nrm, mask, lane, live);
     // srmax >= 0: its bits order like unsigned integers
     const unsigned int mbits = __reduce_max_sync(mask, __float_as_uint(srmax));
     health = __reduce_or_sync(mask, health);
@@ -1033,13 +889,13 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
     if constexpr (!BATCH) {
         if (one.ctl->stop_req) return;
         const int par = one.ctl->parity;
-        const float dtf = f64_to_f32(one.ctl->dt_apply);
+        const float dtf = __double2float_rn(one.ctl->dt_apply);  // once per launch
         for (int q = blockIdx.x; q < n_items; q += gridDim.x) {
             __syncthreads();  // the previous item is finished with shared memory
-            float srmax = 0.0f;
+            float srmax = 0.0f, nrm[NV] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             unsigned int health = 0;
-            process_item<T, SOLVER>(one, q, par, dtf, sm, bp, pf, rp, srmax, health);
-            close_item<T, true>(one, srmax, health, wmax, whealth);
+            process_item<T, SOLVER>(one, q, par, dtf, sm, bp, pf, rp, srmax, health, nrm);
+            close_item<T, true>(one, srmax, health, nrm, wmax, whealth);
         }
     } else {
         __shared__ ProbDesc sd;
@@ -1062,11 +918,11 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
                 cur = pq.x;
             }
             if (s_skip) continue;
-            float srmax = 0.0f;
+            float srmax = 0.0f, nrm[NV] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             unsigned int health = 0;
-            process_item<T, SOLVER>(sd, pq.y, s_par, f64_to_f32(s_dt), sm, bp, pf, rp, srmax, health);
-            if (close_in_kernel) close_item<T, true>(sd, srmax, health, wmax, whealth);
-            else close_item<T, false>(sd, srmax, health, wmax, whealth);
+            process_item<T, SOLVER>(sd, pq.y, s_par, __double2float_rn(s_dt), sm, bp, pf, rp, srmax, health, nrm);
+            if (close_in_kernel) close_item<T, true>(sd, srmax, health, nrm, wmax, whealth);
+            else close_item<T, false>(sd, srmax, health, nrm, wmax, whealth);
         }
     }
 }
@@ -1143,7 +999,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
         unsigned int health = 0;
         // pending update of the own cell and its working copy (store())
         if (own) {
-            const float cf = bp[0].cfxy * (f64_to_f32(sc.dt_apply) * gz.ih);
+            const float cf = bp[0].cfxy * (__double2float_rn(sc.dt_apply) * gz.ih);
             float inc[NV], w[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
@@ -1261,7 +1117,7 @@ __global__ void k_mix_apply(const ProbDesc* __restrict__ probs, int p) {
     const long long c = L.at(i, j, k);
     const int a1 = L.nd == 3 ? j : 0, a2 = L.nd == 3 ? k : (L.nd == 2 ? j : 0);
     const int par = d.ctl->parity;
-    const float dtf = f64_to_f32(d.ctl->dt_apply);
+    const float dtf = __double2float_rn(d.ctl->dt_apply);
     const float cf = (d.kgeo[0][i + d.kgoff[0]].ih * d.kgeo[1][a1 + d.kgoff[1]].ih) *
                      (dtf * d.kgeo[2][a2 + d.kgoff[2]].ih);
     double* U = d.U[par];
@@ -1453,7 +1309,7 @@ void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots) {
     d.nq = d.ncol * ((nz + d.ch - 1) / d.ch);
 }
 
-ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err) {
+ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err, cudaStream_t st) {
     const int nd = mb.desc.L.nd;
     if (nd < 3) ty = 1;
     size_t bytes = 0;
@@ -1470,7 +1326,9 @@ ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string
     mixed_items(mb.desc, tx, ty, zchunks, slots);
     mb.zchunks = nd >= 2 ? (mb.desc.kn[2] + mb.desc.ch - 1) / mb.desc.ch : 1;
     mb.grid = (int)std::min<long long>(mb.desc.nq, slots);
-    if (cudaMemcpy(mb.d_desc, &mb.desc, sizeof(ProbDesc), cudaMemcpyHostToDevice) != cudaSuccess) {
+    // ordered on the stream the steps run on (a pageable source is staged
+    // before the call returns, so mb.desc may change afterwards)
+    if (cudaMemcpyAsync(mb.d_desc, &mb.desc, sizeof(ProbDesc), cudaMemcpyHostToDevice, st) != cudaSuccess) {
         err = "descriptor upload failed";
         return TS_ERR_CUDA;
     }
@@ -1478,7 +1336,7 @@ ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string
 }
 
 ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
-                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err) {
+                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err, cudaStream_t st) {
     if (L.plane > (1LL << 31) - 1) { err = "grid too large for the mixed path"; return TS_ERR_INVALID; }
     d.L = L;
     d.ctl = ctl;
@@ -1519,7 +1377,8 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
         }
         void* p;
         if ((s = alloc(sizeof(AxisGeo) * geo.size(), &p)) != TS_OK) return s;
-        if (cudaMemcpy(p, geo.data(), sizeof(AxisGeo) * geo.size(), cudaMemcpyHostToDevice) != cudaSuccess) {
+        // pageable source: staged before the call returns, so `geo` may go
+        if (cudaMemcpyAsync(p, geo.data(), sizeof(AxisGeo) * geo.size(), cudaMemcpyHostToDevice, st) != cudaSuccess) {
             err = "geometry upload failed";
             return TS_ERR_CUDA;
         }
@@ -1566,6 +1425,7 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
     }
     m.force = ph.force;
     m.accel = ph.accel;
+    m.norms = c.residual_norms != 0;
     for (int a = 0; a < 3; ++a) {
         m.sigma[a] = (float)ph.sigma[a];
         m.g[a] = (float)ph.g[a];
@@ -1574,17 +1434,17 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
 }
 
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
-                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err) {
+                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err, cudaStream_t st, bool zero_buffers) {
     ts_status s;
     ProbDesc& d = mb.desc;
     std::memset(&d, 0, sizeof d);
-    if ((s = mixed_problem(c, L, ph, g, ctl, alloc, d, err)) != TS_OK) return s;
+    if ((s = mixed_problem(c, L, ph, g, ctl, alloc, d, err, st)) != TS_OK) return s;
     for (int b = 0; b < 2; ++b) {
         if ((s = alloc(sizeof(double) * NV * L.plane, (void**)&d.U[b])) != TS_OK) return s;
         if ((s = alloc(sizeof(float) * NV * L.plane, (void**)&d.R[b])) != TS_OK) return s;
-        if (cudaMemset(d.U[b], 0, sizeof(double) * NV * L.plane) != cudaSuccess ||
-            cudaMemset(d.R[b], 0, sizeof(float) * NV * L.plane) != cudaSuccess) {
-            err = "cudaMemset failed";
+        if (zero_buffers && (cudaMemsetAsync(d.U[b], 0, sizeof(double) * NV * L.plane, st) != cudaSuccess ||
+                             cudaMemsetAsync(d.R[b], 0, sizeof(float) * NV * L.plane, st) != cudaSuccess)) {
+            err = "cudaMemsetAsync failed";
             return TS_ERR_CUDA;
         }
     }
@@ -1596,7 +1456,7 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
     // 12.2e9 cell-updates/s for 260-thread rows)
     const int tx = L.nd == 3 ? 32 : (L.nd == 2 ? 132 : 256);
     const int ty = L.nd == 3 ? 8 : 1;
-    return mixed_set_tile(mb, tx, ty, 0, err);
+    return mixed_set_tile(mb, tx, ty, 0, err, st);
 }
 
 void mixed_step(MixedBufs& mb, const Phys&, cudaStream_t st, cudaEvent_t* ev, int* n_launch, const char** names) {
@@ -1726,17 +1586,24 @@ extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* stat
     };
     Ctl* ctl = nullptr;
     if ((s = carve(sizeof(Ctl), (void**)&ctl)) != TS_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
     MixedBufs mb;
     const Phys ph = make_phys(*cfg);
-    if ((s = mixed_init(*cfg, L, ph, grid, ctl, carve, mb, err)) != TS_OK) return fail(s, err);
+    // every upload of the set-up is queued on the caller's stream, ahead of
+    // the steps; the second state and residual buffers need no clearing (the
+    // first stage writes every cell of them before anything reads them)
+    if ((s = mixed_init(*cfg, L, ph, grid, ctl, carve, mb, err, st, false)) != TS_OK) return fail(s, err);
 
-    cudaStream_t st = static_cast<cudaStream_t>(stream);
     Ctl c;
     std::memset(&c, 0, sizeof c);
+    // A fresh run (no info, or iteration 0 at time 0) starts the snapshot
+    // schedule at SaveSolutionTime / SaveSliceTime as Kernel::Init does
+    // (kernel.h:259-263); a continued run keeps the caller's schedule.
+    const bool fresh = !info || (info->iteration == 0 && info->time == 0.0);
     c.time = info ? info->time : 0.0;
     c.iteration = info ? info->iteration : 0;
-    c.next_sol = info ? info->next_solution_time : cfg->save_solution_time;
-    c.next_slice = info ? info->next_slice_time : cfg->save_slice_time;
+    c.next_sol = fresh ? cfg->save_solution_time : info->next_solution_time;
+    c.next_slice = fresh ? cfg->save_slice_time : info->next_slice_time;
     c.max_iteration = cfg->max_iteration;
     c.max_time = cfg->max_time;
     c.save_sol = cfg->save_solution_time;
@@ -1764,7 +1631,7 @@ extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* stat
         info->dt = c.dt;
         info->next_solution_time = c.next_sol;
         info->next_slice_time = c.next_slice;
-        for (int v = 0; v < NV; ++v) info->residual[v] = 0.0;
+        for (int v = 0; v < NV; ++v) info->residual[v] = c.res[v];  // zeros unless cfg->residual_norms
     }
     return TS_OK;
 }

@@ -35,6 +35,7 @@ struct MixPhys {
     float bc_vel[6][3];    // MovingWall velocity
     int force, accel;      // source terms on (kernel.h:941-989)
     float sigma[3], g[3];  // Sigma, UniformAcceleration
+    int norms;             // form the residual norms sum V |R| (kernel.h:326)
 };
 
 // Everything the fused kernel needs about one problem (lives in device memory).
@@ -70,9 +71,10 @@ struct MixedBufs {
 
 using DeviceAlloc = std::function<ts_status(size_t bytes, void** out)>;
 
-// Geometry and physics of one problem (host work + uploads through `alloc`).
+// Geometry and physics of one problem (host work + uploads through `alloc`,
+// queued on stream `st`: work queued there later sees them).
 ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
-                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err);
+                        const DeviceAlloc& alloc, ProbDesc& d, std::string& err, cudaStream_t st);
 // Cells per tile along x and y of a compiled tile of tx x ty threads (one-row
 // tiles of 1D and 2D problems own tx - 4 cells).
 void mixed_tile_cells(int nd, int tx, int ty, int* cx, int* cy);
@@ -106,11 +108,14 @@ bool mixed_tail_ready(int solver, int cluster);
 cudaError_t mixed_launch_tail(int solver, int cluster, int n_problems, const ProbDesc* d_probs, const int* d_list,
                               int budget, cudaStream_t st);
 
+// Set-up of one problem's buffers; every upload and (with zero_buffers) the
+// clearing of the state and residual buffers are queued on `st`.
 ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const HostGrid& g, Ctl* ctl,
-                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err);
+                     const DeviceAlloc& alloc, MixedBufs& mb, std::string& err, cudaStream_t st,
+                     bool zero_buffers = true);
 // Choose the tile shape (tx, ty) and the z chunking (0 = automatic), and
-// recompute the persistent grid.
-ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err);
+// recompute the persistent grid (descriptor upload queued on `st`).
+ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err, cudaStream_t st);
 
 constexpr int kMixedMaxLaunches = 4;
 void mixed_step(MixedBufs& mb, const Phys& ph, cudaStream_t st, cudaEvent_t* ev = nullptr, int* n_launch = nullptr,

@@ -22,8 +22,11 @@ from . import capi
 NAT = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
 
 
-def tubes(count: int = 4096, seed: int = 4096, t_end: float = 0.1, max_iter: int = 10_000_000):
-    """[(case, initial state)] of the batched-tubes configuration."""
+def tubes(count: int = 4096, seed: int = 4096, t_end: float = 0.1, max_iter: int = 10_000_000, fill=None):
+    """[(case, initial state)] of the batched-tubes configuration.  `fill`
+    builds a scenario's state (default: the library's ts_fill_scenario; the
+    CPU legs of the bench pass the oracle's bit-identical restatement)."""
+    fill = fill or capi.fill_scenario
     rng = np.random.default_rng(seed)
     out = []
     for k in range(count):
@@ -37,8 +40,7 @@ def tubes(count: int = 4096, seed: int = 4096, t_end: float = 0.1, max_iter: int
                               eos=capi.EOS_STIFFENED if stiff else capi.EOS_IDEAL, p_inf=6.0 if stiff else 0.0,
                               recon=recon, limiter=capi.LIM_BJ, solver=capi.RS_ROE, cfl=0.5, max_time=t_end,
                               max_iter=max_iter, bc=[NAT] * 6)
-        ic = capi.fill_scenario(case, capi.SCENARIO_SHOCK_TUBE, seed + k,
-                                [0.5, rho[0], u[0], p[0], rho[1], u[1], p[1]])
+        ic = fill(case, capi.SCENARIO_SHOCK_TUBE, seed + k, [0.5, rho[0], u[0], p[0], rho[1], u[1], p[1]])
         out.append((case, ic))
     return out
 
@@ -72,5 +74,5 @@ def stream(rate_hz: float = 200.0, seconds: float = 60.0, seed: int = 200, steps
     return out
 
 
-def stream_state(case: dict, params, seed: int):
-    return capi.fill_scenario(case, capi.SCENARIO_QUADRANTS, seed, params)
+def stream_state(case: dict, params, seed: int, fill=None):
+    return (fill or capi.fill_scenario)(case, capi.SCENARIO_QUADRANTS, seed, params)
