@@ -78,7 +78,8 @@ enum {
     TS_HEALTH_NAN = 1u,
     TS_HEALTH_NEG_DENSITY = 2u,
     TS_HEALTH_NEG_PRESSURE = 4u,
-    TS_HEALTH_RIEMANN = 8u /* the exact (Godunov) solver's p* iteration did not converge at some face */
+    TS_HEALTH_RIEMANN = 8u, /* the exact (Godunov) solver's p* iteration did not converge at some face */
+    TS_HEALTH_TIMEOUT = 16u /* a bounded wait inside a kernel gave up (the step's results are not valid) */
 };
 
 /* BlockNode (KernelConfiguration.h:10-19): stretched-grid block start. */

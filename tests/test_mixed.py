@@ -112,7 +112,7 @@ def test_mixed_tile_and_chunk_independent(nd, tslib):
     if nd == 3:
         case = O.make_case(ndims=3, nx=37, ny=29, nz=21, periodic=(1, 0, 0), recon=3, solver=1, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, SYM, SYM])
-        tiles = [(32, 8, 0), (16, 16, 0), (64, 4, 0), (32, 8, 1), (32, 8, 3), (16, 16, 7)]
+        tiles = [(32, 8, 0), (16, 16, 0), (32, 8, 1), (32, 8, 3), (16, 16, 7), (32, 8, 21)]
         scen, params = 2, [1.0, 0.1, 10.0, 0.2, 0.01]
     elif nd == 2:
         case = O.make_case(ndims=2, nx=70, ny=45, periodic=(1, 0, 1), recon=3, solver=3, cfl=0.4,

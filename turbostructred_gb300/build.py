@@ -30,6 +30,7 @@ UNITS = {
     # FP32 flux path: flush-to-zero and approximate FP32 division/sqrt; FP64
     # arithmetic is unaffected by these flags.
     "ts_mixed.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
+    "ts_mix3d.cu": ["-ftz=true", "-prec-div=false", "-prec-sqrt=false"],
     "ts_capi.cu": [],
     "ts_batch.cu": [],
     "ts_host.cpp": [],

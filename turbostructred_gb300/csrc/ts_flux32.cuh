@@ -190,5 +190,56 @@ __device__ __forceinline__ float flux32(const MixPhys& p, const float UL[NV], co
     return roe32<A>(p, UL, UR, F);
 }
 
+// ---------------------------------------------------------------------------
+// Step bookkeeping shared by the fused kernels
+// ---------------------------------------------------------------------------
+// The residual norms of a warp's cells (FP32 per thread) added in FP64 to the
+// stage's accumulator: one atomic per variable per warp.  `live` lanes of
+// the warp take part (`mask`); values from lanes beyond them are discarded.
+__device__ __forceinline__ void add_norms(Ctl* ctl, const float (&nrm)[NV], unsigned int mask, int lane, int live) {
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        double x = (double)nrm[v];
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const double y = __shfl_down_sync(mask, x, o);
+            if (lane + o < live) x += y;
+        }
+        if (lane == 0 && x != 0.0) atomicAdd(&ctl->res_acc[v], x);
+    }
+}
+
+// dt of one problem from its CFL maximum, and the step's bookkeeping
+// (ComputeTimeStep :1427-1437, time += dt and iteration++ :1486-1487, and the
+// Kernel::Run snapshot/termination rules kernel.h:1763-1846).
+__device__ __forceinline__ void finish_with(Ctl* ctl, float m, double cfl) {
+    double dt = cfl / (double)m;
+    if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
+    if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
+    ctl->dt_min_raw = 1.0 / (double)m;
+    // the stage's residual norms (zeros when they are not formed)
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        ctl->res[v] = ctl->res_acc[v];
+        ctl->res_acc[v] = 0.0;
+    }
+    ctl->dt = dt;
+    ctl->dt_apply = dt;
+    ctl->time += dt;
+    ctl->iteration += 1;
+    ctl->parity ^= 1;
+    ctl->srmax_bits = 0u;
+    ctl->blocks_done = 0u;
+    if (ctl->run_mode) {
+        if ((ctl->save_sol > 0) && (ctl->next_sol == ctl->time)) ctl->next_sol += ctl->save_sol;
+        if ((ctl->save_slice > 0) && (ctl->next_slice == ctl->time)) ctl->next_slice += ctl->save_slice;
+        if (ctl->iteration == ctl->max_iteration || ctl->time >= ctl->max_time) ctl->stop_req = 1;
+    }
+}
+
+__device__ __forceinline__ void finish_problem(Ctl* ctl, double cfl) {
+    finish_with(ctl, __uint_as_float(*(volatile unsigned int*)&ctl->srmax_bits), cfl);
+}
+
 }  // namespace mix32
 }  // namespace ts

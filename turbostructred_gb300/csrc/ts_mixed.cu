@@ -679,54 +679,6 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
     for (int v = 0; v < NV; ++v) __stcg(Rout + v * plane + c, R[v]);
 }
 
-// The residual norms of a warp's cells (FP32 per thread) added in FP64 to the
-// stage's accumulator: one atomic per variable per warp.  `live` lanes of
-// the warp take part (`mask`); values from lanes beyond them are discarded.
-__device__ __forceinline__ void add_norms(Ctl* ctl, const float (&nrm)[NV], unsigned int mask, int lane, int live) {
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        double x = (double)nrm[v];
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const double y = __shfl_down_sync(mask, x, o);
-            if (lane + o < live) x += y;
-        }
-        if (lane == 0 && x != 0.0) atomicAdd(&ctl->res_acc[v], x);
-    }
-}
-
-// dt of one problem from its CFL maximum, and the step's bookkeeping
-// (ComputeTimeStep :1427-1437, time += dt and iteration++ :1486-1487, and the
-// Kernel::Run snapshot/termination rules kernel.h:1763-1846).
-__device__ __forceinline__ void finish_with(Ctl* ctl, float m, double cfl) {
-    double dt = cfl / (double)m;
-    if ((ctl->save_sol > 0) && (ctl->next_sol < ctl->time + dt)) dt = ctl->next_sol - ctl->time;
-    if ((ctl->save_slice > 0) && (ctl->next_slice < ctl->time + dt)) dt = ctl->next_slice - ctl->time;
-    ctl->dt_min_raw = 1.0 / (double)m;
-    // the stage's residual norms (zeros when they are not formed)
-#pragma unroll
-    for (int v = 0; v < NV; ++v) {
-        ctl->res[v] = ctl->res_acc[v];
-        ctl->res_acc[v] = 0.0;
-    }
-    ctl->dt = dt;
-    ctl->dt_apply = dt;
-    ctl->time += dt;
-    ctl->iteration += 1;
-    ctl->parity ^= 1;
-    ctl->srmax_bits = 0u;
-    ctl->blocks_done = 0u;
-    if (ctl->run_mode) {
-        if ((ctl->save_sol > 0) && (ctl->next_sol == ctl->time)) ctl->next_sol += ctl->save_sol;
-        if ((ctl->save_slice > 0) && (ctl->next_slice == ctl->time)) ctl->next_slice += ctl->save_slice;
-        if (ctl->iteration == ctl->max_iteration || ctl->time >= ctl->max_time) ctl->stop_req = 1;
-    }
-}
-
-__device__ void finish_problem(Ctl* ctl, double cfl) {
-    finish_with(ctl, __uint_as_float(*(volatile unsigned int*)&ctl->srmax_bits), cfl);
-}
-
 // ---------------------------------------------------------------------------
 // The fused step kernel
 // ---------------------------------------------------------------------------
@@ -1144,7 +1096,6 @@ __global__ void k_batch_finish(const ProbDesc* __restrict__ probs, const int* __
 // Compiled tiles: (problem dimension, threads along x, threads along y).
 // 3D: two-axis tiles marching z.  2D: one-row tiles marching y.  1D: one-row
 // tiles, one plane.
-#define TS_MIXED_TILES_3D(X) X(3, 32, 8) X(3, 16, 16) X(3, 64, 4)
 #define TS_MIXED_TILES_2D(X) X(2, 260, 1) X(2, 132, 1) X(2, 68, 1)
 #define TS_MIXED_TILES_1D(X) X(1, 512, 1) X(1, 256, 1) X(1, 128, 1)
 
@@ -1162,7 +1113,6 @@ bool with_tile(int nd, int tx, int ty, int solver, F&& f) {
         if (solver == TS_RS_HLLC) f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_HLLC>();         \
         else f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_ROE_PIKE>();                          \
     }
-    TS_MIXED_TILES_3D(TS_TRY)
     TS_MIXED_TILES_2D(TS_TRY)
     TS_MIXED_TILES_1D(TS_TRY)
 #undef TS_TRY
@@ -1314,7 +1264,10 @@ ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string
     if (nd < 3) ty = 1;
     size_t bytes = 0;
     int per_sm = 0;
-    if (!mixed_tile_info(nd, tx, ty, mb.desc.mp.solver, &bytes, &per_sm)) {
+    const bool found = nd == 3 ? mix3d_tile_info(tx, ty, mb.desc.mp.solver, mb.desc.mp.recon, mb.desc.mp.limiter,
+                                                 &bytes, &per_sm)
+                               : mixed_tile_info(nd, tx, ty, mb.desc.mp.solver, &bytes, &per_sm);
+    if (!found) {
         err = "no compiled tile " + std::to_string(tx) + "x" + std::to_string(ty) + " for " + std::to_string(nd) + "D";
         return TS_ERR_UNSUPPORTED;
     }
@@ -1326,6 +1279,12 @@ ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string
     mixed_items(mb.desc, tx, ty, zchunks, slots);
     mb.zchunks = nd >= 2 ? (mb.desc.kn[2] + mb.desc.ch - 1) / mb.desc.ch : 1;
     mb.grid = (int)std::min<long long>(mb.desc.nq, slots);
+    if (nd == 3) {
+        // the 3D kernel closes the step once per CTA, after all its items
+        mb.desc.nq = mb.grid;
+        ts_status s = mix3d_make_maps(mb.desc, tx, ty, mb.maps, err);
+        if (s != TS_OK) return s;
+    }
     // ordered on the stream the steps run on (a pageable source is staged
     // before the call returns, so mb.desc may change afterwards)
     if (cudaMemcpyAsync(mb.d_desc, &mb.desc, sizeof(ProbDesc), cudaMemcpyHostToDevice, st) != cudaSuccess) {
@@ -1460,10 +1419,12 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
 }
 
 void mixed_step(MixedBufs& mb, const Phys&, cudaStream_t st, cudaEvent_t* ev, int* n_launch, const char** names) {
+    const bool d3 = mb.desc.L.nd == 3;
     if (ev) cudaEventRecord(ev[0], st);
-    mixed_launch_single(mb.desc.L.nd, mb.tx, mb.ty, mb.desc.mp.solver, mb.grid, mb.desc, st);
+    if (d3) mix3d_launch(mb.tx, mb.ty, mb.grid, mb.desc, mb.maps, st);
+    else mixed_launch_single(mb.desc.L.nd, mb.tx, mb.ty, mb.desc.mp.solver, mb.grid, mb.desc, st);
     if (ev) cudaEventRecord(ev[1], st);
-    if (names) names[0] = "k_mix_step";
+    if (names) names[0] = d3 ? "k_mix3d" : "k_mix_step";
     if (n_launch) *n_launch = 1;
 }
 

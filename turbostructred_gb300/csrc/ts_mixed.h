@@ -4,6 +4,7 @@
 // by one stage.  See ts_mixed.cu.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <functional>
@@ -59,8 +60,16 @@ struct ProbDesc {
     int ch, nq;            // planes per marching chunk, work items (columns x chunks)
 };
 
+// TMA descriptors of a 3D problem's state buffers (U[b] FP64, R[b] FP32),
+// for the 3D fused kernel; kernel parameters.
+struct Mix3dMaps {
+    CUtensorMap u[2];
+    CUtensorMap r[2];
+};
+
 struct MixedBufs {
     ProbDesc desc;                 // host copy
+    Mix3dMaps maps;                // 3D problems: tensor maps of the state buffers
     ProbDesc* d_desc = nullptr;    // device copy
     int tx = 32, ty = 8;           // tile (one of the compiled shapes)
     int zchunks = 1;               // z chunks per column (3D)
@@ -116,6 +125,13 @@ ts_status mixed_init(const ts_config& c, const Layout& L, const Phys& ph, const 
 // Choose the tile shape (tx, ty) and the z chunking (0 = automatic), and
 // recompute the persistent grid (descriptor upload queued on `st`).
 ts_status mixed_set_tile(MixedBufs& mb, int tx, int ty, int zchunks, std::string& err, cudaStream_t st);
+
+// 3D problems: the TMA-staged fused kernel (ts_mix3d.cu).  Compiled tiles
+// 32x8 and 16x16; smem bytes and resident CTAs per SM, or false.
+bool mix3d_tile_info(int tx, int ty, int solver, int recon, int limiter, size_t* smem, int* per_sm);
+// Tensor maps of the four state buffers for the tile's box.
+ts_status mix3d_make_maps(const ProbDesc& d, int tx, int ty, Mix3dMaps& maps, std::string& err);
+void mix3d_launch(int tx, int ty, int grid, const ProbDesc& d, const Mix3dMaps& maps, cudaStream_t st);
 
 constexpr int kMixedMaxLaunches = 4;
 void mixed_step(MixedBufs& mb, const Phys& ph, cudaStream_t st, cudaEvent_t* ev = nullptr, int* n_launch = nullptr,
