@@ -112,8 +112,9 @@ struct Tile3 {
     static constexpr int FFY = ((N2 + 31) / 32) * 32;  // y far faces: threads [FFY, FFY + TX)
     static constexpr int FFX = FFY + TX;               // x far faces: threads [FFX, FFX + TY)
     static_assert(FFX + TY <= F1 || TX * TY > 512, "far faces on threads without ring cells");
-    // shared memory (bytes): two TMA stages (FP64 U box, FP32 R box), two
-    // working-state planes, two slots of x/y face states, the x/y face fluxes
+    // shared memory (bytes): two TMA stages (FP64 U box, FP32 R box), three
+    // working-state planes (k, k+1, k+2), the x/y face states of one plane,
+    // the x/y face fluxes of one plane
     static constexpr int SU = NBOX * NV * 8, SR = NBOX * NV * 4;
     static constexpr int TX_BYTES = SU + SR;                  // bytes the two boxes of a plane deliver
     static constexpr int STAGE = (TX_BYTES + 127) / 128 * 128;  // stage pitch (128-byte aligned)
@@ -122,8 +123,9 @@ struct Tile3 {
     static constexpr int NW = NV * NBOX;                   // floats per working-state plane
     static constexpr int NFVX = NV * TY * (TX + 2);         // x face states per slot
     static constexpr int NFVY = NV * (TY + 2) * TX;         // y face states per slot
-    static constexpr int OFF_FV = OFF_W + 2 * NW * 4;
-    static constexpr int OFF_FX = OFF_FV + 2 * (NFVX + NFVY) * 4;
+    static constexpr int NWS = 3;                           // working-state planes kept
+    static constexpr int OFF_FV = OFF_W + NWS * NW * 4;
+    static constexpr int OFF_FX = OFF_FV + (NFVX + NFVY) * 4;
     static constexpr int NFX = 6 * TY * (TX + 1), NFY = 6 * (TY + 1) * TX;
     static constexpr int OFF_RED = OFF_FX + (NFX + NFY) * 4;  // per-warp maxima and health words
     static constexpr int OFF_FAIL = OFF_RED + 2 * 32 * 4;      // set once a wait gave up
@@ -134,12 +136,10 @@ struct Tile3 {
 
     // shared-memory indices (floats unless noted)
     static __device__ __forceinline__ int w(int slot, int v, int box) { return slot * NW + v * NBOX + box; }
-    static __device__ __forceinline__ int fvx(int slot, int v, int cy, int c) {
-        return slot * (NFVX + NFVY) + (v * TY + cy) * (TX + 2) + c;
-    }
-    static __device__ __forceinline__ int fvy(int slot, int v, int c, int cx) {
-        return slot * (NFVX + NFVY) + NFVX + (v * (TY + 2) + c) * TX + cx;
-    }
+    // working-state slot of plane j (j >= -2)
+    static __device__ __forceinline__ int wslot(int j) { return (j + 3) % 3; }
+    static __device__ __forceinline__ int fvx(int v, int cy, int c) { return (v * TY + cy) * (TX + 2) + c; }
+    static __device__ __forceinline__ int fvy(int v, int c, int cx) { return NFVX + (v * (TY + 2) + c) * TX + cx; }
     static __device__ __forceinline__ int fx(int v, int cy, int c) { return (v * TY + cy) * (TX + 1) + c; }
     static __device__ __forceinline__ int fy(int v, int c, int cx) { return NFX + (v * (TY + 1) + c) * TX + cx; }
 };
@@ -383,7 +383,7 @@ __device__ __forceinline__ void issue_plane(const ProbDesc& d, const Mix3dMaps& 
 template <class T>
 __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, const unsigned char* stage,
                                         const double* __restrict__ Uin, const float* __restrict__ Rin,
-                                        double* __restrict__ Uout, float* smw, int j, float dtf, W5 (&wout)[2],
+                                        double* __restrict__ Uout, float* smw, int j, float dtf,
                                         unsigned int& health) {
     const MixPhys& mp = d.mp;
     const double* su = reinterpret_cast<const double*>(stage);
@@ -391,9 +391,10 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
     int sk, zs;
     resolve(j, d.kn[2], d.kper[2], 4, sk, zs);
     const float cfz = dtf * __ldg(&d.kgeo[2][sk + d.kgoff[2]].ih);
-    const long long plane = d.L.plane;
-    const long long zoff = d.kbase + (long long)sk * d.kstr[2];
-    const int slot = j & 1;
+    // element offsets fit 32 bits (5 planes < 2^32, checked on the host)
+    const unsigned int plane = (unsigned int)d.L.plane;
+    const unsigned int zoff = (unsigned int)d.kbase + (unsigned int)sk * (unsigned int)d.kstr[2];
+    const int slot = T::wslot(j);
     const bool own_plane = j >= it.z0 && j < it.z1;
     const bool stiff = mp.eos == TS_EOS_STIFFENED_GAS;
 #pragma unroll
@@ -412,32 +413,30 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
             // periodic halo cell of an edge tile: not in the staged box
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                u[v] = __ldg(Uin + v * plane + zoff + c.goff);
-                r[v] = __ldg(Rin + v * plane + zoff + c.goff);
+                u[v] = __ldg(Uin + (zoff + (unsigned int)c.goff + v * plane));
+                r[v] = __ldg(Rin + (zoff + (unsigned int)c.goff + v * plane));
             }
         }
         const float cf = c.cfxy * cfz;
         float inc[NV], w[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
+        const double e4 = stiff ? u[4] - mp.einf_d : u[4];  // shifted energy (uniform choice)
 #pragma unroll
         for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
-        w[4] = (stiff ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4])) + inc[4];
+        w[4] = f64_to_f32(e4) + inc[4];
         if (c.xs >= 0) bc32(mp, c.xs, 0, w);
         if (c.ys >= 0) bc32(mp, c.ys, 1, w);
         if (zs >= 0) bc32(mp, zs, 2, w);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) {
-            smw[T::w(slot, v, c.wbox)] = w[v];
-            wout[p].v[v] = w[v];
-        }
+        for (int v = 0; v < NV; ++v) smw[T::w(slot, v, c.wbox)] = w[v];
         if (p == 0 && own_plane && it.own) {
-            const long long o = it.own_off + (long long)j * d.kstr[2];
+            const unsigned int o = (unsigned int)it.own_off + (unsigned int)j * (unsigned int)d.kstr[2];
             double un[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 un[v] = u[v] + f32_to_f64(inc[v]);
-                __stcs(Uout + v * plane + o, un[v]);
+                __stcs(Uout + (o + v * plane), un[v]);
             }
             // rho > 0 tested on the bit pattern (no FP64 comparison)
             const long long b = __double_as_longlong(un[0]);
@@ -448,21 +447,20 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
     }
 }
 
-// Limited slopes of plane j at the thread's reconstruction positions; the
-// face states go to shared memory (W + dx, W + dy of the cells left of /
-// below a face; W - dx, W - dy of the far ring cells), the own cell's
-// right-hand x/y states and both z states stay in registers.  wm/wp: the
-// working copy of planes j-1 and j+1.
+// Limited slopes of plane j at the thread's reconstruction positions (the
+// working state of planes j-1, j, j+1 in shared memory); the face states go
+// to shared memory (W + dx, W + dy of the cells left of / below a face;
+// W - dx, W - dy of the far ring cells), the own cell's right-hand x/y
+// states and both z states stay in registers.
 template <class T, int KIND>
-__device__ __forceinline__ void reconstruct(const ProbDesc& d, const Item3& it, float* sm, int j,
-                                            const W5 (&wm)[2], const W5 (&wp)[2], W5& urx, W5& ury, W5& ulz,
-                                            W5& urz, float4& own4) {
+__device__ __forceinline__ void reconstruct(const ProbDesc& d, const Item3& it, float* sm, int j, W5& urx, W5& ury,
+                                            W5& ulz, W5& urz) {
     if ((j < 0 || j >= d.kn[2]) && !d.kper[2]) return;
     int sk, s_;
     resolve(j, d.kn[2], 1, 0, sk, s_);
     const AxisGeo gz = d.kgeo[2][sk + d.kgoff[2]];
-    const int slot = j & 1;
-    float* smw = sm + T::OFF_W / 4;
+    const int s0 = T::wslot(j), sm1 = T::wslot(j - 1), sp1 = T::wslot(j + 1);
+    const float* smw = sm + T::OFF_W / 4;
     float* fv = sm + T::OFF_FV / 4;
 #pragma unroll
     for (int p = 0; p < 2; ++p) {
@@ -483,37 +481,42 @@ __device__ __forceinline__ void reconstruct(const ProbDesc& d, const Item3& it, 
             eps2 = 125.0f * (g[0].h * g[1].h * g[2].h);
         }
         const int box = r.box;
+        // second positions: one face state per variable, W + dd or W - dd
+        // along x (ring cells left/right of the tile) or y (below/above)
+        int fdst = 0, fstride = 0, fax = 0;
+        float fsg = 1.0f;
+        if (p == 1) {
+            const int role = it.role;
+            fax = role >= 3 ? 1 : 0;
+            fsg = (role == 2 || role == 4) ? -1.0f : 1.0f;
+            if (role == 1) fdst = T::fvx(0, it.cy2, 0);
+            else if (role == 2) fdst = T::fvx(0, it.cy2, T::TX + 1);
+            else if (role == 3) fdst = T::fvy(0, 0, it.cx2);
+            else fdst = T::fvy(0, T::TY + 1, it.cx2);
+            fstride = fax ? (T::TY + 2) * T::TX : T::TY * (T::TX + 2);
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            const float w0 = smw[T::w(slot, v, box)];
+            const float w0 = smw[T::w(s0, v, box)];
             float nm[3], np[3], dd[3] = {0.0f, 0.0f, 0.0f};
-            nm[0] = smw[T::w(slot, v, box - 1)];
-            np[0] = smw[T::w(slot, v, box + 1)];
-            nm[1] = smw[T::w(slot, v, box - T::BX)];
-            np[1] = smw[T::w(slot, v, box + T::BX)];
-            nm[2] = wm[p].v[v];
-            np[2] = wp[p].v[v];
+            nm[0] = smw[T::w(s0, v, box - 1)];
+            np[0] = smw[T::w(s0, v, box + 1)];
+            nm[1] = smw[T::w(s0, v, box - T::BX)];
+            np[1] = smw[T::w(s0, v, box + T::BX)];
+            nm[2] = smw[T::w(sm1, v, box)];
+            np[2] = smw[T::w(sp1, v, box)];
             if (KIND != K_PWC) half_slopes<KIND>(w0, nm, np, g, eps2, dd);
             if (p == 0) {
-                fv[T::fvx(slot, v, it.cy, it.cx + 1)] = w0 + dd[0];
-                fv[T::fvy(slot, v, it.cy + 1, it.cx)] = w0 + dd[1];
+                fv[T::fvx(v, it.cy, it.cx + 1)] = w0 + dd[0];
+                fv[T::fvy(v, it.cy + 1, it.cx)] = w0 + dd[1];
                 urx.v[v] = w0 - dd[0];
                 ury.v[v] = w0 - dd[1];
                 ulz.v[v] = w0 + dd[2];
                 urz.v[v] = w0 - dd[2];
-            } else if (it.role == 1) {
-                fv[T::fvx(slot, v, it.cy2, 0)] = w0 + dd[0];
-            } else if (it.role == 2) {
-                fv[T::fvx(slot, v, it.cy2, T::TX + 1)] = w0 - dd[0];
-            } else if (it.role == 3) {
-                fv[T::fvy(slot, v, 0, it.cx2)] = w0 + dd[1];
             } else {
-                fv[T::fvy(slot, v, T::TY + 1, it.cx2)] = w0 - dd[1];
+                fv[fdst + v * fstride] = w0 + fsg * (fax ? dd[1] : dd[0]);
             }
         }
-        if (p == 0)
-            own4 = make_float4(smw[T::w(slot, 0, box)], smw[T::w(slot, 1, box)], smw[T::w(slot, 2, box)],
-                               smw[T::w(slot, 3, box)]);
     }
 }
 
@@ -540,7 +543,6 @@ template <class T, int SOLVER>
 __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, float* sm, int k, const W5& urx,
                                          const W5& ury) {
     const MixPhys& mp = d.mp;
-    const int slot = k & 1;
     const float* fv = sm + T::OFF_FV / 4;
     float* ff = sm + T::OFF_FX / 4;
     const int gi = it.i0 + it.cx, gj = it.j0 + it.cy;
@@ -548,21 +550,15 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
         float UL0[NV], UR0[NV], UL1[NV], UR1[NV], F0[NV], F1[NV];
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
-            UL0[v] = fv[T::fvx(slot, v, it.cy, it.cx)];
+            UL0[v] = fv[T::fvx(v, it.cy, it.cx)];
             UR0[v] = urx.v[v];
-            UL1[v] = fv[T::fvy(slot, v, it.cy, it.cx)];
+            UL1[v] = fv[T::fvy(v, it.cy, it.cx)];
             UR1[v] = ury.v[v];
         }
+        // a face outside the domain is computed on whatever the registers
+        // hold and not stored
         const bool ok0 = gi <= d.kn[0] && gj < d.kn[1];
         const bool ok1 = gi < d.kn[0] && gj <= d.kn[1];
-        if (!ok0) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) UL0[v] = UR0[v] = 1.0f;
-        }
-        if (!ok1) {
-#pragma unroll
-            for (int v = 0; v < NV; ++v) UL1[v] = UR1[v] = 1.0f;
-        }
         const float l0 = face_flux<SOLVER, 0>(mp, UL0, UR0, gi, d.kn[0], d.kper[0], F0);
         const float l1 = face_flux<SOLVER, 1>(mp, UL1, UR1, gj, d.kn[1], d.kper[1], F1);
         if (ok0) {
@@ -585,8 +581,8 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
             float UL[NV], UR[NV], F[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                UL[v] = fv[T::fvy(slot, v, T::TY, c)];
-                UR[v] = fv[T::fvy(slot, v, T::TY + 1, c)];
+                UL[v] = fv[T::fvy(v, T::TY, c)];
+                UR[v] = fv[T::fvy(v, T::TY + 1, c)];
             }
             const float l = face_flux<SOLVER, 1>(mp, UL, UR, fj, d.kn[1], d.kper[1], F);
 #pragma unroll
@@ -601,8 +597,8 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
             float UL[NV], UR[NV], F[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                UL[v] = fv[T::fvx(slot, v, r, T::TX)];
-                UR[v] = fv[T::fvx(slot, v, r, T::TX + 1)];
+                UL[v] = fv[T::fvx(v, r, T::TX)];
+                UR[v] = fv[T::fvx(v, r, T::TX + 1)];
             }
             const float l = face_flux<SOLVER, 0>(mp, UL, UR, fi, d.kn[0], d.kper[0], F);
 #pragma unroll
@@ -618,7 +614,7 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
 template <class T, int SOLVER>
 __device__ __forceinline__ void residual3(const ProbDesc& d, const Item3& it, const float* sm,
                                           float* __restrict__ Rout, int k, const float (&fdn)[NV + 1],
-                                          const float (&fup)[NV + 1], float4 own, float& srmax, float (&nrm)[NV]) {
+                                          const float (&fup)[NV + 1], float& srmax, float (&nrm)[NV]) {
     const float* ff = sm + T::OFF_FX / 4;
     const AxisGeo gz = d.kgeo[2][k + d.kgoff[2]];
     const float hz = gz.h, ihz = gz.ih;
@@ -647,9 +643,13 @@ __device__ __forceinline__ void residual3(const ProbDesc& d, const Item3& it, co
     const MixPhys& mp = d.mp;
     const float vol = fsz * hz;
     if (mp.force || mp.accel) {
-        const float ro = own.x;
+        // the own cell's working state of plane k
+        const float* smw = sm + T::OFF_W / 4;
+        const int box = (cx + HB3) + (cy + HB3) * T::BX, s0 = T::wslot(k);
+        const float ro = smw[T::w(s0, 0, box)];
         const float iro = 1.0f / ro;
-        const float vu = own.y * iro, vv = own.z * iro, vw = own.w * iro;
+        const float vu = smw[T::w(s0, 1, box)] * iro, vv = smw[T::w(s0, 2, box)] * iro,
+                    vw = smw[T::w(s0, 3, box)] * iro;
         if (mp.force) {
             R[1] += vol * mp.sigma[0];
             R[2] += vol * mp.sigma[1];
@@ -667,13 +667,16 @@ __device__ __forceinline__ void residual3(const ProbDesc& d, const Item3& it, co
 #pragma unroll
         for (int v = 0; v < NV; ++v) nrm[v] += vol * fabsf(R[v]);
     }
-    const long long o = it.own_off + (long long)k * d.kstr[2];
-    const long long plane = d.L.plane;
+    const unsigned int o = (unsigned int)it.own_off + (unsigned int)k * (unsigned int)d.kstr[2];
+    const unsigned int plane = (unsigned int)d.L.plane;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) __stcs(Rout + v * plane + o, R[v]);
+    for (int v = 0; v < NV; ++v) __stcs(Rout + (o + v * plane), R[v]);
 }
 
-// One work item: the tile column (i0, j0) over planes [z0, z1).
+// One work item: the tile column (i0, j0) over planes [z0, z1).  Planes
+// z0-2 .. z1+1 are loaded.  Pass k (two phases, one barrier each):
+//   A: conversion of plane k+2; x/y faces of plane k;
+//   B: slopes of plane k+1; z face k / k+1; residual of plane k.
 template <class T, int SOLVER, int KIND>
 __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, const Item3& it, int par, float dtf,
                                       unsigned char* smem, uint64_t* bar, unsigned int& phase, float& srmax,
@@ -684,7 +687,7 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
     float* __restrict__ Rout = d.R[par ^ 1];
     float* sm = reinterpret_cast<float*>(smem);
     float* smw = sm + T::OFF_W / 4;
-    const int z0 = it.z0, z1 = it.z1, last = z1 + 1;  // planes z0-2 .. z1+1 are loaded
+    const int z0 = it.z0, z1 = it.z1, last = z1 + 1;
     volatile unsigned int* fail = reinterpret_cast<volatile unsigned int*>(smem + T::OFF_FAIL);
     // after a wait gave up (seen by every thread at the next barrier), no
     // thread waits and no load is issued again: no arrival on a barrier
@@ -703,47 +706,28 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
     auto issue = [&](int j) {
         if (lead && !*fail) issue_plane<T>(d, maps, par, smem, bar, stage_of(j), it.i0, it.j0, j);
     };
-    W5 wa[2], wb[2], wc[2];  // working copy of planes k, k+1, k+2 (per position)
-    W5 urx, ury, ulz, urz;   // own cell: right x/y states of plane k, z states
-    float4 own4 = make_float4(1.0f, 0.0f, 0.0f, 0.0f), own_k = own4;
-    float fdn[NV + 1], fup[NV + 1];
+    W5 urx, ury, ulz, urz;  // own cell: right-hand x/y states of the last reconstructed plane, z states
+    float fdn[NV + 1], fup[NV + 1];  // z-face fluxes below and above the plane of the residual
 #pragma unroll
     for (int v = 0; v <= NV; ++v) fdn[v] = fup[v] = 0.0f;
 
     issue(z0 - 2);
     issue(z0 - 1);
-    convert<T>(d, it, wait_stage(z0 - 2), Uin, Rin, Uout, smw, z0 - 2, dtf, wa, health);
-    __syncthreads();
-    issue(z0);
-    convert<T>(d, it, wait_stage(z0 - 1), Uin, Rin, Uout, smw, z0 - 1, dtf, wb, health);
-    __syncthreads();
-    issue(z0 + 1);
-    // wa = W(z0-2), wb = W(z0-1): shift so that (wa, wb, wc) = (k, k+1, k+2) with k = z0-2
-    convert<T>(d, it, wait_stage(z0), Uin, Rin, Uout, smw, z0, dtf, wc, health);
-    __syncthreads();
-    if (z0 + 2 <= last) issue(z0 + 2);
-    // slopes of plane z0-1 (k = z0-2: wa, wb, wc = planes z0-2, z0-1, z0)
-    reconstruct<T, KIND>(d, it, sm, z0 - 1, wa, wc, urx, ury, ulz, urz, own4);
-#pragma unroll
-    for (int p = 0; p < 2; ++p) { wa[p] = wb[p]; wb[p] = wc[p]; }
-    __syncthreads();
+    // one loop for the start-up passes too (k = z0-4 .. z0-2 convert planes
+    // z0-2 .. z0 and reconstruct plane z0-1): a single copy of each phase
+    // keeps the kernel's code small
 #pragma unroll 1
-    for (int k = z0 - 1; k <= z1; ++k) {
-        // phase A: conversion of plane k+2; residual of plane k-1
-        if (k + 2 <= last) convert<T>(d, it, wait_stage(k + 2), Uin, Rin, Uout, smw, k + 2, dtf, wc, health);
-        if (k - 1 >= z0 && it.own) residual3<T, SOLVER>(d, it, sm, Rout, k - 1, fdn, fup, own_k, srmax, nrm);
+    for (int k = z0 - 4; k < z1; ++k) {
+        // phase A
+        convert<T>(d, it, wait_stage(k + 2), Uin, Rin, Uout, smw, k + 2, dtf, health);
+        if (k >= z0) faces_xy<T, SOLVER>(d, it, sm, k, urx, ury);
         __syncthreads();
         if (k + 4 <= last) issue(k + 4);
-        if (k == z1) break;
-        // phase B (wa, wb, wc = planes k, k+1, k+2): x/y faces of plane k,
-        // slopes of plane k+1, z face k / k+1
-        if (k >= z0) faces_xy<T, SOLVER>(d, it, sm, k, urx, ury);
-        own_k = own4;
+        if (k < z0 - 2) continue;  // k + 1 < z0 - 1: nothing to reconstruct yet
+        // phase B
         const W5 ulz_k = ulz;
-        reconstruct<T, KIND>(d, it, sm, k + 1, wa, wc, urx, ury, ulz, urz, own4);
-        if (it.own) {
-#pragma unroll
-            for (int v = 0; v <= NV; ++v) fdn[v] = fup[v];
+        reconstruct<T, KIND>(d, it, sm, k + 1, urx, ury, ulz, urz);
+        if (k >= z0 - 1 && it.own) {
             float UL[NV], UR[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
@@ -751,9 +735,10 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
                 UR[v] = urz.v[v];
             }
             fup[NV] = face_flux<SOLVER, 2>(d.mp, UL, UR, k + 1, d.kn[2], d.kper[2], fup);
-        }
+            if (k >= z0) residual3<T, SOLVER>(d, it, sm, Rout, k, fdn, fup, srmax, nrm);
 #pragma unroll
-        for (int p = 0; p < 2; ++p) { wa[p] = wb[p]; wb[p] = wc[p]; }
+            for (int v = 0; v <= NV; ++v) fdn[v] = fup[v];
+        }
         __syncthreads();
     }
 }
@@ -786,7 +771,7 @@ __device__ __forceinline__ void close3(const ProbDesc& d, int n_closes, float sr
 }
 
 template <int TX, int TY, int SOLVER, int KIND>
-__global__ void __launch_bounds__(TX * TY, 2) k_mix3d(const __grid_constant__ ProbDesc d,
+__global__ void __launch_bounds__(TX * TY, TX * TY <= 256 ? 2 : 1) k_mix3d(const __grid_constant__ ProbDesc d,
                                                       const __grid_constant__ Mix3dMaps maps) {
     using T = Tile3<TX, TY>;
     // all shared memory is dynamic, so the TMA stages start 128-byte aligned
@@ -822,7 +807,7 @@ __global__ void __launch_bounds__(TX * TY, 2) k_mix3d(const __grid_constant__ Pr
 // ---------------------------------------------------------------------------
 // Host side
 // ---------------------------------------------------------------------------
-#define TS_MIX3D_TILES(X) X(32, 8) X(16, 16)
+#define TS_MIX3D_TILES(X) X(32, 8) X(16, 16) X(32, 16)
 
 template <class F>
 bool with3d(int tx, int ty, int solver, int kind, F&& f) {
@@ -900,6 +885,8 @@ bool mix3d_tile_info(int tx, int ty, int solver, int recon, int limiter, size_t*
 ts_status mix3d_make_maps(const ProbDesc& d, int tx, int ty, Mix3dMaps& maps, std::string& err) {
     const Layout& L = d.L;
     if (L.nd != 3 || L.gx != HB3 || L.gy != HB3 || L.gz != HB3) { err = "3D layout expected"; return TS_ERR_INVALID; }
+    // the kernel addresses the five variable planes with 32-bit element offsets
+    if ((unsigned long long)L.plane * NV >= (1ULL << 32)) { err = "grid too large for the 3D mixed kernel"; return TS_ERR_INVALID; }
     const int bx = tx + 2 * HB3, by = ty + 2 * HB3;
     ts_status s;
     for (int b = 0; b < 2; ++b) {
