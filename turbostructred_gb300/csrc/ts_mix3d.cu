@@ -1,5 +1,5 @@
 // Mixed-precision fused stage kernel for 3D problems on GB300: TMA-staged
-// planes, per-column values in registers.
+// planes, shared working-state planes, per-column face fluxes in registers.
 //
 // The arithmetic is the mixed path's (FP32 reconstruction, EOS and Riemann
 // flux; FP64 state, stage accumulation and dt; deferred update: the kernel of
@@ -17,21 +17,21 @@
 //    non-periodic side are the mirrored cells of the same box (the boundary
 //    image is applied in the conversion), halo cells on a periodic side
 //    (edge tiles only) are read directly from global memory.
-//  * Per-column registers.  Every thread owns one cell of the tile; 80
-//    threads also own one cell of the 1-cell ring around it (the cells the
-//    tile's faces need) and 84 one of the 2-cell frame (the ring cells'
-//    neighbours).  The working copy (FP32) of a thread's cells at planes
-//    k, k+1, k+2 stays in registers, so the z neighbours of the
-//    reconstruction and both states of the z face come from registers; the
-//    z-face flux is used by the same thread for the residuals of planes k
-//    and k+1, so it never touches shared memory either.  Only in-plane
-//    neighbours go through shared memory: the working copy of the plane
-//    being reconstructed, the face states W + dx / W + dy of the ring, and
-//    the x/y face fluxes.
+//  * Positions.  Every thread owns one cell of the tile; 80 threads also
+//    own one cell of the 1-cell ring around it (the cells the tile's faces
+//    need) and 84 one of the 2-cell frame (the ring cells' neighbours).  The
+//    FP32 working copy of three planes (k, k+1, k+2) is kept in shared
+//    memory, so the reconstruction reads its in-plane and z neighbours
+//    there; the reconstruction writes the face states W + dx / W + dy of the
+//    cells left of / below a face to shared memory and keeps the own cell's
+//    other face states in registers.  The z face between planes k and k+1
+//    is solved by the thread that owns the column, and its flux serves the
+//    residuals of planes k and k+1 from registers.
 //  * Per plane k, two phases separated by barriers: (A) convert plane k+2
-//    (FP64 U + dt R / V -> FP32 working copy, U^{n+1} for owned cells) and
-//    form the residual of plane k-1; (B) x/y faces of plane k, the limited
-//    slopes of plane k+1, and the z faces between k and k+1.
+//    (FP64 U + dt R / V -> FP32 working copy) and solve the x/y faces of
+//    plane k; (B) the owned cell's FP64 update U^{n+1} of plane k+2 (its
+//    FP64 adds overlap the FP32 work that follows), the limited slopes of
+//    plane k+1, the z face between k and k+1, and the residual of plane k.
 //
 // Waits on an mbarrier are bounded: a wait that gives up sets
 // TS_HEALTH_TIMEOUT in the problem's health word and the kernel runs on
@@ -194,6 +194,17 @@ struct RPos {
 // Working copy of the state of one position (FP32, shifted energy).
 struct W5 {
     float v[NV];
+};
+
+// The owned cell's FP64 update U^{n+1} = U^n + dt R^n / V of the plane just
+// converted: formed after the barrier that ends the conversion phase, where
+// the FP64 adds (a slow pipe on GB300) overlap FP32 work instead of
+// holding every warp at the barrier.
+struct PendingU {
+    double u[NV];
+    float inc[NV];
+    unsigned int off;  // element offset of the cell
+    bool on;
 };
 
 // Reconstruction kinds (the limiter choice folded in), as the general kernel.
@@ -383,7 +394,7 @@ __device__ __forceinline__ void issue_plane(const ProbDesc& d, const Mix3dMaps& 
 template <class T>
 __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, const unsigned char* stage,
                                         const double* __restrict__ Uin, const float* __restrict__ Rin,
-                                        double* __restrict__ Uout, float* smw, int j, float dtf,
+                                        double* __restrict__ Uout, float* smw, int j, float dtf, PendingU& pu,
                                         unsigned int& health) {
     const MixPhys& mp = d.mp;
     const double* su = reinterpret_cast<const double*>(stage);
@@ -430,21 +441,34 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
         if (zs >= 0) bc32(mp, zs, 2, w);
 #pragma unroll
         for (int v = 0; v < NV; ++v) smw[T::w(slot, v, c.wbox)] = w[v];
-        if (p == 0 && own_plane && it.own) {
-            const unsigned int o = (unsigned int)it.own_off + (unsigned int)j * (unsigned int)d.kstr[2];
-            double un[NV];
+        if (p == 0) {
+            pu.on = own_plane && it.own;
+            pu.off = (unsigned int)it.own_off + (unsigned int)j * (unsigned int)d.kstr[2];
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                un[v] = u[v] + f32_to_f64(inc[v]);
-                __stcs(Uout + (o + v * plane), un[v]);
+                pu.u[v] = u[v];
+                pu.inc[v] = inc[v];
             }
-            // rho > 0 tested on the bit pattern (no FP64 comparison)
-            const long long b = __double_as_longlong(un[0]);
-            if (b <= 0 || b > 0x7FF0000000000000LL)
-                health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
-            if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
+            if (pu.on && !(w[4] == w[4])) health |= TS_HEALTH_NAN;
         }
     }
+}
+
+// U^{n+1} of the owned cell of the last converted plane, written in FP64.
+__device__ __forceinline__ void apply_pending(const ProbDesc& d, double* __restrict__ Uout, const PendingU& pu,
+                                              unsigned int& health) {
+    if (!pu.on) return;
+    const unsigned int plane = (unsigned int)d.L.plane;
+    double un[NV];
+#pragma unroll
+    for (int v = 0; v < NV; ++v) {
+        un[v] = pu.u[v] + f32_to_f64(pu.inc[v]);
+        __stcs(Uout + (pu.off + v * plane), un[v]);
+    }
+    // rho > 0 tested on the bit pattern (no FP64 comparison)
+    const long long b = __double_as_longlong(un[0]);
+    if (b <= 0 || b > 0x7FF0000000000000LL)
+        health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
 }
 
 // Limited slopes of plane j at the thread's reconstruction positions (the
@@ -706,6 +730,8 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
     auto issue = [&](int j) {
         if (lead && !*fail) issue_plane<T>(d, maps, par, smem, bar, stage_of(j), it.i0, it.j0, j);
     };
+    PendingU pu;
+    pu.on = false;
     W5 urx, ury, ulz, urz;  // own cell: right-hand x/y states of the last reconstructed plane, z states
     float fdn[NV + 1], fup[NV + 1];  // z-face fluxes below and above the plane of the residual
 #pragma unroll
@@ -719,10 +745,12 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
 #pragma unroll 1
     for (int k = z0 - 4; k < z1; ++k) {
         // phase A
-        convert<T>(d, it, wait_stage(k + 2), Uin, Rin, Uout, smw, k + 2, dtf, health);
+        convert<T>(d, it, wait_stage(k + 2), Uin, Rin, Uout, smw, k + 2, dtf, pu, health);
         if (k >= z0) faces_xy<T, SOLVER>(d, it, sm, k, urx, ury);
         __syncthreads();
         if (k + 4 <= last) issue(k + 4);
+        // the owned cell's FP64 update of plane k+2 overlaps the work below
+        apply_pending(d, Uout, pu, health);
         if (k < z0 - 2) continue;  // k + 1 < z0 - 1: nothing to reconstruct yet
         // phase B
         const W5 ulz_k = ulz;
