@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define TS_FVM_ABI_VERSION 4
+#define TS_FVM_ABI_VERSION 5
 
 typedef enum ts_status {
     TS_OK = 0,
@@ -100,10 +100,15 @@ typedef struct ts_bc_config {
     double temperature;
 } ts_bc_config;
 
+/* Extra boundary-condition configurations a position-dependent side can
+   select (ts_config.bc_kinds). */
+#define TS_MAX_BC_KINDS 8
+
 /* KernelConfiguration (KernelConfiguration.h:21-93) with its
    MethodConfiguration (MethodConfiguration.h:26-37), reduced to the fields the
    explicit inviscid step reads.  One BC per domain side, in the order
-   x-, x+, y-, y+, z-, z+ (the reference's trivial-marker DomainBCinfo). */
+   x-, x+, y-, y+, z-, z+ (the reference's trivial-marker DomainBCinfo),
+   unless the side has a marker array (see bc_marker below). */
 typedef struct ts_config {
     int32_t abi_version;   /* TS_FVM_ABI_VERSION */
     int32_t n_dims;        /* nDims */
@@ -149,6 +154,25 @@ typedef struct ts_config {
        residual.  The FP64 path always forms them. */
     int32_t residual_norms;
     double viscosity;              /* Viscosity */
+    /* Position-dependent boundary conditions: a domain side carrying several
+       BCs (DomainBCinfo::isComplex and getMarker,
+       BoundaryConditionConfiguration.h:43-66, honoured by
+       Kernel::InitBoundaryConditions, kernel.h:284-316).  bc_kinds[0 ..
+       n_bc_kinds) are further BC configurations (the reference's
+       MyConditions entries).  A side whose bc_marker[side] is non-NULL takes,
+       at each of its boundary faces, bc_kinds[bc_marker[side][f]] in place of
+       bc[side]; the caller evaluates its marker function at the faces'
+       centres (as ComputeResidual does, ExplicitRungeKuttaFVM.h:1193-1209)
+       and the same marker serves the ghost cells of that face's row.  Faces
+       f are numbered by the side's two tangential cell indices, the lower
+       axis fastest: x sides j + ny*k, y sides i + nx*k, z sides i + nx*j
+       (ny*nz, nx*nz, nx*ny entries; inactive axes have one cell).  The arrays
+       are copied by ts_create.  Single problems only (batches, served solves
+       and ts_advance_noalloc refuse them with TS_ERR_UNSUPPORTED). */
+    int32_t n_bc_kinds;
+    int32_t reserved4;
+    ts_bc_config bc_kinds[TS_MAX_BC_KINDS];
+    const uint8_t* bc_marker[6];
 } ts_config;
 
 /* StepInfo (kernel.h:31-39) plus a health word. */

@@ -187,6 +187,21 @@ static void bc_dummy_values(const orc_config* c, int side, const double* in, vec
     }
 }
 
+/* BC table entry of the boundary face of `side` in the row of cell (i, j, k)
+   (values-array indices; the tangential ones identify the face): the side's
+   own BC, or for a position-dependent side the kind its marker function gave
+   at the face's centre (Kernel::InitBoundaryConditions kernel.h:284-316,
+   BCinfo::getMarker BCGeneral.h:52-56). */
+static int bc_entry(const orc_ctx* w, int side, int i, int j, int k) {
+    const unsigned char* m = w->c->bc_marker[side];
+    if (!m) return side;
+    const int a = side / 2;
+    const int ii = i - w->imin, jj = j - w->jmin, kk = k - w->kmin;
+    const int nx = w->c->nx, ny = w->c->ndims > 1 ? w->c->ny : 1;
+    const int f = a == 0 ? jj + ny * kk : (a == 1 ? ii + nx * kk : ii + nx * jj);
+    return 6 + m[f];
+}
+
 /* ExchangeValues (kernel.h:334-690) on one rank, then ComputeDummyCellValues
    (kernel.h:693-915): periodic axes copy the opposite interior layer, other
    axes apply the side's BC to the mirror cell with faceNormalL on both sides
@@ -206,8 +221,8 @@ static void fill_ghosts(orc_ctx* w, double* U) {
                 memcpy(lo, last, sizeof(double) * NV);
             } else {
                 vec3 nl = {-1.0, 0.0, 0.0};
-                bc_dummy_values(c, 0, first, nl, out); memcpy(lo, out, sizeof out);
-                bc_dummy_values(c, 1, last, nl, out); memcpy(hi, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 0, w->imin, j, k), first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 1, w->imax, j, k), last, nl, out); memcpy(hi, out, sizeof out);
             }
         }
     if (c->ndims < 2) return;
@@ -222,8 +237,8 @@ static void fill_ghosts(orc_ctx* w, double* U) {
                 memcpy(lo, last, sizeof(double) * NV);
             } else {
                 vec3 nl = {0.0, -1.0, 0.0};
-                bc_dummy_values(c, 2, first, nl, out); memcpy(lo, out, sizeof out);
-                bc_dummy_values(c, 3, last, nl, out); memcpy(hi, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 2, i, w->jmin, k), first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 3, i, w->jmax, k), last, nl, out); memcpy(hi, out, sizeof out);
             }
         }
     if (c->ndims < 3) return;
@@ -238,8 +253,8 @@ static void fill_ghosts(orc_ctx* w, double* U) {
                 memcpy(lo, last, sizeof(double) * NV);
             } else {
                 vec3 nl = {0.0, 0.0, -1.0};
-                bc_dummy_values(c, 4, first, nl, out); memcpy(lo, out, sizeof out);
-                bc_dummy_values(c, 5, last, nl, out); memcpy(hi, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 4, i, j, w->kmin), first, nl, out); memcpy(lo, out, sizeof out);
+                bc_dummy_values(c, bc_entry(w, 5, i, j, w->kmax), last, nl, out); memcpy(hi, out, sizeof out);
             }
         }
 }
@@ -797,7 +812,7 @@ static void dummy_gradient(orc_ctx* w, const double* U, int a, int side, int i, 
     vec3 n = {a == 0 ? (side ? 1.0 : -1.0) : 0.0, a == 1 ? (side ? 1.0 : -1.0) : 0.0,
               a == 2 ? (side ? 1.0 : -1.0) : 0.0};
     double du[NV], Vf[NV];
-    bc_dummy_values(c, 2 * a + side, Vin, n, du);
+    bc_dummy_values(c, bc_entry(w, 2 * a + side, i, j, k), Vin, n, du);
     for (int v = 0; v < NV; ++v) Vf[v] = 0.5 * (Vin[v] + du[v]);
     /* stencil: the cell, its neighbours along the other active axes, the ghost */
     int st[7][3], m = 0;
@@ -977,10 +992,10 @@ static void residual_line(orc_ctx* w, int a, int p, int q) {
         double hr = -0.5 * hh[s];
         if (s == lo && !c->periodic[a]) {
             sample(w, cp, a, hr, UR);
-            bc_dummy_values(c, 2 * a, UR, fn, UL);
+            bc_dummy_values(c, bc_entry(w, 2 * a, i, j, k), UR, fn, UL);
         } else if (s == hi + 1 && !c->periodic[a]) {
             sample(w, cm, a, hl, UL);
-            bc_dummy_values(c, 2 * a + 1, UL, fn, UR);
+            bc_dummy_values(c, bc_entry(w, 2 * a + 1, i, j, k), UL, fn, UR);
         } else {
             sample(w, cm, a, hl, UL);
             sample(w, cp, a, hr, UR);

@@ -24,6 +24,8 @@ extern "C" {
 #endif
 
 #define ORC_MAX_BLOCKS 16
+#define ORC_MAX_BC_KINDS 8
+#define ORC_BC_IDS (6 + ORC_MAX_BC_KINDS)
 
 enum { ORC_RECON_PWC = 0, ORC_RECON_LINEAR2 = 1, ORC_RECON_ENO2 = 2, ORC_RECON_LINEAR2_LIM = 3 };
 enum { ORC_LIM_BJ = 0, ORC_LIM_VENKAT = 1 };
@@ -49,10 +51,12 @@ typedef struct {
     double eps, cfl;
     int max_iteration;
     double max_time, save_solution_time, save_slice_time;
-    /* Per side xL,xR,yL,yR,zL,zR: BoundaryConditionType and its parameters
+    /* BC table: entries 0-5 per side xL,xR,yL,yR,zL,zR, entries 6.. the
+       extra kinds (KernelConfiguration::MyConditions entries): a
+       BoundaryConditionType and its parameters
        (BoundaryConditionConfiguration.h:21-35). */
-    int bc_type[6];
-    double bc_density[6], bc_velocity[6][3], bc_pstatic[6];
+    int bc_type[ORC_BC_IDS];
+    double bc_density[ORC_BC_IDS], bc_velocity[ORC_BC_IDS][3], bc_pstatic[ORC_BC_IDS];
     int threads; /* OpenMP threads (0 = runtime default) */
     /* Source terms: IsExternalForceRequared with Sigma, IsUnifromAccelerationRequared
        with UniformAcceleration (KernelConfiguration.h:50-51,87-88). */
@@ -63,6 +67,11 @@ typedef struct {
        (ExplicitRungeKuttaFVM.h:1239-1248). */
     int viscous;
     double viscosity;
+    /* Position-dependent sides (DomainBCinfo::isComplex / getMarker,
+       BoundaryConditionConfiguration.h:43-66): per boundary face the extra
+       kind (entry 6 + marker) it takes, faces numbered by the tangential
+       interior cell indices, lower axis fastest; NULL: the side's own BC. */
+    const unsigned char* bc_marker[6];
 } orc_config;
 
 typedef struct {

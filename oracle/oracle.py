@@ -27,6 +27,8 @@ LIB_PATH = os.path.join(HERE, "liboracle.so")
 REF_RUN = os.path.join(HERE, "_ref", "ref_run")
 
 MAX_BLOCKS = 16
+MAX_BC_KINDS = 8
+BC_IDS = 6 + MAX_BC_KINDS
 
 # Enum values: MethodConfiguration.h:5-23, BoundaryConditionConfiguration.h:12-19
 RECON_PWC, RECON_LINEAR2, RECON_ENO2, RECON_LINEAR2_LIM = 0, 1, 2, 3
@@ -50,14 +52,15 @@ class OrcConfig(C.Structure):
         ("eps", C.c_double), ("cfl", C.c_double),
         ("max_iteration", C.c_int),
         ("max_time", C.c_double), ("save_solution_time", C.c_double), ("save_slice_time", C.c_double),
-        ("bc_type", C.c_int * 6),
-        ("bc_density", C.c_double * 6),
-        ("bc_velocity", (C.c_double * 3) * 6),
-        ("bc_pstatic", C.c_double * 6),
+        ("bc_type", C.c_int * BC_IDS),
+        ("bc_density", C.c_double * BC_IDS),
+        ("bc_velocity", (C.c_double * 3) * BC_IDS),
+        ("bc_pstatic", C.c_double * BC_IDS),
         ("threads", C.c_int),
         ("external_force", C.c_int), ("uniform_acceleration", C.c_int),
         ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
         ("viscous", C.c_int), ("viscosity", C.c_double),
+        ("bc_marker", C.POINTER(C.c_ubyte) * 6),
     ]
 
 
@@ -112,7 +115,8 @@ def make_case(**kw) -> dict:
                 gamma=1.4, eos=EOS_IDEAL, p_inf=0.0, recon=RECON_PWC, limiter=LIM_BJ, solver=RS_ROE,
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
                 save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
-                external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0)
+                external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0,
+                bc_kinds=[], bc_split={})
     case.update(kw)
     return case
 
@@ -132,7 +136,7 @@ def to_struct(case: dict, threads: int = 0) -> OrcConfig:
     c.eps, c.cfl = case["eps"], case["cfl"]
     c.max_iteration, c.max_time = case["max_iter"], case["max_time"]
     c.save_solution_time, c.save_slice_time = case["save_solution_time"], case["save_slice_time"]
-    for s, (t, dens, vel, ps) in enumerate(case["bc"]):
+    for s, (t, dens, vel, ps) in enumerate(list(case["bc"]) + list(case.get("bc_kinds", []))):
         c.bc_type[s], c.bc_density[s], c.bc_pstatic[s] = t, dens, ps
         for a in range(3):
             c.bc_velocity[s][a] = vel[a]
@@ -145,7 +149,35 @@ def to_struct(case: dict, threads: int = 0) -> OrcConfig:
             getattr(c, vec)[a] = v[a] if v is not None else 0.0
     c.viscous = int(bool(case.get("viscous", False)))
     c.viscosity = float(case.get("viscosity", 0.0))
+    c._markers = []
+    if case.get("bc_split"):
+        for side, arr in split_markers(case).items():
+            c._markers.append(arr)
+            c.bc_marker[side] = arr.ctypes.data_as(C.POINTER(C.c_ubyte))
     return c
+
+
+def split_markers(case: dict) -> dict:
+    """Per-face markers of the case's split sides: case["bc_split"] maps a
+    side (0..5) to (axis, pos, kind_lo, kind_hi); a boundary face whose
+    centre lies below pos along the tangential `axis` takes kind_lo, the
+    others kind_hi.  Face centres' tangential coordinates are the cell
+    centres of the oracle's own grid (the reference evaluates its marker
+    function at the face centre, ExplicitRungeKuttaFVM.h:1193-1209)."""
+    nd = case["ndims"]
+    x, _, y, _, z, _ = grid(dict(case, bc_split={}))
+    centres = [x[1:-1], y[1:-1] if nd > 1 else y[:1], z[1:-1] if nd > 2 else z[:1]]
+    out = {}
+    for side, (axis, pos, lo, hi) in case["bc_split"].items():
+        a = side // 2
+        t = [b for b in range(3) if b != a]
+        if axis not in t:
+            raise ValueError("the split axis must be tangential to the side")
+        cp, cq = centres[t[0]], centres[t[1]]
+        coord = cp[:, None] if axis == t[0] else cq[None, :]
+        m = np.where(coord < pos, lo, hi) * np.ones((len(cp), len(cq)), dtype=np.int64)
+        out[side] = np.ascontiguousarray(m.T.reshape(-1), dtype=np.uint8)
+    return out
 
 
 def dims(case: dict):
@@ -246,6 +278,10 @@ def _ref_config_text(case: dict, ic_path: str, out_path: str, toro: int = 0, ste
     for s, name in enumerate(["bc_xl", "bc_xr", "bc_yl", "bc_yr", "bc_zl", "bc_zr"]):
         t, dens, vel, ps = case["bc"][s]
         lines.append(f"{name} {t} {dens!r} {vel[0]!r} {vel[1]!r} {vel[2]!r} {ps!r}")
+    for m, (t, dens, vel, ps) in enumerate(case.get("bc_kinds", [])):
+        lines.append(f"bc_kind {m} {t} {dens!r} {vel[0]!r} {vel[1]!r} {vel[2]!r} {ps!r}")
+    for side, (axis, pos, lo, hi) in sorted(case.get("bc_split", {}).items()):
+        lines.append(f"bc_split {side} {axis} {pos!r} {lo} {hi}")
     if case.get("external_force") is not None:
         lines.append("external_force " + " ".join(repr(float(v)) for v in case["external_force"]))
     if case.get("uniform_acceleration") is not None:

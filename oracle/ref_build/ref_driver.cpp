@@ -13,6 +13,10 @@
 //   eps cfl rk_order max_iter max_time save_solution_time save_slice_time
 //   bc_xl|bc_xr|bc_yl|bc_yr|bc_zl|bc_zr  type [density vx vy vz pstatic]
 //       (type = BoundaryConditionType value, BoundaryConditionConfiguration.h:12-19)
+//   bc_kind m type [density vx vy vz pstatic]   (extra MyConditions entry, marker 100+m)
+//   bc_split side axis pos m_lo m_hi   (side 0..5 = x-,x+,y-,y+,z-,z+ made complex:
+//       DomainBCinfo::isComplex with getMarker(r) = r[axis] < pos ? 100+m_lo : 100+m_hi,
+//       BoundaryConditionConfiguration.h:43-66, as src/Tests/2DTests/BlasiusFlow.h:115-120)
 //   blocks_x|blocks_y|blocks_z  n  pos q ncells  pos q ncells ...
 //   ic_file path   (interior cells, x fastest then y then z, 5 doubles each)
 //   out_file path
@@ -62,6 +66,29 @@ void set_bc(KernelConfiguration& conf, DomainBCinfo& side, int marker, const std
     side.SetMarker(marker);
 }
 
+void set_kind(KernelConfiguration& conf, const std::vector<std::string>& w) {
+    BoundaryConditionConfiguration bc((BoundaryConditionType)std::stoi(w[2]));
+    bc.Density = w.size() > 3 ? std::stod(w[3]) : 0.0;
+    bc.Velocity = Vector(w.size() > 4 ? std::stod(w[4]) : 0.0, w.size() > 5 ? std::stod(w[5]) : 0.0,
+                         w.size() > 6 ? std::stod(w[6]) : 0.0);
+    bc.Pstatic = w.size() > 7 ? std::stod(w[7]) : 0.0;
+    conf.MyConditions[100 + std::stoi(w[1])] = bc;
+}
+
+void set_split(KernelConfiguration& conf, const std::vector<std::string>& w) {
+    DomainBCinfo* sides[6] = {&conf.xLeftBoundary, &conf.xRightBoundary, &conf.yLeftBoundary,
+                              &conf.yRightBoundary, &conf.zLeftBoundary, &conf.zRightBoundary};
+    DomainBCinfo& side = *sides[std::stoi(w[1])];
+    const int axis = std::stoi(w[2]);
+    const double pos = std::stod(w[3]);
+    const int lo = 100 + std::stoi(w[4]), hi = 100 + std::stoi(w[5]);
+    side.isComplex = true;
+    side.getMarker = [axis, pos, lo, hi](const Vector r) {
+        const double c = axis == 0 ? r.x : (axis == 1 ? r.y : r.z);
+        return c < pos ? lo : hi;
+    };
+}
+
 DriverConfig parse(const char* path) {
     DriverConfig d;
     KernelConfiguration& c = d.conf;
@@ -106,6 +133,8 @@ DriverConfig parse(const char* path) {
         else if (k == "bc_yr") set_bc(c, c.yRightBoundary, 4, w);
         else if (k == "bc_zl") set_bc(c, c.zLeftBoundary, 5, w);
         else if (k == "bc_zr") set_bc(c, c.zRightBoundary, 6, w);
+        else if (k == "bc_kind") set_kind(c, w);
+        else if (k == "bc_split") set_split(c, w);
         else if (k == "blocks_x" || k == "blocks_y" || k == "blocks_z") {
             int a = k[7] - 'x';
             int n = I(1);

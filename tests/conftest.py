@@ -27,6 +27,8 @@ def load_golden(name):
     case["length"] = tuple(case["length"])
     case["bc"] = [(t, dens, tuple(vel), ps) for t, dens, vel, ps in case["bc"]]
     case["blocks"] = {int(k): [tuple(b) for b in v] for k, v in case.get("blocks", {}).items()}
+    case["bc_kinds"] = [(t, dens, tuple(vel), ps) for t, dens, vel, ps in case.get("bc_kinds", [])]
+    case["bc_split"] = {int(k): tuple(v) for k, v in case.get("bc_split", {}).items()}
     d["case"] = case
     d["meta"] = meta
     d["iteration"] = int(d["scalars"][0])

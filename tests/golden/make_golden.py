@@ -114,6 +114,19 @@ def cases():
                     max_time=1e30, external_force=(0.0, 0.2, -0.1), uniform_acceleration=(0.1, 0.0, -0.5),
                     bc=[SYM] * 6)
     out.append(("sources3d_both", c, ("scenario", T.SCENARIO_BLAST, 21, [1.0, 0.5, 2.0, 0.3, 0.01]), 8))
+    # position-dependent sides (DomainBCinfo::isComplex / getMarker): a plate
+    # on the bottom side from x = 0.3 on (Symmetry before it, Wall after, as
+    # src/Tests/2DTests/BlasiusFlow.h:115-120), inlet on the left
+    c = O.make_case(ndims=2, nx=32, ny=16, periodic=(0, 0, 1), recon=O.RECON_LINEAR2_LIM, solver=O.RS_ROE,
+                    cfl=0.4, eps=0.05, max_iter=10**6, max_time=1e9, bc=[INLET, NAT, NAT, NAT, NAT, NAT],
+                    bc_kinds=[SYM, WALL], bc_split={2: (0, 0.3, 0, 1)})
+    out.append(("marker2d_plate", c, ("scenario", T.SCENARIO_SHEAR_LAYER, 31, [1.2, 1.0, 0.4, 2.0, 0.02]), 20))
+    # 3D: the z-low side split along y (Wall below y = 0.45, moving wall
+    # above), the x-high side split along z (Natural / Symmetry)
+    c = O.make_case(ndims=3, nx=12, ny=10, nz=8, periodic=(0, 0, 0), recon=O.RECON_LINEAR2_LIM,
+                    solver=O.RS_ROE, cfl=0.4, max_iter=10**6, max_time=1e9, bc=[SYM, NAT, SYM, SYM, NAT, NAT],
+                    bc_kinds=[WALL, MOVW, NAT, SYM], bc_split={4: (1, 0.45, 0, 1), 1: (2, 0.55, 2, 3)})
+    out.append(("marker3d_split", c, ("scenario", T.SCENARIO_BLAST, 32, [1.0, 0.5, 3.0, 0.3, 0.01]), 8))
     # HLLC and the stiffened gas are not in the reference: no fixture.
     return out
 
@@ -137,10 +150,19 @@ def initial_state(case, spec):
 
 
 def main():
+    """python tests/golden/make_golden.py [name ...]: all cases, or the named
+    ones (merged into index.json)."""
     if not O.ref_available():
         sys.exit("oracle/_ref/ref_run is not built (make -C oracle/ref_build)")
+    only = set(sys.argv[1:])
     index = {}
+    ipath = os.path.join(HERE, "index.json")
+    if only and os.path.exists(ipath):
+        with open(ipath) as f:
+            index = json.load(f)
     for name, case, spec, steps in cases():
+        if only and name not in only:
+            continue
         ic = initial_state(case, spec)
         toro = spec[1] if spec[0] == "toro" else 0
         r = O.run_reference(case, ic, toro=toro, steps=steps)
@@ -156,7 +178,7 @@ def main():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)
         index[name] = dict(iteration=r["iteration"], time=r["time"], seconds=r["seconds"])
         print(f"{name:24s} iterations {r['iteration']:5d} t {r['time']!r}")
-    with open(os.path.join(HERE, "index.json"), "w") as f:
+    with open(ipath, "w") as f:
         json.dump(index, f, indent=1, sort_keys=True)
 
 

@@ -123,3 +123,37 @@ def test_oracle_scenarios_equal_the_library_scenarios(nd, scenario, params, tsli
     b = oracle_mod.fill_scenario(case, scenario, 2024, params)
     assert a.shape == b.shape
     assert np.array_equal(a, b)
+
+
+@pytest.mark.parametrize("name", ["marker2d_plate", "marker3d_split"])
+def test_split_markers_equal_the_oracles(name, tslib, oracle_mod):
+    """Per-face BC markers of a split side, from the library's grid and from
+    the oracle's, are the same arrays (the reference's marker function
+    evaluated at the face centres gives the fixture's results)."""
+    from turbostructred_gb300 import capi
+    g = load_golden(name)
+    case = g["case"]
+    a = capi.split_markers(capi.make_case(**case))
+    b = oracle_mod.split_markers(case)
+    assert sorted(a) == sorted(b) and len(a) > 0
+    for side in a:
+        assert np.array_equal(a[side], b[side])
+        assert len(set(a[side].tolist())) == 2  # the split falls inside the side
+
+
+def test_markers_are_validated(tslib):
+    """Markers beyond n_bc_kinds, or on a periodic side, are refused; batches
+    refuse position-dependent sides."""
+    from turbostructred_gb300 import capi
+    nat = (capi.BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)
+    case = capi.make_case(ndims=2, nx=8, ny=6, periodic=(0, 0, 1), bc=[nat] * 6, bc_kinds=[nat],
+                          bc_split={2: (0, 0.5, 0, 1)})
+    cfg, keep = capi.to_config(case, capi.PRECISION_MIXED)
+    assert tslib.ts_batch_problem_bytes(C.byref(cfg)) == 0  # kind 1 does not exist
+    case = dict(case, bc_kinds=[nat, nat])
+    cfg, keep = capi.to_config(case, capi.PRECISION_MIXED)
+    assert tslib.ts_batch_problem_bytes(C.byref(cfg)) == 0  # valid, but batches take no markers
+    cfg.periodic[1] = 1  # the split side becomes periodic
+    null = C.POINTER(C.c_double)()
+    assert tslib.ts_grid_coordinates(C.byref(cfg), *([null] * 6)) == 1
+    assert b"periodic" in tslib.ts_last_error()

@@ -18,7 +18,8 @@ import numpy as np
 PKG = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(PKG, "libtsfvm.so")
 
-ABI_VERSION = 4
+ABI_VERSION = 5
+MAX_BC_KINDS = 8
 
 # enum values (include/ts_fvm.h)
 RECON_PWC, RECON_LINEAR2, RECON_ENO2, RECON_LINEAR2_LIM = 0, 1, 2, 3
@@ -64,6 +65,8 @@ class Config(C.Structure):
         ("external_force", C.c_int32), ("uniform_acceleration", C.c_int32),
         ("sigma", C.c_double * 3), ("acceleration", C.c_double * 3),
         ("viscous", C.c_int32), ("residual_norms", C.c_int32), ("viscosity", C.c_double),
+        ("n_bc_kinds", C.c_int32), ("reserved4", C.c_int32), ("bc_kinds", BcConfig * MAX_BC_KINDS),
+        ("bc_marker", C.POINTER(C.c_uint8) * 6),
     ]
 
 
@@ -225,7 +228,7 @@ def make_case(**kw) -> dict:
                 eps=0.0, cfl=0.25, max_iter=1000, max_time=1.0, save_solution_time=0.0,
                 save_slice_time=0.0, bc=[(BC_NATURAL, 0.0, (0.0, 0.0, 0.0), 0.0)] * 6,
                 external_force=None, uniform_acceleration=None, viscous=False, viscosity=0.0,
-                residual_norms=False)
+                residual_norms=False, bc_kinds=[], bc_split={})
     case.update(kw)
     return case
 
@@ -269,7 +272,51 @@ def to_config(case: dict, precision: int = PRECISION_FP64, device: int = 0):
     c.viscous = int(bool(case.get("viscous", False)))
     c.viscosity = float(case.get("viscosity", 0.0))
     c.residual_norms = int(bool(case.get("residual_norms", False)))
+    # position-dependent sides: extra BC kinds and per-face markers
+    kinds = case.get("bc_kinds", [])
+    c.n_bc_kinds = len(kinds)
+    for m, (t, dens, vel, ps) in enumerate(kinds):
+        c.bc_kinds[m].type, c.bc_kinds[m].density, c.bc_kinds[m].pstatic = t, dens, ps
+        for a in range(3):
+            c.bc_kinds[m].velocity[a] = vel[a]
+    if case.get("bc_split"):
+        for side, arr in split_markers(case, c).items():
+            keep.append(arr)
+            c.bc_marker[side] = arr.ctypes.data_as(C.POINTER(C.c_uint8))
     return c, keep
+
+
+def split_markers(case: dict, cfg=None) -> dict:
+    """Per-face marker arrays of the case's split sides.  case["bc_split"]
+    maps a side (0..5: x-, x+, y-, y+, z-, z+) to (axis, pos, kind_lo,
+    kind_hi): a boundary face whose centre's coordinate along the tangential
+    `axis` is below pos takes bc_kinds[kind_lo], the others
+    bc_kinds[kind_hi] -- a marker function like the reference's
+    DomainBCinfo::getMarker, evaluated at the faces' centres.  Faces are
+    numbered as ts_config.bc_marker expects (x sides j + ny k, y sides
+    i + nx k, z sides i + nx j)."""
+    if cfg is None:
+        cfg, _ = to_config(dict(case, bc_split={}))
+    nd = case["ndims"]
+    nx, ny, nz = case["nx"], case["ny"] if nd > 1 else 1, case["nz"] if nd > 2 else 1
+    arrs = [np.zeros(n) for n in (nx + 2, nx + 2, (ny + 2) if nd > 1 else 1, (ny + 2) if nd > 1 else 1,
+                                  (nz + 2) if nd > 2 else 1, (nz + 2) if nd > 2 else 1)]
+    P = C.POINTER(C.c_double)
+    check(load().ts_grid_coordinates(C.byref(cfg), *[a.ctypes.data_as(P) for a in arrs]))
+    centres = [arrs[0][1:-1] if nd >= 1 else arrs[0], arrs[2][1:-1] if nd > 1 else arrs[2][:1],
+               arrs[4][1:-1] if nd > 2 else arrs[4][:1]]
+    out = {}
+    for side, (axis, pos, lo, hi) in case["bc_split"].items():
+        a = side // 2
+        t = [b for b in range(3) if b != a]          # tangential axes, lower first
+        if axis not in t:
+            raise ValueError("the split axis must be tangential to the side")
+        # face (p, q): p along t[0] (fastest), q along t[1]
+        cp, cq = centres[t[0]], centres[t[1]]
+        coord = cp[:, None] if axis == t[0] else cq[None, :]
+        m = np.where(coord < pos, lo, hi) * np.ones((len(cp), len(cq)), dtype=np.int64)
+        out[side] = np.ascontiguousarray(m.T.reshape(-1), dtype=np.uint8)
+    return out
 
 
 def interior_shape(case: dict):

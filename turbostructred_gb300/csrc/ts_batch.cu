@@ -573,7 +573,7 @@ size_t ts_batch_problem_bytes(const ts_config* cfg) {
     if (!cfg) return 0;
     std::string err;
     if (validate_config(*cfg, err) != TS_OK) return 0;
-    if (cfg->n_dims > 2 || cfg->precision != TS_PRECISION_MIXED) return 0;
+    if (cfg->n_dims > 2 || cfg->precision != TS_PRECISION_MIXED || has_markers(*cfg)) return 0;
     return problem_bytes(make_layout(*cfg));
 }
 
@@ -581,6 +581,7 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
     if (!b || !cfg || !values || !id) return fail(TS_ERR_INVALID, "NULL argument");
     if (cfg->precision != TS_PRECISION_MIXED) return fail(TS_ERR_UNSUPPORTED, "batches run the mixed-precision step");
     if (cfg->n_dims > 2) return fail(TS_ERR_UNSUPPORTED, "batches hold 1D and 2D problems");
+    if (has_markers(*cfg)) return fail(TS_ERR_UNSUPPORTED, "batches take one boundary condition per side (no bc_marker)");
     HostGrid grid;
     std::string err;
     ts_status s = build_grid(*cfg, grid, err);

@@ -75,6 +75,7 @@ __global__ void k_gather(double* __restrict__ aos, Layout L, const double* __res
 struct ts_handle {
     ts_config cfg{};
     std::vector<ts_block_node> blocks[3];
+    std::vector<uint8_t> marks[6];  // copies of the per-face BC markers
     Layout L{};
     Phys ph{};
     HostGrid grid;
@@ -276,6 +277,7 @@ ts_status ts_create(const ts_config* cfg, ts_handle** out) {
     *out = nullptr;
     std::unique_ptr<ts_handle> h(new ts_handle());
     h->cfg = *cfg;
+    for (int sd = 0; sd < 6; ++sd) h->cfg.bc_marker[sd] = nullptr;  // copied once the sizes are checked
     for (int a = 0; a < 3; ++a) {
         if (cfg->n_blocks[a] > 0 && cfg->blocks[a]) {
             h->blocks[a].assign(cfg->blocks[a], cfg->blocks[a] + cfg->n_blocks[a]);
@@ -288,6 +290,14 @@ ts_status ts_create(const ts_config* cfg, ts_handle** out) {
     std::string err;
     ts_status s = build_grid(h->cfg, h->grid, err);
     if (s != TS_OK) return fail(s, err);
+    for (int sd = 0; sd < 6; ++sd) {
+        if (!cfg->bc_marker[sd]) continue;
+        if (sd >= 2 * h->cfg.n_dims || h->cfg.periodic[sd / 2])
+            return fail(TS_ERR_INVALID, "bc_marker on a periodic or inactive side");
+        h->marks[sd].assign(cfg->bc_marker[sd], cfg->bc_marker[sd] + side_faces(h->cfg, sd));
+        h->cfg.bc_marker[sd] = h->marks[sd].data();
+    }
+    if ((s = validate_config(h->cfg, err)) != TS_OK) return fail(s, err);
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0)
         return fail(TS_ERR_CUDA, "no CUDA device available");
@@ -297,6 +307,15 @@ ts_status ts_create(const ts_config* cfg, ts_handle** out) {
     h->L = make_layout(h->cfg);
     h->ph = make_phys(h->cfg);
     TS_CUDA(cudaStreamCreateWithFlags(&h->stream, cudaStreamNonBlocking));
+    // per-face BC markers on the device (read by the ghost, face and
+    // conversion code of both paths)
+    for (int sd = 0; sd < 6; ++sd) {
+        if (h->marks[sd].empty()) continue;
+        uint8_t* dm = nullptr;
+        if ((s = h->alloc(&dm, h->marks[sd].size())) != TS_OK) return s;
+        TS_CUDA(cudaMemcpyAsync(dm, h->marks[sd].data(), h->marks[sd].size(), cudaMemcpyHostToDevice, h->stream));
+        h->ph.bc.mark[sd] = dm;
+    }
     TS_CUDA(cudaMallocHost(&h->ctl_h, sizeof(Ctl)));
     std::memset(h->ctl_h, 0, sizeof(Ctl));
     Ctl& c = *h->ctl_h;

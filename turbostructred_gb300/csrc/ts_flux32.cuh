@@ -50,7 +50,11 @@ __device__ __forceinline__ void resolve(int idx, int n, int periodic, int side_l
     }
 }
 
-// Boundary-condition image of a state (shifted energy) across `side`.
+// BC table entry of boundary face f of `side` (ts_internal.h: face_index).
+__device__ __forceinline__ int bc_id32(const MixPhys& p, int side, int f) { return bc_id(p.mark, side, f); }
+
+// Boundary-condition image of a state (shifted energy) for BC table entry
+// `side` (a domain side, or the kind its marker selected) on axis A.
 __device__ __forceinline__ void bc32(const MixPhys& p, int side, int A, float w[NV]) {
     const int t = p.bc_type[side];
     if (t == TS_BC_SYMMETRY) {

@@ -116,6 +116,20 @@ ts_status validate_config(const ts_config& c, std::string& err) {
         if (c.periodic[s / 2]) continue;
         if (c.bc[s].type < TS_BC_WALL || c.bc[s].type > TS_BC_NATURAL) { err = "unknown boundary condition"; return TS_ERR_INVALID; }
     }
+    if (c.n_bc_kinds < 0 || c.n_bc_kinds > TS_MAX_BC_KINDS) { err = "n_bc_kinds out of range"; return TS_ERR_INVALID; }
+    for (int k = 0; k < c.n_bc_kinds; ++k)
+        if (c.bc_kinds[k].type < TS_BC_WALL || c.bc_kinds[k].type > TS_BC_NATURAL) {
+            err = "unknown boundary condition in bc_kinds"; return TS_ERR_INVALID;
+        }
+    for (int s = 0; s < 6; ++s) {
+        if (!c.bc_marker[s]) continue;
+        if (s >= 2 * c.n_dims || c.periodic[s / 2]) {
+            err = "bc_marker on a periodic or inactive side"; return TS_ERR_INVALID;
+        }
+        const long long nf = side_faces(c, s);
+        for (long long f = 0; f < nf; ++f)
+            if (c.bc_marker[s][f] >= c.n_bc_kinds) { err = "bc_marker entry beyond n_bc_kinds"; return TS_ERR_INVALID; }
+    }
     if (c.precision != TS_PRECISION_FP64 && c.precision != TS_PRECISION_MIXED) { err = "unknown precision"; return TS_ERR_INVALID; }
     if (!(c.viscosity >= 0.0) || !std::isfinite(c.viscosity)) { err = "viscosity must be finite and >= 0"; return TS_ERR_INVALID; }
     if ((c.viscous || c.viscosity != 0.0) && c.precision != TS_PRECISION_FP64) {
@@ -167,12 +181,17 @@ Phys make_phys(const ts_config& c) {
     p.p_inf = c.eos == TS_EOS_STIFFENED_GAS ? c.p_inf : 0.0;
     p.eps = c.eps;
     p.cfl = c.cfl;
-    for (int s = 0; s < 6; ++s) {
-        p.bc.type[s] = c.bc[s].type;
-        p.bc.density[s] = c.bc[s].density;
-        for (int a = 0; a < 3; ++a) p.bc.vel[s][a] = c.bc[s].velocity[a];
-        p.bc.pstatic[s] = c.bc[s].pstatic;
+    for (int id = 0; id < kBcIds; ++id) {
+        const bool side = id < 6;
+        if (!side && id - 6 >= c.n_bc_kinds) continue;
+        const ts_bc_config& b = side ? c.bc[id] : c.bc_kinds[id - 6];
+        p.bc.type[id] = b.type;
+        p.bc.density[id] = b.density;
+        for (int a = 0; a < 3; ++a) p.bc.vel[id][a] = b.velocity[a];
+        p.bc.pstatic[id] = b.pstatic;
     }
+    // device marker arrays are set by their owner after the upload
+    for (int s = 0; s < 6; ++s) p.bc.mark[s] = nullptr;
     p.viscous = c.viscous != 0;
     p.visc = c.viscosity;
     p.force = c.external_force != 0;

@@ -45,13 +45,43 @@ struct Layout {
 
 Layout make_layout(const ts_config& c);
 
-// Boundary conditions of the six domain sides (x-, x+, y-, y+, z-, z+).
+// Boundary conditions: entries 0-5 are the six domain sides' own BCs (x-,
+// x+, y-, y+, z-, z+), entries 6.. the extra kinds a position-dependent side
+// selects face by face through its marker array (device memory; null for a
+// side with one BC).
+constexpr int kBcIds = 6 + TS_MAX_BC_KINDS;
 struct BcSet {
-    int type[6];
-    double density[6];
-    double vel[6][3];
-    double pstatic[6];
+    int type[kBcIds];
+    double density[kBcIds];
+    double vel[kBcIds][3];
+    double pstatic[kBcIds];
+    const uint8_t* mark[6];
 };
+
+// BC table entry of boundary face f of `side` (faces numbered by the side's
+// tangential cell indices, lower axis fastest: x sides j + ny k, y sides
+// i + nx k, z sides i + nx j).
+TS_HD int bc_id(const uint8_t* const mark[6], int side, int f) {
+    const uint8_t* m = mark[side];
+    return m ? 6 + (int)m[f] : side;
+}
+TS_HD int face_index(int side, int i, int j, int k, int nx, int ny) {
+    const int a = side >> 1;
+    return a == 0 ? j + ny * k : (a == 1 ? i + nx * k : i + nx * j);
+}
+
+// Boundary faces of a side (the length of its marker array).
+inline long long side_faces(const ts_config& c, int side) {
+    const long long nx = c.nx, ny = c.n_dims > 1 ? c.ny : 1, nz = c.n_dims > 2 ? c.nz : 1;
+    const int a = side >> 1;
+    return a == 0 ? ny * nz : (a == 1 ? nx * nz : nx * ny);
+}
+// A config with at least one position-dependent side.
+inline bool has_markers(const ts_config& c) {
+    for (int s = 0; s < 6; ++s)
+        if (c.bc_marker[s]) return true;
+    return false;
+}
 
 // Physics and method selection passed by value to kernels.
 struct Phys {

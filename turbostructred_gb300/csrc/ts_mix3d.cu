@@ -436,9 +436,22 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
 #pragma unroll
         for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
         w[4] = f64_to_f32(e4) + inc[4];
-        if (c.xs >= 0) bc32(mp, c.xs, 0, w);
-        if (c.ys >= 0) bc32(mp, c.ys, 1, w);
-        if (zs >= 0) bc32(mp, zs, 2, w);
+        if ((c.xs | c.ys | zs) >= 0) {
+            // a halo cell beyond a non-periodic side: the BC of the boundary
+            // face of its row (source cell indices recovered from the box or
+            // the plane offset; halo cells only)
+            int si, sj;
+            if (c.sbox >= 0) {
+                si = c.sbox % T::BX + it.i0 - HB3;
+                sj = c.sbox / T::BX + it.j0 - HB3;
+            } else {
+                si = c.goff % (int)d.kstr[1];
+                sj = c.goff / (int)d.kstr[1];
+            }
+            if (c.xs >= 0) bc32(mp, bc_id32(mp, c.xs, sj + d.kn[1] * sk), 0, w);
+            if (c.ys >= 0) bc32(mp, bc_id32(mp, c.ys, si + d.kn[0] * sk), 1, w);
+            if (zs >= 0) bc32(mp, bc_id32(mp, zs, si + d.kn[0] * sj), 2, w);
+        }
 #pragma unroll
         for (int v = 0; v < NV; ++v) smw[T::w(slot, v, c.wbox)] = w[v];
         if (p == 0) {
@@ -548,15 +561,17 @@ __device__ __forceinline__ void reconstruct(const ProbDesc& d, const Item3& it, 
 // non-periodic domain face: g == 0 or g == n), stored at `out` (stride vs).
 template <int SOLVER, int A>
 __device__ __forceinline__ float face_flux(const MixPhys& mp, float UL[NV], float UR[NV], int g, int n, int per,
-                                           float F[NV]) {
+                                           int f, float F[NV]) {
+    // f: the face's index on its side (tangential cell indices), for a
+    // position-dependent side's marker
     if (g == 0 && !per) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) UL[v] = UR[v];
-        bc32(mp, 2 * A, A, UL);
+        bc32(mp, bc_id32(mp, 2 * A, f), A, UL);
     } else if (g == n && !per) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) UR[v] = UL[v];
-        bc32(mp, 2 * A + 1, A, UR);
+        bc32(mp, bc_id32(mp, 2 * A + 1, f), A, UR);
     }
     return flux32<SOLVER, A>(mp, UL, UR, F);
 }
@@ -583,8 +598,8 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
         // hold and not stored
         const bool ok0 = gi <= d.kn[0] && gj < d.kn[1];
         const bool ok1 = gi < d.kn[0] && gj <= d.kn[1];
-        const float l0 = face_flux<SOLVER, 0>(mp, UL0, UR0, gi, d.kn[0], d.kper[0], F0);
-        const float l1 = face_flux<SOLVER, 1>(mp, UL1, UR1, gj, d.kn[1], d.kper[1], F1);
+        const float l0 = face_flux<SOLVER, 0>(mp, UL0, UR0, gi, d.kn[0], d.kper[0], gj + d.kn[1] * k, F0);
+        const float l1 = face_flux<SOLVER, 1>(mp, UL1, UR1, gj, d.kn[1], d.kper[1], gi + d.kn[0] * k, F1);
         if (ok0) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) ff[T::fx(v, it.cy, it.cx)] = F0[v];
@@ -608,7 +623,7 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
                 UL[v] = fv[T::fvy(v, T::TY, c)];
                 UR[v] = fv[T::fvy(v, T::TY + 1, c)];
             }
-            const float l = face_flux<SOLVER, 1>(mp, UL, UR, fj, d.kn[1], d.kper[1], F);
+            const float l = face_flux<SOLVER, 1>(mp, UL, UR, fj, d.kn[1], d.kper[1], fi + d.kn[0] * k, F);
 #pragma unroll
             for (int v = 0; v < NV; ++v) ff[T::fy(v, T::TY, c)] = F[v];
             ff[T::fy(NV, T::TY, c)] = l;
@@ -624,7 +639,7 @@ __device__ __forceinline__ void faces_xy(const ProbDesc& d, const Item3& it, flo
                 UL[v] = fv[T::fvx(v, r, T::TX)];
                 UR[v] = fv[T::fvx(v, r, T::TX + 1)];
             }
-            const float l = face_flux<SOLVER, 0>(mp, UL, UR, fi, d.kn[0], d.kper[0], F);
+            const float l = face_flux<SOLVER, 0>(mp, UL, UR, fi, d.kn[0], d.kper[0], fj + d.kn[1] * k, F);
 #pragma unroll
             for (int v = 0; v < NV; ++v) ff[T::fx(v, r, T::TX)] = F[v];
             ff[T::fx(NV, r, T::TX)] = l;
@@ -762,7 +777,8 @@ __device__ __forceinline__ void march(const ProbDesc& d, const Mix3dMaps& maps, 
                 UL[v] = ulz_k.v[v];
                 UR[v] = urz.v[v];
             }
-            fup[NV] = face_flux<SOLVER, 2>(d.mp, UL, UR, k + 1, d.kn[2], d.kper[2], fup);
+            fup[NV] = face_flux<SOLVER, 2>(d.mp, UL, UR, k + 1, d.kn[2], d.kper[2],
+                                           (it.i0 + it.cx) + d.kn[0] * (it.j0 + it.cy), fup);
             if (k >= z0) residual3<T, SOLVER>(d, it, sm, Rout, k, fdn, fup, srmax, nrm);
 #pragma unroll
             for (int v = 0; v <= NV; ++v) fdn[v] = fup[v];

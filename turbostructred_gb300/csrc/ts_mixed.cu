@@ -237,9 +237,11 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
         for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(pf[k].u[v]) + inc[v];
         w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf[k].u[4] - mp.einf_d) : f64_to_f32(pf[k].u[4])) +
                inc[4];
-        if (bp[k].xs >= 0) bc32(mp, bp[k].xs, 0, w);
-        if (T::HAS_Y && bp[k].ys >= 0) bc32(mp, bp[k].ys, 1, w);
-        if (T::MARCH && zs >= 0) bc32(mp, zs, phys_axis<T, 2>(), w);
+        // BC of the boundary face of this ghost's row (one-row tiles: the x
+        // sides' faces are numbered by the plane, the marching sides' by x)
+        static_assert(!T::HAS_Y, "one-row tiles only");
+        if (bp[k].xs >= 0) bc32(mp, bc_id32(mp, bp[k].xs, sk), 0, w);
+        if (T::MARCH && zs >= 0) bc32(mp, bc_id32(mp, zs, bp[k].off), phys_axis<T, 2>(), w);
 #pragma unroll
         for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp[k].box)] = w[v];
         if (own_plane && bp[k].own) {
@@ -487,14 +489,18 @@ __device__ __forceinline__ bool face_in(const ProbDesc& d, const float* sm, int 
         UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, SA, v, rl)]);
         UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, SA, v, rr)]);
     }
+    // boundary faces: the BC of this face (one-row tiles: an x face is
+    // numbered by its plane, a marching-axis face by its x index)
+    static_assert(!T::HAS_Y, "one-row tiles only");
+    const int f = AX == 0 ? z : gi;
     if (g == 0 && !per) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) UL[v] = UR[v];
-        bc32(d.mp, 2 * A, A, UL);
+        bc32(d.mp, bc_id32(d.mp, 2 * A, f), A, UL);
     } else if (g == n && !per) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) UR[v] = UL[v];
-        bc32(d.mp, 2 * A + 1, A, UR);
+        bc32(d.mp, bc_id32(d.mp, 2 * A + 1, f), A, UR);
     }
     return true;
 }
@@ -977,7 +983,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
             float w[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) w[v] = owner[T::w(0, v, opos)];
-            if (bp[0].xs >= 0) bc32(mp, bp[0].xs, 0, w);
+            if (bp[0].xs >= 0) bc32(mp, bc_id32(mp, bp[0].xs, 0), 0, w);
 #pragma unroll
             for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp[0].box)] = w[v];
         }
@@ -1370,7 +1376,7 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
     m.einf = (float)m.einf_d;
     m.eps = (float)ph.eps;
     m.cfl = ph.cfl;
-    for (int sd = 0; sd < 6; ++sd) {
+    for (int sd = 0; sd < kBcIds; ++sd) {
         m.bc_type[sd] = ph.bc.type[sd];
         const double r = ph.bc.density[sd];
         const double vx = ph.bc.vel[sd][0], vy = ph.bc.vel[sd][1], vz = ph.bc.vel[sd][2];
@@ -1382,6 +1388,7 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
         m.bc_state[sd][4] = (float)(ph.bc.pstatic[sd] / (ph.gamma - 1) + 0.5 * r * (vx * vx + vy * vy + vz * vz));
         for (int a = 0; a < 3; ++a) m.bc_vel[sd][a] = (float)ph.bc.vel[sd][a];
     }
+    for (int sd = 0; sd < 6; ++sd) m.mark[sd] = ph.bc.mark[sd];
     m.force = ph.force;
     m.accel = ph.accel;
     m.norms = c.residual_norms != 0;
@@ -1501,6 +1508,8 @@ extern "C" ts_status ts_advance_noalloc(const ts_config* cfg, const double* stat
     if (n_steps < 0) return fail(TS_ERR_INVALID, "n_steps must be >= 0");
     if (cfg->precision != TS_PRECISION_MIXED)
         return fail(TS_ERR_UNSUPPORTED, "ts_advance_noalloc runs the mixed-precision step only");
+    if (has_markers(*cfg))
+        return fail(TS_ERR_UNSUPPORTED, "ts_advance_noalloc takes one boundary condition per side (no bc_marker)");
     HostGrid grid;
     std::string err;
     ts_status s = build_grid(*cfg, grid, err);

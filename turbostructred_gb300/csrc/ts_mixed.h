@@ -31,9 +31,12 @@ struct MixPhys {
     float gamma, gm1, pinf, einf, eps;
     double einf_d;        // gamma p_inf / (gamma - 1): energy shift, applied in FP64
     double cfl;
-    int bc_type[6];
-    float bc_state[6][5];  // SubsonicInlet ghost state (shifted energy)
-    float bc_vel[6][3];    // MovingWall velocity
+    // BC table: the six sides' own BCs, then the extra kinds that
+    // position-dependent sides select per face through `mark`
+    int bc_type[kBcIds];
+    float bc_state[kBcIds][5];  // SubsonicInlet ghost state (shifted energy)
+    float bc_vel[kBcIds][3];    // MovingWall velocity
+    const uint8_t* mark[6];     // per-face kind of a position-dependent side (device), or null
     int force, accel;      // source terms on (kernel.h:941-989)
     float sigma[3], g[3];  // Sigma, UniformAcceleration
     int norms;             // form the residual norms sum V |R| (kernel.h:326)

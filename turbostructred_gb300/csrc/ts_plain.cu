@@ -31,7 +31,8 @@ namespace {
 __device__ __forceinline__ long long vidx(const Layout& L, int v) { return (long long)v * L.plane; }
 
 // ---------------------------------------------------------------------------
-// Boundary conditions (BCGeneral.h:186-268) for a normal sgn*e_A.
+// Boundary conditions (BCGeneral.h:186-268) for a normal sgn*e_A; `side` is
+// the BC table entry (the domain side, or the kind a marker selected).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ void bc_values(const Phys& ph, int side, int A, double sgn, const double in[NV],
                                           double out[NV]) {
@@ -446,17 +447,21 @@ __global__ void k_ghost(PlainBufs b, Phys ph) {
         return;
     }
     double in[NV], out[NV];
+    // the BC of this row's boundary face on each side (its marker, if the
+    // side is position-dependent: the same one for both ghost layers)
+    const int idl = bc_id(ph.bc.mark, 2 * A, face_index(2 * A, i, j, k, L.nx, L.ny));
+    const int idr = bc_id(ph.bc.mark, 2 * A + 1, face_index(2 * A + 1, i, j, k, L.nx, L.ny));
     // left side ghosts mirror cells 0 and 1; right side mirror n-1 and n-2
     // (ComputeDummyCellValues, kernel.h:731-765); faceNormalL on both sides.
     for (int layer = 1; layer <= GHOST; ++layer) {
 #pragma unroll
         for (int v = 0; v < NV; ++v) in[v] = U[vidx(L, v) + c0 + (long long)(layer - 1) * st];
-        bc_values(ph, 2 * A, A, -1.0, in, out);
+        bc_values(ph, idl, A, -1.0, in, out);
 #pragma unroll
         for (int v = 0; v < NV; ++v) U[vidx(L, v) + c0 - (long long)layer * st] = out[v];
 #pragma unroll
         for (int v = 0; v < NV; ++v) in[v] = U[vidx(L, v) + c0 + (long long)(n - layer) * st];
-        bc_values(ph, 2 * A + 1, A, -1.0, in, out);
+        bc_values(ph, idr, A, -1.0, in, out);
 #pragma unroll
         for (int v = 0; v < NV; ++v) U[vidx(L, v) + c0 + (long long)(n - 1 + layer) * st] = out[v];
     }
@@ -554,7 +559,8 @@ __device__ void dummy_gradient(const PlainBufs& b, const Phys& ph, int side, int
     double Vin[NV], du[NV], Vf[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) Vin[v] = b.U[vidx(L, v) + inner];
-    bc_values(ph, 2 * A + side, A, side ? 1.0 : -1.0, Vin, du);
+    bc_values(ph, bc_id(ph.bc.mark, 2 * A + side, face_index(2 * A + side, i, j, k, L.nx, L.ny)), A,
+              side ? 1.0 : -1.0, Vin, du);
 #pragma unroll
     for (int v = 0; v < NV; ++v) Vf[v] = 0.5 * (Vin[v] + du[v]);
     // stencil: the cell, its neighbours along the other active axes (+ then -), the ghost
@@ -788,10 +794,10 @@ __global__ void k_flux(PlainBufs b, Phys ph) {
     double UL[NV], UR[NV];
     if (s == 0 && !ph.periodic[A]) {
         sample(b, ph, cf, A, -0.5 * H[s + g0], UR);
-        bc_values(ph, 2 * A, A, 1.0, UR, UL);
+        bc_values(ph, bc_id(ph.bc.mark, 2 * A, face_index(2 * A, i, j, k, L.nx, L.ny)), A, 1.0, UR, UL);
     } else if (s == n && !ph.periodic[A]) {
         sample(b, ph, cf - st, A, 0.5 * H[s - 1 + g0], UL);
-        bc_values(ph, 2 * A + 1, A, 1.0, UL, UR);
+        bc_values(ph, bc_id(ph.bc.mark, 2 * A + 1, face_index(2 * A + 1, i, j, k, L.nx, L.ny)), A, 1.0, UL, UR);
     } else {
         // A ghost reconstruction on a periodic axis is the opposite interior
         // cell's object sampled with the ghost's own h (ExchangeReconstructions).

@@ -282,7 +282,8 @@ ts_status ts_server_submit(ts_server* s, const ts_config* cfg, const double* val
     if (bytes == 0) {
         std::string err;
         if (ts::validate_config(*cfg, err) != TS_OK) return ts::fail(TS_ERR_INVALID, err);
-        return ts::fail(TS_ERR_UNSUPPORTED, "served solves are 1D/2D mixed precision");
+        return ts::fail(TS_ERR_UNSUPPORTED,
+                        "served solves are 1D/2D mixed precision with one boundary condition per side");
     }
     if (bytes > s->budget) return ts::fail(TS_ERR_NO_MEMORY, "solve larger than the server's memory budget");
     Req r = std::make_shared<Request>();
