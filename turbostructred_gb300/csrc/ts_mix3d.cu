@@ -436,7 +436,7 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
 #pragma unroll
         for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
         w[4] = f64_to_f32(e4) + inc[4];
-        if ((c.xs | c.ys | zs) >= 0) {
+        if (c.xs >= 0 || c.ys >= 0 || zs >= 0) {
             // a halo cell beyond a non-periodic side: the BC of the boundary
             // face of its row (source cell indices recovered from the box or
             // the plane offset; halo cells only)
