@@ -621,14 +621,21 @@ def run_served(args, rank, ws, lr, dist, emit=True):
     lat = []
     done = threading.Event()
 
+    # served results kept for the error against the FP64 path: every 40th
+    # request of side <= 256
+    sample = {k for k, (_, c, _, _) in enumerate(reqs) if k % 40 == 0 and c["nx"] <= 256}
+    kept = {}
+
     def collector():
         k = 0
         while not (done.is_set() and k >= len(ids)):
             if k >= len(ids):
                 time.sleep(0.001)
                 continue
-            _, info, t = srv.wait(ids[k])
+            state, info, t = srv.wait(ids[k])
             lat.append((t["submit_s"], t["admit_s"], t["finish_s"], info["iteration"]))
+            if k in sample:
+                kept[k] = (state, info)
             k += 1
 
     th = threading.Thread(target=collector)
@@ -684,6 +691,7 @@ def run_served(args, rank, ws, lr, dist, emit=True):
                            "admission": {"order": args.order, "max_cells_in_flight": int(args.max_cells)}},
                 "latency_ms": {"p50": pct(lat_ms, 50), "p99": pct(lat_ms, 99), "max": lat_ms[-1] if lat_ms else None},
                 "admission_wait_ms": {"p50": pct(wait_ms, 50), "p99": pct(wait_ms, 99)},
+                "mixed_error_vs_fp64": served_errors(reqs, kept, lr),
                 "e2e": {"value": value, "unit": "cell-updates/s", "h2d_bytes_per_step": bytes_io / max(1, len(reqs)),
                         "d2h_bytes_per_step": bytes_io / max(1, len(reqs)),
                         "note": "latency and throughput are end to end: host submit (copy of the initial state) "
@@ -710,6 +718,24 @@ def run_served(args, rank, ws, lr, dist, emit=True):
         if emit:
             print(json.dumps(line), flush=True)
         return line
+
+
+def served_errors(reqs, kept, lr):
+    """Largest L1/Linf errors of sampled served results against the same
+    requests run alone on the FP64 path."""
+    from turbostructred_gb300 import capi, workloads
+    errs = []
+    for k, (state, info) in sorted(kept.items()):
+        _, case, params, seed = reqs[k]
+        with capi.Solver(case, capi.PRECISION_FP64, device=lr) as s:
+            s.set_state(workloads.stream_state(case, params, seed))
+            ref_info = s.run()
+            ref = s.get_state()
+        if ref_info["iteration"] == info["iteration"]:
+            errs.append(rel_errors(state.reshape(ref.shape), ref))
+    if not errs:
+        return None
+    return {"requests_sampled": len(errs), **{key: max(e[key] for e in errs) for key in errs[0]}}
 
 
 SHEAR = [2.0, 1.0, 0.5, 2.5, 0.01]  # rho_in, rho_out, u, p, noise
@@ -1006,8 +1032,12 @@ def main():
     p.add_argument("--max-cells", type=float, default=16e6)
     args = p.parse_args()
     if args.steps is None:
-        # the 3D blast's timed region spans ~0.7 s (several clock samples)
-        args.steps = 3 if args.workload == "tubes" else (500 if args.workload == "blast3d" else 200)
+        # the 3D blast's timed region spans ~0.5 s (several clock samples);
+        # the reference arm's CPU step of the whole 256^3 box takes ~0.7 s
+        if args.impl == "reference":
+            args.steps = 1 if args.workload == "tubes" else 20
+        else:
+            args.steps = 3 if args.workload == "tubes" else (500 if args.workload == "blast3d" else 200)
     if args.warmup is None:
         args.warmup = 3 if args.workload == "tubes" else 5
     if args.impl == "reference":

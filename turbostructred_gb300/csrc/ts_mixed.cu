@@ -858,7 +858,7 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
     } else {
         __shared__ ProbDesc sd;
         __shared__ int s_skip, s_par;
-        __shared__ double s_dt;
+        __shared__ float s_dtf;  // the pending dt, rounded to FP32 once per problem
         const int nwords = (int)(sizeof(ProbDesc) / sizeof(int));
         int cur = -1;
         for (int it = blockIdx.x; it < n_items; it += gridDim.x) {
@@ -870,7 +870,7 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
                     const Ctl& c = ctls[pq.x];
                     s_skip = c.stop_req;
                     s_par = c.parity;
-                    s_dt = c.dt_apply;
+                    s_dtf = __double2float_rn(c.dt_apply);
                 }
                 __syncthreads();
                 cur = pq.x;
@@ -878,7 +878,7 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
             if (s_skip) continue;
             float srmax = 0.0f, nrm[NV] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
             unsigned int health = 0;
-            process_item<T, SOLVER>(sd, pq.y, s_par, __double2float_rn(s_dt), sm, bp, pf, rp, srmax, health, nrm);
+            process_item<T, SOLVER>(sd, pq.y, s_par, s_dtf, sm, bp, pf, rp, srmax, health, nrm);
             if (close_in_kernel) close_item<T, true>(sd, srmax, health, nrm, wmax, whealth);
             else close_item<T, false>(sd, srmax, health, nrm, wmax, whealth);
         }
@@ -916,6 +916,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
     __shared__ unsigned int red[2][2];      // per stage parity: max bits, health (first CTA's are used)
     __shared__ Ctl sc;                      // this CTA's copy of the control word
     __shared__ int s_stop;
+    __shared__ float s_dtf;                 // sc.dt_apply rounded to FP32 (once per stage)
     const int tid = threadIdx.x;
     const unsigned int rank = cluster.block_rank();
     const ProbDesc& d = probs[list[blockIdx.x / cluster.num_blocks()]];
@@ -926,6 +927,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
     if (tid == 0) {
         sc = *d.ctl;
         s_stop = sc.stop_req;
+        s_dtf = __double2float_rn(sc.dt_apply);
     }
     const int kind = recon_kind(mp);
     const bool pwc = kind == 0;
@@ -957,7 +959,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
         unsigned int health = 0;
         // pending update of the own cell and its working copy (store())
         if (own) {
-            const float cf = bp[0].cfxy * (__double2float_rn(sc.dt_apply) * gz.ih);
+            const float cf = bp[0].cfxy * (s_dtf * gz.ih);
             float inc[NV], w[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
@@ -1018,6 +1020,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
             const unsigned int hh = slot[1];
             sc.health |= hh;
             finish_with(&sc, m, mp.cfl);
+            s_dtf = __double2float_rn(sc.dt_apply);
             // the first CTA clears the slots of the next stage (read by
             // nobody since the previous stage's second barrier)
             if (rank == 0) { red[(st + 1) & 1][0] = 0u; red[(st + 1) & 1][1] = 0u; }
