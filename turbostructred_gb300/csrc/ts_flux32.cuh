@@ -56,21 +56,24 @@ __device__ __forceinline__ int bc_id32(const MixPhys& p, int side, int f) { retu
 // Boundary-condition image of a state (shifted energy) for BC table entry
 // `side` (a domain side, or the kind its marker selected) on axis A.
 __device__ __forceinline__ void bc32(const MixPhys& p, int side, int A, float w[NV]) {
-    const int t = p.bc_type[side];
+    // entries 0-5 inline, 6.. from the extra-kinds table
+    const bool extra = side >= 6;
+    const int t = extra ? p.kinds->type[side - 6] : p.bc_type[side];
     if (t == TS_BC_SYMMETRY) {
         w[1 + A] = -w[1 + A];
     } else if (t == TS_BC_WALL) {
         w[1] = -w[1]; w[2] = -w[2]; w[3] = -w[3];
     } else if (t == TS_BC_MOVING_WALL) {
+        const float* bv = extra ? p.kinds->vel[side - 6] : p.bc_vel[side];
         const float r = w[0], ir = 1.0f / r;
         const float vx = w[1] * ir, vy = w[2] * ir, vz = w[3] * ir;
-        const float dx = 2.0f * p.bc_vel[side][0] - vx, dy = 2.0f * p.bc_vel[side][1] - vy,
-                    dz = 2.0f * p.bc_vel[side][2] - vz;
+        const float dx = 2.0f * bv[0] - vx, dy = 2.0f * bv[1] - vy, dz = 2.0f * bv[2] - vz;
         w[1] = r * dx; w[2] = r * dy; w[3] = r * dz;
         w[4] = w[4] + 0.5f * r * ((dx * dx + dy * dy + dz * dz) - (vx * vx + vy * vy + vz * vz));
     } else if (t == TS_BC_SUBSONIC_INLET) {
+        const float* bs = extra ? p.kinds->state[side - 6] : p.bc_state[side];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) w[v] = p.bc_state[side][v];
+        for (int v = 0; v < NV; ++v) w[v] = bs[v];
     }
 }
 

@@ -1379,19 +1379,38 @@ ts_status mixed_problem(const ts_config& c, const Layout& L, const Phys& ph, con
     m.einf = (float)m.einf_d;
     m.eps = (float)ph.eps;
     m.cfl = ph.cfl;
+    // the six sides' BCs inline; a position-dependent side's extra kinds in
+    // device memory
+    MixBcKinds kinds;
+    std::memset(&kinds, 0, sizeof kinds);
     for (int sd = 0; sd < kBcIds; ++sd) {
-        m.bc_type[sd] = ph.bc.type[sd];
         const double r = ph.bc.density[sd];
         const double vx = ph.bc.vel[sd][0], vy = ph.bc.vel[sd][1], vz = ph.bc.vel[sd][2];
-        m.bc_state[sd][0] = (float)r;
-        m.bc_state[sd][1] = (float)(r * vx);
-        m.bc_state[sd][2] = (float)(r * vy);
-        m.bc_state[sd][3] = (float)(r * vz);
-        // inlet ghost energy, shifted: p/(g-1) + rho|v|^2/2 (the p_inf terms cancel)
-        m.bc_state[sd][4] = (float)(ph.bc.pstatic[sd] / (ph.gamma - 1) + 0.5 * r * (vx * vx + vy * vy + vz * vz));
-        for (int a = 0; a < 3; ++a) m.bc_vel[sd][a] = (float)ph.bc.vel[sd][a];
+        // inlet ghost state, energy shifted: p/(g-1) + rho|v|^2/2 (the p_inf terms cancel)
+        const float inl[5] = {(float)r, (float)(r * vx), (float)(r * vy), (float)(r * vz),
+                             (float)(ph.bc.pstatic[sd] / (ph.gamma - 1) + 0.5 * r * (vx * vx + vy * vy + vz * vz))};
+        int* type = sd < 6 ? &m.bc_type[sd] : &kinds.type[sd - 6];
+        float* state = sd < 6 ? m.bc_state[sd] : kinds.state[sd - 6];
+        float* vel = sd < 6 ? m.bc_vel[sd] : kinds.vel[sd - 6];
+        *type = ph.bc.type[sd];
+        for (int v = 0; v < 5; ++v) state[v] = inl[v];
+        for (int a = 0; a < 3; ++a) vel[a] = (float)ph.bc.vel[sd][a];
     }
-    for (int sd = 0; sd < 6; ++sd) m.mark[sd] = ph.bc.mark[sd];
+    bool marked = false;
+    for (int sd = 0; sd < 6; ++sd) {
+        m.mark[sd] = ph.bc.mark[sd];
+        marked = marked || ph.bc.mark[sd];
+    }
+    m.kinds = nullptr;
+    if (marked) {
+        void* p;
+        if ((s = alloc(sizeof(MixBcKinds), &p)) != TS_OK) return s;
+        if (cudaMemcpyAsync(p, &kinds, sizeof kinds, cudaMemcpyHostToDevice, st) != cudaSuccess) {
+            err = "boundary-condition table upload failed";
+            return TS_ERR_CUDA;
+        }
+        m.kinds = static_cast<const MixBcKinds*>(p);
+    }
     m.force = ph.force;
     m.accel = ph.accel;
     m.norms = c.residual_norms != 0;

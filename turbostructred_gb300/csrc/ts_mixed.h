@@ -31,15 +31,24 @@ struct MixPhys {
     float gamma, gm1, pinf, einf, eps;
     double einf_d;        // gamma p_inf / (gamma - 1): energy shift, applied in FP64
     double cfl;
-    // BC table: the six sides' own BCs, then the extra kinds that
-    // position-dependent sides select per face through `mark`
-    int bc_type[kBcIds];
-    float bc_state[kBcIds][5];  // SubsonicInlet ghost state (shifted energy)
-    float bc_vel[kBcIds][3];    // MovingWall velocity
-    const uint8_t* mark[6];     // per-face kind of a position-dependent side (device), or null
+    // BC table: the six sides' own BCs (entries 0-5) inline; the extra kinds
+    // a position-dependent side selects per face through `mark` (entries
+    // 6..) in device memory, read only at such faces
+    int bc_type[6];
+    float bc_state[6][5];  // SubsonicInlet ghost state (shifted energy)
+    float bc_vel[6][3];    // MovingWall velocity
+    const uint8_t* mark[6];            // per-face kind of a position-dependent side (device), or null
+    const struct MixBcKinds* kinds;    // entries 6.. (device), or null
     int force, accel;      // source terms on (kernel.h:941-989)
     float sigma[3], g[3];  // Sigma, UniformAcceleration
     int norms;             // form the residual norms sum V |R| (kernel.h:326)
+};
+
+// The extra BC kinds of position-dependent sides (table entries 6..).
+struct MixBcKinds {
+    int type[TS_MAX_BC_KINDS];
+    float state[TS_MAX_BC_KINDS][5];
+    float vel[TS_MAX_BC_KINDS][3];
 };
 
 // Everything the fused kernel needs about one problem (lives in device memory).
