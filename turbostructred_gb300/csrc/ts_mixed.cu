@@ -107,12 +107,16 @@ struct Tile {
     static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TY * TX : 0);
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
     static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
-    // resident CTAs per SM the register allocation is sized for (about 24
-    // warps per SM for one-row tiles: sized for 16 warps, a single 1024^2
-    // problem ran 1.5 % faster but batches of problems 17 % slower; two CTAs
-    // per SM for the shared-memory-heavy two-axis tiles)
+    // resident CTAs per SM the register allocation is sized for: about 28
+    // warps per SM for one-row tiles that do not march (a 4096-tube batch
+    // took 2.00 s at 77 registers, 6 CTAs of 128 threads per SM, and 1.81 s
+    // sized for 28 warps), 24 for marching one-row tiles (which spill at 28;
+    // sized for 16 warps, a single 1024^2 problem ran 1.5 % faster but
+    // batches of problems 17 % slower), and two CTAs per SM for the
+    // shared-memory-heavy two-axis tiles
     static constexpr int WARPS = (NT + 31) / 32;
-    static constexpr int MINB = HAS_Y ? 2 : (WARPS >= 16 ? 2 : (24 + WARPS - 1) / WARPS);
+    static constexpr int MINB =
+        HAS_Y ? 2 : (WARPS >= 16 ? 2 : ((MARCH ? 24 : 28) + WARPS - 1) / WARPS);
 
     static __device__ __forceinline__ int wslot(int p) { return TWO_PHASE ? (p & 3) : (p + 3) % 3; }
     static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
