@@ -14,23 +14,22 @@
 // pass per step: 40 B FP64 read + 20 B FP32 read + 40 B + 20 B written per
 // cell-update.  A final apply pass materialises the state for the host.
 //
-// Work items.  A problem is cut into tile columns of TX x TY cells (x-y,
-// compile-time, one thread per tile cell) and, in 3D, z chunks; one item is
-// one (problem, column, chunk).  A CTA marches z through its item (2.5D
-// blocking), keeping a ring of the FP32 working state with a 2-cell halo
-// (four planes for 3D tiles, which run two phases per plane; three for the
-// one-row 1D/2D tiles, three phases), a 2-plane ring of limited half-slopes
-// with a 1-cell halo and the face fluxes in shared memory.  Every thread has
-// fixed roles: up to two working-state positions of the halo box (the next
-// plane's loads are issued into registers as soon as the current plane is
-// stored, so their latency hides behind the plane's compute), up to two
-// reconstruction positions (second rounds dealt from the last thread), the
-// x face left of its cell and the y face below (solved side by side), the z
-// face above (the tile's far faces go to the first and the last warp), and
-// its cell's residual.  Items are
-// indexed z-chunk-major and dealt round-robin to the persistent CTAs, so CTAs
-// running at the same time sweep neighbouring columns at the same z and share
-// halo rows through L2.  Each problem has its own control word: the CTA that
+// This file holds the 1D and 2D kernels (3D problems run the TMA-staged
+// k_mix3d of ts_mix3d.cu, on the same descriptors and control words).
+//
+// Work items.  A problem is cut into one-row tiles of TX cells along x (one
+// thread per cell plus two halo threads at each end) and, in 2D, chunks of
+// rows; one item is one (problem, tile, chunk).  A 2D item marches y through
+// its chunk (2.5D blocking), keeping three rows of the FP32 working state, a
+// 2-row ring of limited half-slopes and the face fluxes in shared memory.
+// Every thread has fixed roles: one working-state position of the row (the
+// next row's loads are issued into registers as soon as the current row is
+// stored, so their latency hides behind the row's compute), at most one
+// reconstruction position, the x face left of its cell (thread TX: the far
+// face), the y face above its cell, and its cell's residual.  Items are
+// indexed chunk-major and dealt round-robin to the persistent CTAs, so CTAs
+// running at the same time sweep neighbouring tiles at the same y and share
+// halo cells through L2.  Each problem has its own control word: the CTA that
 // completes a problem's last item turns its CFL maximum into that problem's
 // dt, so many problems of different sizes advance with their own time steps
 // in one launch.  The last few long 1D problems of a batch run in the
@@ -73,85 +72,67 @@ using namespace mix32;
 // axis (z in 3D, y in 2D).  ProbDesc maps each kernel axis to the problem's
 // geometry, extent, strides and physical direction.
 //
-// Two-axis tiles (3D): TX_ x TY_ threads own TX_ x TY_ cells.  One-row tiles
-// (1D, and 2D marching along y): TX_ threads own TX_ - 4 cells, so every
-// thread has exactly one box position, at most one reconstruction position
-// and at most one face per axis (no thread does a second round).
-template <int TX_, int TY_, bool MARCH_>
+// One-row tiles (1D problems, and 2D problems marching along y): NT_
+// threads own NT_ - 4 cells along x, so every thread has exactly one box
+// position, at most one reconstruction position and at most one face per
+// axis.  Kernel axis 1 of these problems is the inactive one (one cell).
+template <int NT_, bool MARCH_>
 struct Tile {
-    static constexpr bool HAS_Y = TY_ > 1;
     static constexpr bool MARCH = MARCH_;
-    static constexpr int NT = TX_ * TY_;
-    static constexpr int TX = HAS_Y ? TX_ : TX_ - 2 * HB;  // cells along x
-    static constexpr int TY = HAS_Y ? TY_ : 1;             // cells along kernel axis 1
-    static constexpr int NAX = 1 + (HAS_Y ? 1 : 0) + (MARCH ? 1 : 0);  // active axes
-    static constexpr int AZ = HAS_Y ? 2 : 1;               // slope slot of the marching axis
-    static constexpr int BX = TX + 2 * HB;                 // working-state box
-    static constexpr int BY = HAS_Y ? TY + 2 * HB : 1;
+    static constexpr int NT = NT_;
+    static constexpr int TX = NT - 2 * HB;                 // cells along x
+    static constexpr int NAX = MARCH ? 2 : 1;              // active axes: x and the marching axis
+    static constexpr int AZ = 1;                           // slope slot of the marching axis
+    static constexpr int BX = TX + 2 * HB;                 // working-state box (one position per thread)
     static constexpr int RX = TX + 2;                      // reconstruction ring
-    static constexpr int RY = HAS_Y ? TY + 2 : 1;
-    static constexpr int NBOX = BX * BY;
-    static constexpr int NRING = RX * RY;
-    static constexpr int NA = (NBOX + NT - 1) / NT;        // box positions per thread
-    static constexpr int NB = (NRING + NT - 1) / NT;       // ring positions per thread
-    // two-axis tiles march in two phases per plane (four working-state
-    // planes live), one-row tiles in three (three planes live)
-    static constexpr bool TWO_PHASE = HAS_Y && MARCH;
-    static constexpr int WS = MARCH ? (TWO_PHASE ? 4 : 3) : 1;  // working-state planes kept
+    static constexpr int WS = MARCH ? 3 : 1;               // working-state planes kept
     static constexpr int DS = MARCH ? 2 : 1;               // slope planes kept
     static constexpr int W_OFF = 0;
-    static constexpr int D_OFF = W_OFF + WS * NV * NBOX;
-    static constexpr int FX_OFF = D_OFF + DS * NAX * NV * NRING;
-    static constexpr int FY_OFF = FX_OFF + 6 * TY * (TX + 1);
-    static constexpr int FZ_OFF = FY_OFF + (HAS_Y ? 6 * (TY + 1) * TX : 0);
-    static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TY * TX : 0);
+    static constexpr int D_OFF = W_OFF + WS * NV * BX;
+    static constexpr int FX_OFF = D_OFF + DS * NAX * NV * RX;
+    static constexpr int FZ_OFF = FX_OFF + 6 * (TX + 1);
+    static constexpr int TOTAL = FZ_OFF + (MARCH ? 2 * 6 * TX : 0);
     static constexpr size_t BYTES = (size_t)TOTAL * sizeof(float);
-    static_assert(HAS_Y || NA == 1, "one-row tiles give every thread one box position");
+    static_assert(BX == NT && RX <= NT, "one box position and at most one ring position per thread");
     // resident CTAs per SM the register allocation is sized for: about 28
-    // warps per SM for one-row tiles that do not march (a 4096-tube batch
-    // took 2.00 s at 77 registers, 6 CTAs of 128 threads per SM, and 1.81 s
-    // sized for 28 warps), 24 for marching one-row tiles (which spill at 28;
-    // sized for 16 warps, a single 1024^2 problem ran 1.5 % faster but
-    // batches of problems 17 % slower), and two CTAs per SM for the
-    // shared-memory-heavy two-axis tiles
+    // warps per SM for tiles that do not march (a 4096-tube batch took 2.00 s
+    // at 77 registers, 6 CTAs of 128 threads per SM, and 1.81 s sized for 28
+    // warps), 24 for marching tiles (which spill at 28; sized for 16 warps, a
+    // single 1024^2 problem ran 1.5 % faster but batches of problems 17 %
+    // slower)
     static constexpr int WARPS = (NT + 31) / 32;
-    static constexpr int MINB =
-        HAS_Y ? 2 : (WARPS >= 16 ? 2 : ((MARCH ? 24 : 28) + WARPS - 1) / WARPS);
+    static constexpr int MINB = WARPS >= 16 ? 2 : ((MARCH ? 24 : 28) + WARPS - 1) / WARPS;
 
-    static __device__ __forceinline__ int wslot(int p) { return TWO_PHASE ? (p & 3) : (p + 3) % 3; }
-    static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * NBOX + box; }
+    static __device__ __forceinline__ int wslot(int p) { return (p + 3) % 3; }
+    static __device__ __forceinline__ int w(int s, int v, int box) { return W_OFF + (s * NV + v) * BX + box; }
     static __device__ __forceinline__ int d(int s, int ax, int v, int ring) {
-        return D_OFF + ((s * NAX + ax) * NV + v) * NRING + ring;
+        return D_OFF + ((s * NAX + ax) * NV + v) * RX + ring;
     }
-    static __device__ __forceinline__ int fx(int v, int y, int x) { return FX_OFF + (v * TY + y) * (TX + 1) + x; }
-    static __device__ __forceinline__ int fy(int v, int y, int x) { return FY_OFF + (v * (TY + 1) + y) * TX + x; }
-    static __device__ __forceinline__ int fz(int s, int v, int y, int x) {
-        return FZ_OFF + ((s * 6 + v) * TY + y) * TX + x;
-    }
-    // the cell (x, y) of this thread in the tile; false if it owns none
-    static __device__ __forceinline__ bool cell(int tid, int& x, int& y) {
-        if (HAS_Y) { x = tid % TX; y = tid / TX; return true; }
-        x = tid; y = 0;
+    static __device__ __forceinline__ int fx(int v, int x) { return FX_OFF + v * (TX + 1) + x; }
+    static __device__ __forceinline__ int fz(int s, int v, int x) { return FZ_OFF + (s * 6 + v) * TX + x; }
+    // the cell x of this thread in the tile; false if it owns none
+    static __device__ __forceinline__ bool cell(int tid, int& x) {
+        x = tid;
         return tid < TX;
     }
 };
 
-// Problem axis of kernel axis AX: fixed by the tile kind (3D two-axis tiles:
-// x, y, z; one-row marching tiles serve 2D problems: x, -, y; 1D: x).
+// Problem axis of kernel axis AX (0 or the marching axis 2): one-row
+// marching tiles serve 2D problems (x, -, y), the others 1D problems (x).
 template <class T, int AX>
 __device__ __forceinline__ constexpr int phys_axis() {
-    return AX == 0 ? 0 : (AX == 1 ? 1 : (T::HAS_Y ? 2 : 1));
+    return AX == 0 ? 0 : 1;
 }
 
 __device__ __forceinline__ int dslot(int p) { return (p + 2) & 1; }
 
-// One working-state position of a thread: where its source cell lives in a
+// The working-state position of a thread: where its source cell lives in a
 // plane and how to turn it into the working copy.
 struct BoxPos {
     int off;        // element offset of the source cell within a plane; -1: not used
     int box;        // box index in shared memory
     float cfxy;     // 1 / (h0 h1) of the source cell (kernel axes 0 and 1)
-    int xs, ys;     // boundary side applied after mirroring, or -1
+    int xs;         // boundary side applied after mirroring, or -1
     bool own;       // the cell belongs to this tile: write U^{n+1}
 };
 
@@ -161,29 +142,18 @@ struct Prefetch {
 };
 
 template <class T>
-__device__ __forceinline__ void setup_box(const ProbDesc& d, int i0, int j0, BoxPos (&bp)[T::NA]) {
-#pragma unroll
-    for (int k = 0; k < T::NA; ++k) {
-        const int t = threadIdx.x + k * T::NT;
-        bp[k].off = -1;
-        if (t >= T::NBOX) continue;
-        const int lx = t % T::BX, ly = t / T::BX;
-        const int dx = lx < HB ? HB - lx : (lx >= T::TX + HB ? lx - T::TX - HB + 1 : 0);
-        const int dy = T::HAS_Y ? (ly < HB ? HB - ly : (ly >= T::TY + HB ? ly - T::TY - HB + 1 : 0)) : 0;
-        if (dx + dy > HB) continue;
-        const int gi = i0 + lx - HB;
-        const int gj = T::HAS_Y ? j0 + ly - HB : 0;
-        if (gi >= d.kn[0] + HB) continue;
-        if (T::HAS_Y && gj >= d.kn[1] + HB) continue;
-        int si, sj = 0;
-        resolve(gi, d.kn[0], d.kper[0], 0, si, bp[k].xs);
-        bp[k].ys = -1;
-        if (T::HAS_Y) resolve(gj, d.kn[1], d.kper[1], 2 * d.kphys[1], sj, bp[k].ys);
-        bp[k].off = (int)(si + sj * d.kstr[1]);
-        bp[k].box = t;
-        bp[k].cfxy = __ldg(&d.kgeo[0][si + d.kgoff[0]].ih) * __ldg(&d.kgeo[1][sj + d.kgoff[1]].ih);
-        bp[k].own = dx == 0 && dy == 0 && gi < d.kn[0] && gj < d.kn[1];
-    }
+__device__ __forceinline__ void setup_box(const ProbDesc& d, int i0, BoxPos& bp) {
+    const int lx = threadIdx.x;
+    bp.off = -1;
+    const int dx = lx < HB ? HB - lx : (lx >= T::TX + HB ? lx - T::TX - HB + 1 : 0);
+    const int gi = i0 + lx - HB;
+    if (gi >= d.kn[0] + HB) return;
+    int si;
+    resolve(gi, d.kn[0], d.kper[0], 0, si, bp.xs);
+    bp.off = si;
+    bp.box = lx;
+    bp.cfxy = __ldg(&d.kgeo[0][si + d.kgoff[0]].ih) * __ldg(&d.kgeo[1][d.kgoff[1]].ih);
+    bp.own = dx == 0 && gi < d.kn[0];
 }
 
 // Source plane of marching index p (wrapped or mirrored), and the boundary
@@ -199,29 +169,23 @@ __device__ __forceinline__ int plane_of(const ProbDesc& d, int p, int& zs) {
 // Issue the loads of plane p (FP64 state and FP32 pending residual) into registers.
 template <class T>
 __device__ __forceinline__ void issue(const ProbDesc& d, const double* __restrict__ Uin,
-                                      const float* __restrict__ Rin, int p, const BoxPos (&bp)[T::NA],
-                                      Prefetch (&pf)[T::NA]) {
+                                      const float* __restrict__ Rin, int p, const BoxPos& bp, Prefetch& pf) {
     const long long plane = d.L.plane;
     int zs;
     const int sk = plane_of<T>(d, p, zs);
-    const long long zoff = d.kbase + sk * d.kstr[2];
+    if (bp.off < 0) return;
+    const long long c = d.kbase + sk * d.kstr[2] + bp.off;
 #pragma unroll
-    for (int k = 0; k < T::NA; ++k) {
-        if (bp[k].off < 0) continue;
-        const long long c = zoff + bp[k].off;
+    for (int v = 0; v < NV; ++v) pf.u[v] = __ldcg(Uin + v * plane + c);
 #pragma unroll
-        for (int v = 0; v < NV; ++v) pf[k].u[v] = __ldcg(Uin + v * plane + c);
-#pragma unroll
-        for (int v = 0; v < NV; ++v) pf[k].r[v] = __ldcg(Rin + v * plane + c);
-    }
+    for (int v = 0; v < NV; ++v) pf.r[v] = __ldcg(Rin + v * plane + c);
 }
 
 // Turn the prefetched plane p into the FP32 working copy in shared memory and
 // write U^{n+1} = U^n + dt R^n / V for the owned cells of planes [z0, z1).
 template <class T>
 __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __restrict__ Uout, int p, int z0, int z1,
-                                      float dtf, const BoxPos (&bp)[T::NA], const Prefetch (&pf)[T::NA],
-                                      unsigned int& health) {
+                                      float dtf, const BoxPos& bp, const Prefetch& pf, unsigned int& health) {
     const MixPhys& mp = d.mp;
     const long long plane = d.L.plane;
     int zs = -1;
@@ -230,39 +194,34 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
     const float cfz = dtf * __ldg(&d.kgeo[2][sk + d.kgoff[2]].ih);
     const int slot = T::MARCH ? T::wslot(p) : 0;
     const bool own_plane = p >= z0 && p < z1;
+    if (bp.off < 0) return;
+    const float cf = bp.cfxy * cfz;
+    float inc[NV], w[NV];
 #pragma unroll
-    for (int k = 0; k < T::NA; ++k) {
-        if (bp[k].off < 0) continue;
-        const float cf = bp[k].cfxy * cfz;
-        float inc[NV], w[NV];
+    for (int v = 0; v < NV; ++v) inc[v] = cf * pf.r[v];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) inc[v] = cf * pf[k].r[v];
+    for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(pf.u[v]) + inc[v];
+    w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf.u[4] - mp.einf_d) : f64_to_f32(pf.u[4])) + inc[4];
+    // BC of the boundary face of this ghost's row (the x sides' faces are
+    // numbered by the plane, the marching sides' by x)
+    if (bp.xs >= 0) bc32(mp, bc_id32(mp, bp.xs, sk), 0, w);
+    if (T::MARCH && zs >= 0) bc32(mp, bc_id32(mp, zs, bp.off), phys_axis<T, 2>(), w);
 #pragma unroll
-        for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(pf[k].u[v]) + inc[v];
-        w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf[k].u[4] - mp.einf_d) : f64_to_f32(pf[k].u[4])) +
-               inc[4];
-        // BC of the boundary face of this ghost's row (one-row tiles: the x
-        // sides' faces are numbered by the plane, the marching sides' by x)
-        static_assert(!T::HAS_Y, "one-row tiles only");
-        if (bp[k].xs >= 0) bc32(mp, bc_id32(mp, bp[k].xs, sk), 0, w);
-        if (T::MARCH && zs >= 0) bc32(mp, bc_id32(mp, zs, bp[k].off), phys_axis<T, 2>(), w);
+    for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp.box)] = w[v];
+    if (own_plane && bp.own) {
+        const long long c = zoff + bp.off;
+        double un[NV];
 #pragma unroll
-        for (int v = 0; v < NV; ++v) sm[T::w(slot, v, bp[k].box)] = w[v];
-        if (own_plane && bp[k].own) {
-            const long long c = zoff + bp[k].off;
-            double un[NV];
-#pragma unroll
-            for (int v = 0; v < NV; ++v) {
-                un[v] = pf[k].u[v] + f32_to_f64(inc[v]);
-                __stcg(Uout + v * plane + c, un[v]);
-            }
-            // rho > 0 tested on the bit pattern (no FP64 comparison): positive
-            // finite values and +inf are the integers 1 .. 0x7FF0000000000000
-            const long long b = __double_as_longlong(un[0]);
-            if (b <= 0 || b > 0x7FF0000000000000LL)
-                health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
-            if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
+        for (int v = 0; v < NV; ++v) {
+            un[v] = pf.u[v] + f32_to_f64(inc[v]);
+            __stcg(Uout + v * plane + c, un[v]);
         }
+        // rho > 0 tested on the bit pattern (no FP64 comparison): positive
+        // finite values and +inf are the integers 1 .. 0x7FF0000000000000
+        const long long b = __double_as_longlong(un[0]);
+        if (b <= 0 || b > 0x7FF0000000000000LL)
+            health |= (b & 0x7FFFFFFFFFFFFFFFLL) > 0x7FF0000000000000LL ? TS_HEALTH_NAN : TS_HEALTH_NEG_DENSITY;
+        if (!(w[4] == w[4])) health |= TS_HEALTH_NAN;
     }
 }
 
@@ -286,48 +245,28 @@ __device__ __forceinline__ Slots slots_of(int p) {
     return s;
 }
 
-// One reconstruction position of a thread for the current item: its ring
-// index, box index and geometry entries (fixed while the item marches).
+// The reconstruction position of a thread for the current item (ring index
+// = thread index): its box index and geometry entry (fixed while the item
+// marches).
 struct RingPos {
     int box;        // box index of the cell; -1: nothing to do
-    int g0, g1;     // geometry indices along kernel axes 0 and 1
-    float ks0, ks1; // central-slope factors along kernel axes 0 and 1 (marching tiles)
+    int g0;         // geometry index along kernel axis 0
+    float ks0;      // central-slope factor along kernel axis 0 (marching tiles)
 };
 
-// Ring position of round k of this thread.  Second rounds run from the last
-// thread down: the first threads already have a second working-state
-// position, so the extra work of the two phases lands on different warps.
 template <class T>
-__device__ __forceinline__ int ring_index(int k) {
-    return k == 0 ? (int)threadIdx.x : k * T::NT + (T::NT - 1 - (int)threadIdx.x);
-}
-
-template <class T>
-__device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, int j0, RingPos (&rp)[T::NB]) {
-#pragma unroll
-    for (int k = 0; k < T::NB; ++k) {
-        const int t = ring_index<T>(k);
-        rp[k].box = -1;
-        if (t >= T::NRING) continue;
-        const int rx = t % T::RX, ry = t / T::RX;
-        const bool ox = rx < 1 || rx > T::TX;
-        const bool oy = T::HAS_Y && (ry < 1 || ry > T::TY);
-        if (ox && oy) continue;
-        const int gi = i0 + rx - 1, gj = T::HAS_Y ? j0 + ry - 1 : 0;
-        if (gi > d.kn[0] || (T::HAS_Y && gj > d.kn[1])) continue;
-        if ((gi < 0 || gi >= d.kn[0]) && !d.kper[0]) continue;
-        if (T::HAS_Y && (gj < 0 || gj >= d.kn[1]) && !d.kper[1]) continue;
-        int si, sj = 0, xs, ys;
-        resolve(gi, d.kn[0], 1, 0, si, xs);
-        if (T::HAS_Y) resolve(gj, d.kn[1], 1, 0, sj, ys);
-        rp[k].box = (T::HAS_Y ? (ry + 1) * T::BX : 0) + rx + 1;
-        rp[k].g0 = si + d.kgoff[0];
-        rp[k].g1 = sj + d.kgoff[1];
-        if (T::MARCH) {
-            rp[k].ks0 = d.kgeo[0][rp[k].g0].ks;
-            rp[k].ks1 = T::HAS_Y ? d.kgeo[1][rp[k].g1].ks : 0.0f;
-        }
-    }
+__device__ __forceinline__ void setup_ring(const ProbDesc& d, int i0, RingPos& rp) {
+    const int rx = threadIdx.x;
+    rp.box = -1;
+    if (rx >= T::RX) return;
+    const int gi = i0 + rx - 1;
+    if (gi > d.kn[0]) return;
+    if ((gi < 0 || gi >= d.kn[0]) && !d.kper[0]) return;
+    int si, xs;
+    resolve(gi, d.kn[0], 1, 0, si, xs);
+    rp.box = rx + 1;
+    rp.g0 = si + d.kgoff[0];
+    if (T::MARCH) rp.ks0 = d.kgeo[0][rp.g0].ks;
 }
 
 // Reconstruction kinds (the limiter choice folded in).
@@ -341,11 +280,10 @@ __host__ __device__ __forceinline__ int recon_kind(const MixPhys& mp) {
     return 0;
 }
 
-// Limited half-slopes of plane p on the tile and its 1-cell ring (corners
-// excluded); ring cells outside a non-periodic boundary are not needed.
+// Limited half-slopes of plane p on the tile and its 1-cell ring; ring cells
+// outside a non-periodic boundary are not needed.
 template <class T, int KIND>
-__device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, const Slots& s,
-                                        const RingPos (&rp)[T::NB]) {
+__device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, const Slots& s, const RingPos& rp) {
     int sk = 0;
     if (T::MARCH) {
         if ((p < 0 || p >= d.kn[2]) && !d.kper[2]) return;
@@ -354,19 +292,16 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
     }
     AxisGeo gz;
     if (T::MARCH) gz = d.kgeo[2][sk + d.kgoff[2]];
-#pragma unroll
-    for (int k = 0; k < T::NB; ++k) {
-        if (rp[k].box < 0) continue;
-        const int t = ring_index<T>(k);
-        const int box = rp[k].box;
-        AxisGeo g[3];
+    if (rp.box < 0) return;
+    {
+        const int t = threadIdx.x;
+        const int box = rp.box;
+        AxisGeo g[T::NAX];
         if (T::MARCH && (KIND == RK_LINEAR || KIND == RK_LIM_BJ)) {
             // central slopes need only ks, kept in registers while the item marches
-            g[0].ks = rp[k].ks0;
-            if (T::HAS_Y) g[1].ks = rp[k].ks1;
+            g[0].ks = rp.ks0;
         } else {
-            g[0] = d.kgeo[0][rp[k].g0];
-            if (T::HAS_Y) g[1] = d.kgeo[1][rp[k].g1];
+            g[0] = d.kgeo[0][rp.g0];
         }
         if (T::MARCH) g[T::AZ] = gz;
         float eps2 = 0.0f;
@@ -375,17 +310,16 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
             float vol = g[0].h;
 #pragma unroll
             for (int ax = 1; ax < T::NAX; ++ax) vol *= g[ax].h;
-            eps2 = 125.0f * (T::NAX == 3 ? vol : (T::NAX == 2 ? vol * sqrtf(vol) : vol * vol * vol));
+            eps2 = 125.0f * (T::NAX == 2 ? vol * sqrtf(vol) : vol * vol * vol);
         }
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             const float w0 = sm[T::w(s.w0, v, box)];
-            float nm[3], np[3];
+            float nm[T::NAX], np[T::NAX];
             nm[0] = sm[T::w(s.w0, v, box - 1)];
             np[0] = sm[T::w(s.w0, v, box + 1)];
-            if (T::HAS_Y) { nm[1] = sm[T::w(s.w0, v, box - T::BX)]; np[1] = sm[T::w(s.w0, v, box + T::BX)]; }
             if (T::MARCH) { nm[T::AZ] = sm[T::w(s.wm, v, box)]; np[T::AZ] = sm[T::w(s.wp, v, box)]; }
-            float dd[3];
+            float dd[T::NAX];
             if (KIND == RK_ENO2) {
 #pragma unroll
                 for (int ax = 0; ax < T::NAX; ++ax) {
@@ -448,7 +382,7 @@ __device__ __forceinline__ void recon_k(const ProbDesc& d, float* sm, int p, con
 
 template <class T>
 __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int p, int kind, const Slots& s,
-                                      const RingPos (&rp)[T::NB]) {
+                                      const RingPos& rp) {
     switch (kind) {
     case RK_LINEAR: recon_k<T, RK_LINEAR>(d, sm, p, s, rp); break;
     case RK_ENO2: recon_k<T, RK_ENO2>(d, sm, p, s, rp); break;
@@ -457,45 +391,39 @@ __device__ __forceinline__ void recon(const ProbDesc& d, float* sm, int p, int k
     }
 }
 
-// One face on kernel axis AX between the cells (fx-1, fy) and (fx, fy) of the
-// tile (AX = 0), (fx, fy-1) and (fx, fy) (AX = 1), or (fx, fy) of planes z and
-// z+1 (AX = 2): face states, boundary image, Riemann flux and eigenvalue into
-// the face array.  s holds the slots of plane z.
+// One face on kernel axis AX between the cells fx-1 and fx of the tile
+// (AX = 0) or between cell fx of planes z and z+1 (AX = 2, the marching
+// axis): face states, boundary image, Riemann flux and eigenvalue into the
+// face array.  s holds the slots of plane z.
 template <class T, int AX>
-__device__ __forceinline__ bool face_in(const ProbDesc& d, const float* sm, int fx, int fy, int gi, int gj, int z,
-                                        const Slots& s, bool pwc, float UL[NV], float UR[NV], int& out, int& vs) {
+__device__ __forceinline__ bool face_in(const ProbDesc& d, const float* sm, int fx, int gi, int z, const Slots& s,
+                                        bool pwc, float UL[NV], float UR[NV], int& out, int& vs) {
+    static_assert(AX == 0 || (AX == 2 && T::MARCH), "faces on x or the marching axis");
     constexpr int A = phys_axis<T, AX>();
-    constexpr int SA = AX == 0 ? 0 : (AX == 1 ? 1 : T::AZ);
+    constexpr int SA = AX == 0 ? 0 : T::AZ;
     int bl, br, rl, rr, g, n, per;
     int wl = s.w0, wr = s.w0, dl = s.d0, dr = s.d0;
     if (AX == 0) {
-        if (gi > d.kn[0] || gj >= d.kn[1]) return false;
-        bl = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + 1; br = bl + 1;
-        rl = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx; rr = rl + 1;
+        if (gi > d.kn[0]) return false;
+        bl = fx + 1; br = bl + 1;
+        rl = fx; rr = rl + 1;
         g = gi; n = d.kn[0]; per = d.kper[0];
-        out = T::fx(0, fy, fx); vs = T::TY * (T::TX + 1);
-    } else if (AX == 1) {
-        if (gi >= d.kn[0] || gj > d.kn[1]) return false;
-        bl = (fy + 1) * T::BX + fx + HB; br = bl + T::BX;
-        rl = fy * T::RX + fx + 1; rr = rl + T::RX;
-        g = gj; n = d.kn[1]; per = d.kper[1];
-        out = T::fy(0, fy, fx); vs = (T::TY + 1) * T::TX;
+        out = T::fx(0, fx); vs = T::TX + 1;
     } else {
-        if (gi >= d.kn[0] || gj >= d.kn[1]) return false;
-        bl = br = (T::HAS_Y ? (fy + HB) * T::BX : 0) + fx + HB;
-        rl = rr = (T::HAS_Y ? (fy + 1) * T::RX : 0) + fx + 1;
+        if (gi >= d.kn[0]) return false;
+        bl = br = fx + HB;
+        rl = rr = fx + 1;
         wr = s.wp; dr = s.d1;
         g = z + 1; n = d.kn[2]; per = d.kper[2];
-        out = T::fz(s.d1, 0, fy, fx); vs = T::TY * T::TX;
+        out = T::fz(s.d1, 0, fx); vs = T::TX;
     }
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         UL[v] = sm[T::w(wl, v, bl)] + (pwc ? 0.0f : sm[T::d(dl, SA, v, rl)]);
         UR[v] = sm[T::w(wr, v, br)] - (pwc ? 0.0f : sm[T::d(dr, SA, v, rr)]);
     }
-    // boundary faces: the BC of this face (one-row tiles: an x face is
-    // numbered by its plane, a marching-axis face by its x index)
-    static_assert(!T::HAS_Y, "one-row tiles only");
+    // boundary faces: the BC of this face (an x face is numbered by its
+    // plane, a marching-axis face by its x index)
     const int f = AX == 0 ? z : gi;
     if (g == 0 && !per) {
 #pragma unroll
@@ -510,67 +438,26 @@ __device__ __forceinline__ bool face_in(const ProbDesc& d, const float* sm, int 
 }
 
 template <class T, int SOLVER, int AX>
-__device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
-                                     const Slots& s, bool pwc) {
+__device__ __forceinline__ void face(const ProbDesc& d, float* sm, int fx, int gi, int z, const Slots& s, bool pwc) {
     float UL[NV], UR[NV], F[NV];
     int out, vs;
-    if (!face_in<T, AX>(d, sm, fx, fy, gi, gj, z, s, pwc, UL, UR, out, vs)) return;
+    if (!face_in<T, AX>(d, sm, fx, gi, z, s, pwc, UL, UR, out, vs)) return;
     const float lam = flux32<SOLVER, phys_axis<T, AX>()>(d.mp, UL, UR, F);
 #pragma unroll
     for (int v = 0; v < NV; ++v) sm[out + v * vs] = F[v];
     sm[out + NV * vs] = lam;
 }
 
-// Faces on kernel axes 0 and 1 of one thread computed side by side (one
-// basic block, so the two Riemann solutions interleave).
+// The faces of plane z this thread computes: the x face left of its cell
+// (thread TX: the tile's far x face) and, marching, the face above its cell
+// (between z and z+1).
 template <class T, int SOLVER>
-__device__ __forceinline__ void face_pair(const ProbDesc& d, float* sm, int fx, int fy, int gi, int gj, int z,
-                                          const Slots& s, bool pwc) {
-    float UL0[NV], UR0[NV], UL1[NV], UR1[NV], F0[NV], F1[NV];
-#pragma unroll
-    for (int v = 0; v < NV; ++v) UL0[v] = UR0[v] = UL1[v] = UR1[v] = 1.0f;
-    int o0, v0, o1, v1;
-    const bool ok0 = face_in<T, 0>(d, sm, fx, fy, gi, gj, z, s, pwc, UL0, UR0, o0, v0);
-    const bool ok1 = face_in<T, 1>(d, sm, fx, fy, gi, gj, z, s, pwc, UL1, UR1, o1, v1);
-    const float l0 = flux32<SOLVER, phys_axis<T, 0>()>(d.mp, UL0, UR0, F0);
-    const float l1 = flux32<SOLVER, phys_axis<T, 1>()>(d.mp, UL1, UR1, F1);
-    if (ok0) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) sm[o0 + v * v0] = F0[v];
-        sm[o0 + NV * v0] = l0;
-    }
-    if (ok1) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) sm[o1 + v * v1] = F1[v];
-        sm[o1 + NV * v1] = l1;
-    }
-}
-
-// The faces of plane z this thread computes: on kernel axis 0 the face left
-// of its cell, on axis 1 the face below it (the two side by side), on the
-// marching axis the face above it (between z and z+1).  The tile's far faces
-// go to different warps of a two-axis tile: axis 1 (face TY) to the first TX
-// threads, axis 0 (face TX) to the last TY threads; in a one-row tile thread
-// TX computes the far face.
-template <class T, int SOLVER>
-__device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int j0, int z, bool pwc, bool do_xy,
-                                       bool do_z, const Slots& s) {
-    const int tid = threadIdx.x;
-    const int tx = T::HAS_Y ? tid % T::TX : tid, ty = T::HAS_Y ? tid / T::TX : 0;
-    if (do_xy) {
-        if constexpr (T::HAS_Y) {
-            face_pair<T, SOLVER>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
-            // far faces: axis 1 on the first warp(s), axis 0 on the last threads
-            if (tid < T::TX) face<T, SOLVER, 1>(d, sm, tid, T::TY, i0 + tid, j0 + T::TY, z, s, pwc);
-            else if (tid >= T::NT - T::TY) {
-                const int fy = tid - (T::NT - T::TY);
-                face<T, SOLVER, 0>(d, sm, T::TX, fy, i0 + T::TX, j0 + fy, z, s, pwc);
-            }
-        } else {
-            if (tx <= T::TX) face<T, SOLVER, 0>(d, sm, tx, 0, i0 + tx, j0, z, s, pwc);
-        }
-    }
-    if (T::MARCH && do_z && (T::HAS_Y || tx < T::TX)) face<T, SOLVER, 2>(d, sm, tx, ty, i0 + tx, j0 + ty, z, s, pwc);
+__device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int z, bool pwc, bool do_x, bool do_z,
+                                       const Slots& s) {
+    const int tx = threadIdx.x;
+    if (do_x && tx <= T::TX) face<T, SOLVER, 0>(d, sm, tx, i0 + tx, z, s, pwc);
+    if constexpr (T::MARCH)
+        if (do_z && tx < T::TX) face<T, SOLVER, 2>(d, sm, tx, i0 + tx, z, s, pwc);
 }
 
 // The working state (rho, momentum) of the thread's own cell in plane z, for
@@ -578,35 +465,34 @@ __device__ __forceinline__ void fluxes(const ProbDesc& d, float* sm, int i0, int
 // next plane's store reuses the slot).
 template <class T>
 __device__ __forceinline__ float4 own_state(const float* sm, const Slots& s) {
-    int tx, ty;
-    if (!T::cell(threadIdx.x, tx, ty)) return make_float4(1.0f, 0.0f, 0.0f, 0.0f);
-    const int box = (T::HAS_Y ? (ty + HB) * T::BX : 0) + tx + HB;
+    int tx;
+    if (!T::cell(threadIdx.x, tx)) return make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+    const int box = tx + HB;
     return make_float4(sm[T::w(s.w0, 0, box)], sm[T::w(s.w0, 1, box)], sm[T::w(s.w0, 2, box)],
                        sm[T::w(s.w0, 3, box)]);
 }
 
 // Geometry of the thread's own cell along kernel axes 0 and 1 (fixed while
 // an item marches): sizes, the face area normal to the marching axis, the
-// inverse area, and the spectral-radius factors of the high boundary faces
-// (0 where the cell is not the last one along the axis).
+// inverse area, and the spectral-radius factor of the high x boundary face
+// (0 where the cell is not the last one along x).
 struct CellGeo {
-    float hx, hy, fsz, ixy, farx, fary;
+    float hx, hy, fsz, ixy, farx;
 };
 
 template <class T>
-__device__ __forceinline__ CellGeo cell_geo(const ProbDesc& d, int i0, int j0) {
-    CellGeo c{1.0f, 1.0f, 1.0f, 1.0f, 0.0f, 0.0f};
-    int tx, ty;
-    if (!T::cell(threadIdx.x, tx, ty)) return c;
-    const int gi = i0 + tx, gj = j0 + ty;
-    if (gi >= d.kn[0] || gj >= d.kn[1]) return c;
-    const AxisGeo gx = d.kgeo[0][gi + d.kgoff[0]], gy = d.kgeo[1][gj + d.kgoff[1]];
+__device__ __forceinline__ CellGeo cell_geo(const ProbDesc& d, int i0) {
+    CellGeo c{1.0f, 1.0f, 1.0f, 1.0f, 0.0f};
+    int tx;
+    if (!T::cell(threadIdx.x, tx)) return c;
+    const int gi = i0 + tx;
+    if (gi >= d.kn[0]) return c;
+    const AxisGeo gx = d.kgeo[0][gi + d.kgoff[0]], gy = d.kgeo[1][d.kgoff[1]];
     c.hx = gx.h;
     c.hy = gy.h;
     c.fsz = gx.h * gy.h;
     c.ixy = gx.ih * gy.ih;
     if (gi == d.kn[0] - 1) c.farx = d.kgeo[0][d.kn[0] + d.kgoff[0]].ih * gy.ih;
-    if (T::HAS_Y && gj == d.kn[1] - 1) c.fary = gx.ih * d.kgeo[1][d.kn[1] + d.kgoff[1]].ih;
     return c;
 }
 
@@ -614,35 +500,28 @@ __device__ __forceinline__ CellGeo cell_geo(const ProbDesc& d, int i0, int j0) {
 // (hz, ihz: size and inverse size of plane z); false if the thread owns no
 // cell.
 template <class T, int SOLVER>
-__device__ __forceinline__ bool residual_of(const ProbDesc& d, const float* sm, int i0, int j0, int z, const Slots& s,
+__device__ __forceinline__ bool residual_of(const ProbDesc& d, const float* sm, int i0, int z, const Slots& s,
                                             float4 own, const CellGeo& cg, float hz, float ihz, float& srmax,
                                             float R[NV]) {
-    int tx, ty;
-    if (!T::cell(threadIdx.x, tx, ty)) return false;
-    const int gi = i0 + tx, gj = j0 + ty;
-    if (gi >= d.kn[0] || gj >= d.kn[1]) return false;
-    const float fsx = cg.hy * hz, fsy = cg.hx * hz, fsz = cg.fsz;
+    int tx;
+    if (!T::cell(threadIdx.x, tx)) return false;
+    const int gi = i0 + tx;
+    if (gi >= d.kn[0]) return false;
+    const float fsx = cg.hy * hz, fsz = cg.fsz;
     const float iv = cg.ixy * ihz;
     // face areas times the stored-flux factor
-    const float kx = flux_scale<SOLVER>() * fsx, ky = flux_scale<SOLVER>() * fsy, kz = flux_scale<SOLVER>() * fsz;
-    const float lxl = sm[T::fx(5, ty, tx)], lxr = sm[T::fx(5, ty, tx + 1)];
+    const float kx = flux_scale<SOLVER>() * fsx, kz = flux_scale<SOLVER>() * fsz;
+    const float lxl = sm[T::fx(5, tx)], lxr = sm[T::fx(5, tx + 1)];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, ty, tx + 1)] - sm[T::fx(v, ty, tx)]) * kx;
+    for (int v = 0; v < NV; ++v) R[v] = -(sm[T::fx(v, tx + 1)] - sm[T::fx(v, tx)]) * kx;
     float sr = fsx * (lxl + lxr);
     if (cg.farx != 0.0f) srmax = fmaxf(srmax, fsx * lxr * cg.farx * ihz);
-    if (T::HAS_Y) {
-#pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fy(v, ty + 1, tx)] - sm[T::fy(v, ty, tx)]) * ky;
-        const float lyr = sm[T::fy(5, ty + 1, tx)];
-        sr += fsy * (sm[T::fy(5, ty, tx)] + lyr);
-        if (cg.fary != 0.0f) srmax = fmaxf(srmax, fsy * lyr * cg.fary * ihz);
-    }
     if (T::MARCH) {
         const int dn = s.d0, up = s.d1;
 #pragma unroll
-        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, ty, tx)] - sm[T::fz(dn, v, ty, tx)]) * kz;
-        const float lzr = sm[T::fz(up, 5, ty, tx)];
-        sr += fsz * (sm[T::fz(dn, 5, ty, tx)] + lzr);
+        for (int v = 0; v < NV; ++v) R[v] -= (sm[T::fz(up, v, tx)] - sm[T::fz(dn, v, tx)]) * kz;
+        const float lzr = sm[T::fz(up, 5, tx)];
+        sr += fsz * (sm[T::fz(dn, 5, tx)] + lzr);
         if (z == d.kn[2] - 1) srmax = fmaxf(srmax, fsz * lzr * cg.ixy * d.kgeo[2][d.kn[2] + d.kgoff[2]].ih);
     }
     srmax = fmaxf(srmax, sr * iv);
@@ -671,19 +550,19 @@ __device__ __forceinline__ bool residual_of(const ProbDesc& d, const float* sm, 
 
 // The same, written to the pending-residual planes Rout.
 template <class T, int SOLVER>
-__device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int j0,
-                                         int z, const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
+__device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, float* __restrict__ Rout, int i0, int z,
+                                         const Slots& s, float4 own, const CellGeo& cg, float hz, float ihz,
                                          float& srmax, float (&nrm)[NV]) {
     float R[NV];
-    if (!residual_of<T, SOLVER>(d, sm, i0, j0, z, s, own, cg, hz, ihz, srmax, R)) return;
+    if (!residual_of<T, SOLVER>(d, sm, i0, z, s, own, cg, hz, ihz, srmax, R)) return;
     if (d.mp.norms) {
         const float vol = cg.fsz * hz;
 #pragma unroll
         for (int v = 0; v < NV; ++v) nrm[v] += vol * fabsf(R[v]);
     }
-    int tx, ty;
-    T::cell(threadIdx.x, tx, ty);
-    const long long c = d.kbase + (i0 + tx) + (j0 + ty) * d.kstr[1] + z * d.kstr[2];
+    int tx;
+    T::cell(threadIdx.x, tx);
+    const long long c = d.kbase + (i0 + tx) + z * d.kstr[2];
     const long long plane = d.L.plane;
 #pragma unroll
     for (int v = 0; v < NV; ++v) __stcg(Rout + v * plane + c, R[v]);
@@ -695,9 +574,9 @@ __device__ __forceinline__ void residual(const ProbDesc& d, const float* sm, flo
 
 // One work item (tile column and chunk q of problem d).
 template <class T, int SOLVER>
-__device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, float dtf, float* sm,
-                                             BoxPos (&bp)[T::NA], Prefetch (&pf)[T::NA], RingPos (&rp)[T::NB],
-                                             float& srmax, unsigned int& health, float (&nrm)[NV]) {
+__device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, float dtf, float* sm, BoxPos& bp,
+                                             Prefetch& pf, RingPos& rp, float& srmax, unsigned int& health,
+                                             float (&nrm)[NV]) {
     const double* __restrict__ Uin = d.U[par];
     double* __restrict__ Uout = d.U[par ^ 1];
     const float* __restrict__ Rin = d.R[par];
@@ -705,25 +584,24 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
     const int kind = recon_kind(d.mp);
     const bool pwc = kind == 0;
     const bool src = d.mp.force || d.mp.accel;
-    const int col = q % d.ncol;
-    const int i0 = (col % d.ncx) * T::TX, j0 = (col / d.ncx) * T::TY;
-    setup_box<T>(d, i0, j0, bp);
-    if (!pwc) setup_ring<T>(d, i0, j0, rp);
-    if (!T::MARCH) {
+    const int i0 = (q % d.ncol) * T::TX;
+    setup_box<T>(d, i0, bp);
+    if (!pwc) setup_ring<T>(d, i0, rp);
+    if constexpr (!T::MARCH) {
         const Slots s = slots_of<T>(0);
         issue<T>(d, Uin, Rin, 0, bp, pf);
         store<T>(d, sm, Uout, 0, 0, 1, dtf, bp, pf, health);
         __syncthreads();
         if (!pwc) { recon<T>(d, sm, 0, kind, s, rp); __syncthreads(); }
-        fluxes<T, SOLVER>(d, sm, i0, j0, 0, pwc, true, false, s);
+        fluxes<T, SOLVER>(d, sm, i0, 0, pwc, true, false, s);
         const float4 own = src ? own_state<T>(sm, s) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
         // a single plane: the geometry is loaded where it is used
-        const CellGeo cg = cell_geo<T>(d, i0, j0);
+        const CellGeo cg = cell_geo<T>(d, i0);
         const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
-        residual<T, SOLVER>(d, sm, Rout, i0, j0, 0, s, own, cg, gz.h, gz.ih, srmax, nrm);
-    } else if constexpr (!T::TWO_PHASE) {
-        const CellGeo cg = cell_geo<T>(d, i0, j0);
+        residual<T, SOLVER>(d, sm, Rout, i0, 0, s, own, cg, gz.h, gz.ih, srmax, nrm);
+    } else {
+        const CellGeo cg = cell_geo<T>(d, i0);
         const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
         // Planes z0-2 .. z1+1 are loaded; the first two loop passes only
         // build the slopes of planes z0-1, z0 and the marching face z0-1/2.
@@ -742,56 +620,13 @@ __device__ __forceinline__ void process_item(const ProbDesc& d, int q, int par, 
             if (z + 3 <= z1 + 1) issue<T>(d, Uin, Rin, z + 3, bp, pf);
             __syncthreads();
             if (!pwc) { recon<T>(d, sm, z + 1, kind, sr, rp); __syncthreads(); }
-            if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, j0, z, pwc, z >= z0, true, sf);
+            if (z >= z0 - 1) fluxes<T, SOLVER>(d, sm, i0, z, pwc, z >= z0, true, sf);
             const float4 own = src && z >= z0 ? own_state<T>(sm, sf) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
             __syncthreads();
             if (z >= z0) {
                 const AxisGeo gz = d.kgeo[2][z + d.kgoff[2]];
-                residual<T, SOLVER>(d, sm, Rout, i0, j0, z, sf, own, cg, gz.h, gz.ih, srmax, nrm);
+                residual<T, SOLVER>(d, sm, Rout, i0, z, sf, own, cg, gz.h, gz.ih, srmax, nrm);
             }
-        }
-    } else {
-        const CellGeo cg = cell_geo<T>(d, i0, j0);
-        const int z0 = (q / d.ncol) * d.ch, z1 = min(d.kn[2], z0 + d.ch);
-        // Planes z0-2 .. z1+1 are loaded.  Pass P has two phases:
-        //   A: store plane P+2, slopes of plane P, residual of plane P-2;
-        //   B: faces of plane P-1 (axes 0, 1) and the marching face P-1/P.
-        // Four working-state planes (P-1 .. P+2) and two slope planes are
-        // live, so the two phases need one barrier each.
-        issue<T>(d, Uin, Rin, z0 - 2, bp, pf);
-        store<T>(d, sm, Uout, z0 - 2, z0, z1, dtf, bp, pf, health);
-        issue<T>(d, Uin, Rin, z0 - 1, bp, pf);
-        store<T>(d, sm, Uout, z0 - 1, z0, z1, dtf, bp, pf, health);
-        issue<T>(d, Uin, Rin, z0, bp, pf);
-        store<T>(d, sm, Uout, z0, z0, z1, dtf, bp, pf, health);
-        issue<T>(d, Uin, Rin, z0 + 1, bp, pf);
-        __syncthreads();
-        float4 own = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
-#pragma unroll 1
-        for (int P = z0 - 1; P <= z1 + 1; ++P) {
-            // geometry of the residual's plane first: its load overlaps the phase
-            float hz = 1.0f, ihz = 1.0f;
-            if (P - 2 >= z0) {
-                const AxisGeo gz = d.kgeo[2][P - 2 + d.kgoff[2]];
-                hz = gz.h;
-                ihz = gz.ih;
-            }
-            // plane P+2 was prefetched during the previous pass
-            if (P + 2 <= z1 + 1) {
-                store<T>(d, sm, Uout, P + 2, z0, z1, dtf, bp, pf, health);
-                if (P + 3 <= z1 + 1) issue<T>(d, Uin, Rin, P + 3, bp, pf);
-            }
-            if (!pwc && P <= z1) recon<T>(d, sm, P, kind, slots_of<T>(P), rp);
-            if (P - 2 >= z0) residual<T, SOLVER>(d, sm, Rout, i0, j0, P - 2, slots_of<T>(P - 2), own, cg, hz, ihz, srmax, nrm);
-            if (P > z1) break;
-            __syncthreads();
-            if (P < z0) continue;
-            const Slots sf = slots_of<T>(P - 1);
-            fluxes<T, SOLVER>(d, sm, i0, j0, P - 1, pwc, P - 1 >= z0, true, sf);
-            // the residual of plane P-1 runs in the next pass, after the
-            // store that reuses this working-state slot
-            if (src && P - 1 >= z0) own = own_state<T>(sm, sf);
-            __syncthreads();
         }
     }
 }
@@ -845,9 +680,9 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
     extern __shared__ float sm[];
     __shared__ float wmax[32];
     __shared__ unsigned int whealth[32];
-    BoxPos bp[T::NA];
-    Prefetch pf[T::NA];
-    RingPos rp[T::NB];
+    BoxPos bp;
+    Prefetch pf;
+    RingPos rp;
     if constexpr (!BATCH) {
         if (one.ctl->stop_req) return;
         const int par = one.ctl->parity;
@@ -905,7 +740,7 @@ __global__ void __launch_bounds__(T::NT, T::MINB) k_mix_step(const __grid_consta
 // CTA repeats on its own copy of the control word (the same maximum gives
 // every CTA the same dt and the same stop decision, so all CTAs run the same
 // number of stages and barriers).
-using TailTile = Tile<512, 1, false>;
+using TailTile = Tile<512, false>;
 
 template <int SOLVER>
 __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict__ probs,
@@ -937,20 +772,20 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
     const bool pwc = kind == 0;
     const bool src = mp.force || mp.accel;
     const bool stiff = mp.eos == TS_EOS_STIFFENED_GAS;
-    BoxPos bp[T::NA];
-    RingPos rp[T::NB];
-    setup_box<T>(d, i0, 0, bp);
-    if (!pwc) setup_ring<T>(d, i0, 0, rp);
-    const CellGeo cg0 = cell_geo<T>(d, i0, 0);
+    BoxPos bp;
+    RingPos rp;
+    setup_box<T>(d, i0, bp);
+    if (!pwc) setup_ring<T>(d, i0, rp);
+    const CellGeo cg0 = cell_geo<T>(d, i0);
     const AxisGeo gz = d.kgeo[2][d.kgoff[2]];
     const Slots sl = slots_of<T>(0);
-    const bool own = bp[0].off >= 0 && bp[0].own;
+    const bool own = bp.off >= 0 && bp.own;
     __syncthreads();
     double u[NV];
     float r[NV];
     if (own) {
         const int par = sc.parity;
-        const long long c = d.kbase + bp[0].off;
+        const long long c = d.kbase + bp.off;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             u[v] = __ldcg(d.U[par] + v * plane + c);
@@ -963,7 +798,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
         unsigned int health = 0;
         // pending update of the own cell and its working copy (store())
         if (own) {
-            const float cf = bp[0].cfxy * (s_dtf * gz.ih);
+            const float cf = bp.cfxy * (s_dtf * gz.ih);
             float inc[NV], w[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
@@ -971,7 +806,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
             for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
             w[4] = (stiff ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4])) + inc[4];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp[0].box)] = w[v];
+            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp.box)] = w[v];
 #pragma unroll
             for (int v = 0; v < NV; ++v) u[v] = u[v] + f32_to_f64(inc[v]);
             const long long b = __double_as_longlong(u[0]);
@@ -981,25 +816,25 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
         }
         cluster.sync();
         // halo positions: the owner's working copy, then the boundary image
-        if (bp[0].off >= 0 && !own) {
-            const int si = bp[0].off;
+        if (bp.off >= 0 && !own) {
+            const int si = bp.off;
             const int orank = si / T::TX;
             const float* owner = cluster.map_shared_rank(sm, orank);
             const int opos = si - orank * T::TX + HB;
             float w[NV];
 #pragma unroll
             for (int v = 0; v < NV; ++v) w[v] = owner[T::w(0, v, opos)];
-            if (bp[0].xs >= 0) bc32(mp, bc_id32(mp, bp[0].xs, 0), 0, w);
+            if (bp.xs >= 0) bc32(mp, bc_id32(mp, bp.xs, 0), 0, w);
 #pragma unroll
-            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp[0].box)] = w[v];
+            for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp.box)] = w[v];
         }
         __syncthreads();
         if (!pwc) { recon<T>(d, sm, 0, kind, sl, rp); __syncthreads(); }
-        fluxes<T, SOLVER>(d, sm, i0, 0, 0, pwc, true, false, sl);
+        fluxes<T, SOLVER>(d, sm, i0, 0, pwc, true, false, sl);
         const float4 ow = src ? own_state<T>(sm, sl) : make_float4(1.0f, 0.0f, 0.0f, 0.0f);
         __syncthreads();
         float srmax = 0.0f, R[NV];
-        if (residual_of<T, SOLVER>(d, sm, i0, 0, 0, sl, ow, cg0, gz.h, gz.ih, srmax, R)) {
+        if (residual_of<T, SOLVER>(d, sm, i0, 0, sl, ow, cg0, gz.h, gz.ih, srmax, R)) {
 #pragma unroll
             for (int v = 0; v < NV; ++v) rbuf[v * T::TX + tid] = R[v];
         }
@@ -1033,7 +868,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
         }
         __syncthreads();
         if (own) {
-            const int lx = bp[0].box - HB;
+            const int lx = bp.box - HB;
 #pragma unroll
             for (int v = 0; v < NV; ++v) r[v] = rbuf[v * T::TX + lx];
         }
@@ -1043,7 +878,7 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
     __syncthreads();
     if (own) {
         const int par = sc.parity;
-        const long long c = d.kbase + bp[0].off;
+        const long long c = d.kbase + bp.off;
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             d.U[par][v * plane + c] = u[v];
@@ -1106,25 +941,22 @@ __global__ void k_batch_finish(const ProbDesc* __restrict__ probs, const int* __
     finish_problem(d.ctl, d.mp.cfl);
 }
 
-// Compiled tiles: (problem dimension, threads along x, threads along y).
-// 3D: two-axis tiles marching z.  2D: one-row tiles marching y.  1D: one-row
-// tiles, one plane.
-#define TS_MIXED_TILES_2D(X) X(2, 260, 1) X(2, 132, 1) X(2, 68, 1)
-#define TS_MIXED_TILES_1D(X) X(1, 512, 1) X(1, 256, 1) X(1, 128, 1)
-
-template <int ND, int TX, int TY>
-using TileFor = Tile<TX, (ND == 3 ? TY : 1), (ND >= 2)>;
+// Compiled tiles: (problem dimension, threads).  2D: one-row tiles marching
+// y.  1D: one-row tiles, one plane.  (3D problems run k_mix3d.)
+#define TS_MIXED_TILES_2D(X) X(2, 260) X(2, 132) X(2, 68)
+#define TS_MIXED_TILES_1D(X) X(1, 512) X(1, 256) X(1, 128)
 
 // Calls f.template operator()<Tile, SOLVER>() for the compiled tile matching
-// (nd, tx, ty); returns false when there is none.
+// (nd, tx) (ty is 1 for these problems); returns false when there is none.
 template <class F>
 bool with_tile(int nd, int tx, int ty, int solver, F&& f) {
     bool found = false;
-#define TS_TRY(ND_, TX_, TY_)                                                                           \
-    if (!found && nd == ND_ && tx == TX_ && (ND_ < 3 || ty == TY_)) {                                  \
+    (void)ty;
+#define TS_TRY(ND_, TX_)                                                                                \
+    if (!found && nd == ND_ && tx == TX_) {                                                            \
         found = true;                                                                                  \
-        if (solver == TS_RS_HLLC) f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_HLLC>();         \
-        else f.template operator()<TileFor<ND_, TX_, TY_>, TS_RS_ROE_PIKE>();                          \
+        if (solver == TS_RS_HLLC) f.template operator()<Tile<TX_, (ND_ >= 2)>, TS_RS_HLLC>();          \
+        else f.template operator()<Tile<TX_, (ND_ >= 2)>, TS_RS_ROE_PIKE>();                           \
     }
     TS_MIXED_TILES_2D(TS_TRY)
     TS_MIXED_TILES_1D(TS_TRY)
@@ -1143,17 +975,13 @@ bool mixed_tile_info(int nd, int tx, int ty, int solver, size_t* smem, int* per_
                   cudaSuccess;
         // all of the unified L1 / shared storage as shared memory: more resident CTAs
         cudaFuncSetAttribute(k_mix_step<T, S, false>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        if constexpr (!T::HAS_Y)
-            cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
-        if constexpr (!T::HAS_Y)
-            ok = ok && cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
-                           cudaSuccess;
+        cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+        ok = ok && cudaFuncSetAttribute(k_mix_step<T, S, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, b) ==
+                       cudaSuccess;
         if (!ok) return;
-        if constexpr (!T::HAS_Y) {
-            if (batch) {
-                cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, true>, T::NT, T::BYTES);
-                return;
-            }
+        if (batch) {
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, true>, T::NT, T::BYTES);
+            return;
         }
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(per_sm, k_mix_step<T, S, false>, T::NT, T::BYTES);
     });
@@ -1173,9 +1001,8 @@ bool mixed_launch_batch(int nd, int tx, int ty, int solver, int grid, const Prob
     ProbDesc none;
     std::memset(&none, 0, sizeof none);
     return with_tile(nd, tx, ty, solver, [&]<class T, int S>() {
-        if constexpr (!T::HAS_Y)
-            k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items,
-                                                                  close_in_kernel ? 1 : 0);
+        k_mix_step<T, S, true><<<grid, T::NT, T::BYTES, st>>>(none, d_probs, d_ctls, d_items, n_items,
+                                                              close_in_kernel ? 1 : 0);
     });
 }
 
