@@ -235,7 +235,7 @@ ts_status ts_get_step_info(ts_handle* h, ts_step_info* info);
 ts_status ts_set_step_info(ts_handle* h, const ts_step_info* info);
 
 /* Launch shape of the mixed-precision fused kernel: the tile (threads per
-   CTA along x and y; compiled shapes: 3D 32x8, 16x16, 64x4, each thread one
+   CTA along x and y; compiled shapes: 3D 32x8, 16x16, 32x16, each thread one
    cell, marching z; 2D 260, 132, 68 one-row tiles marching y; 1D 512, 256,
    128; one-row tiles own tx - 4 cells) and the number of chunks each tile
    column's march is cut into (0 = chosen from the grid and the SM count).
