@@ -892,7 +892,10 @@ def run_batch2d(args, rank, ws, lr, dist):
     s1 = b.stats()
     clocks = sampler.stop()
     b.close()
-    value = replica_rate(s1["cell_updates"] - s0["cell_updates"], t1 - t0, dist)
+    cu = s1["cell_updates"] - s0["cell_updates"]
+    value = replica_rate(cu, t1 - t0, dist)
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL_UPDATE * cu / (t1 - t0) / 1e9
     if rank == 0:
         print(json.dumps({"metric": METRIC, "value": value, "unit": "cell-updates/s", "n_gpus": ws,
                           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * (t1 - t0) / args.steps,
@@ -901,6 +904,15 @@ def run_batch2d(args, rank, ws, lr, dist):
                           "config": {"workload": "batch of 24 2D quadrant problems (8 x 1024^2, 8 x 512^2, "
                                                  "8 x 256^2), Linear2psLim(BJ), Roe/HLLC", "cells": cells,
                                      "tile": choice},
+                          "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                                       "frac": achieved / peak,
+                                       "traffic": profile_traffic("batch2d", "k_mix_step", cells),
+                                       "kernel": "k_mix_step (batched, one-row 2D tiles)",
+                                       "algorithmic_bytes": BYTES_PER_CELL_UPDATE * cells,
+                                       "basis": "80 B x the batch's cell-updates over the timed stages' wall "
+                                                "time (one launch per (solver, tile) group per stage); traffic: "
+                                                "the captured bytes per cell times the batch's cells, per stage",
+                                       "peak_source": peak_kind},
                           "clocks": clocks, "gpu_launches": s1["launches"] - s0["launches"]}), flush=True)
 
 
