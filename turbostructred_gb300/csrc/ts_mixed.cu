@@ -1081,6 +1081,26 @@ void mixed_items(ProbDesc& d, int tx, int ty, int zchunks, long long slots) {
     d.ncol = d.ncx * ncy;
     const bool march = nd >= 2;
     const int nz = march ? d.kn[2] : 1;
+    if (nd == 2 && zchunks <= 0) {
+        // A stage of one 2D problem ends with its longest march: the chunk
+        // count minimises the modelled stage time, over the waves of items,
+        // (rows per item + 2.5 rows of start-up) x a per-row time that grows
+        // with the wave's share of the CTA slots, 1 + fill (fitted on the
+        // 1024^2 shear layer: 4.2 us per row at 67 % of the slots, 5.0 at
+        // 99 %).  Measured on the shear layer, 132-thread rows: it picks the
+        // fastest of the chunkings tried at 128^2 .. 2048^2 (1024^2: 94
+        // chunks of 11 rows, 67 us per stage against 78 us for 64 chunks of
+        // 16; 256^2: rows of one, 21 us against 51 us).
+        const long long sl = std::max(1LL, slots);
+        double best = 1e300;
+        for (int c = 1; c <= nz; ++c) {
+            const int ch = (nz + c - 1) / c;
+            const long long q = (long long)d.ncol * ((nz + ch - 1) / ch);
+            const long long full = q / sl, rest = q % sl;
+            const double t = (ch + 2.5) * (2.0 * (double)full + (rest ? 1.0 + (double)rest / (double)sl : 0.0));
+            if (t < best - 1e-9) { best = t; zchunks = c; }
+        }
+    }
     if (march && zchunks <= 0) {
         // Chunks of >= 16 planes; pick the count that best fills the
         // persistent grid, charging ~2 planes of start-up per chunk.
