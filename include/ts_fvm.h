@@ -202,11 +202,21 @@ void ts_destroy(ts_handle* h);
    (kernel.h:125-146) for a point-sampled field, from a host array. */
 ts_status ts_set_state(ts_handle* h, const double* values, int32_t layout);
 
-/* Same from a device pointer on the handle's device (no host copy). */
+/* Same from a device pointer on the handle's device (no host copy).  The
+   handle reads it on its own stream, which does not wait for the caller's
+   streams: work that writes device_values must have completed before the
+   call (synchronize its stream).  The call returns after the read, so the
+   buffer may be reused at once. */
 ts_status ts_set_state_device(ts_handle* h, const double* device_values, int32_t layout);
 
 /* Reads Kernel::values back (kernel.h:88). */
 ts_status ts_get_state(ts_handle* h, double* values, int32_t layout);
+
+/* Same into a device buffer on the handle's device (no host copy and no
+   staging buffer; the state of a grid too large for host memory can be
+   read this way).  Returns after the buffer is written; work of the caller
+   that uses device_values may run on any stream after the call. */
+ts_status ts_get_state_device(ts_handle* h, double* device_values, int32_t layout);
 
 /* n_steps calls of ExplicitRungeKuttaFVM::IterationStep (:1440-1491). */
 ts_status ts_step(ts_handle* h, int32_t n_steps, ts_step_info* info);

@@ -224,3 +224,86 @@ def test_mixed_residual_norms_match_fp64(nd, tslib):
         live = ref > 1e-12 * ref.max()
         assert np.all(np.abs(got[live] - ref[live]) <= 1e-4 * ref[live]), (got, ref)
     assert all(np.all(x == 0.0) for x in norms[(1, False)])
+
+
+def test_mixed_3d_grid_beyond_32bit_element_offsets(tslib, oracle_mod):
+    """The largest grids the device holds: 1024^3 cells, whose five FP64
+    variable planes (5 x 1028^3 padded elements) exceed 2^32 elements.  A Sod
+    tube along x, uniform in y and z, Symmetry walls, Linear2psLim(BJ) + Roe:
+    after 20 stages every (y, z) column is the same bit for bit and equals the
+    mixed run of a 1024 x 2 x 2 grid of the same spacing (a cell's update
+    depends only on its stencil, its geometry and the global dt), at the same
+    time; that run is within the mixed bar of the FP64 oracle.  The state is
+    built and read on the device (about 175 GB in use); skipped where less
+    device memory is free."""
+    torch = pytest.importorskip("torch")
+    from turbostructred_gb300 import capi
+    free, _ = torch.cuda.mem_get_info()
+    if free < 200e9:
+        pytest.skip(f"needs about 200 GB of free device memory, {free / 1e9:.0f} GB free")
+    n, steps, gamma = 1024, 20, 1.4
+    sym = (capi.BC_SYMMETRY, 0.0, (0.0, 0.0, 0.0), 0.0)
+    common = dict(ndims=3, nx=n, periodic=(0, 0, 0), recon=3, solver=1, cfl=0.4, max_iter=10**6, max_time=1e30,
+                  bc=[sym] * 6)
+    x = (np.arange(n) + 0.5) / n
+    col = np.zeros((n, 5))
+    col[:, 0] = np.where(x < 0.5, 1.0, 0.125)
+    col[:, 4] = np.where(x < 0.5, 1.0, 0.1) / (gamma - 1.0)
+
+    small = capi.make_case(**dict(common, ny=2, nz=2, length=(1.0, 2.0 / n, 2.0 / n)))
+    with capi.Solver(small, precision=1) as s:
+        s.set_state(np.broadcast_to(col, (2, 2, n, 5)).copy())
+        info_small = s.step(steps)
+        got_small = s.get_state()
+    ref_full, _ = oracle_mod.advance(small, oracle_mod.embed(small, np.broadcast_to(col, (2, 2, n, 5))), steps)
+    e = errors(got_small, interior(small, ref_full).reshape(got_small.shape))
+    assert e["rho"] <= RHO_L1 and e["mom"] <= MOM_E_L1 and e["E"] <= MOM_E_L1, e
+
+    big = capi.make_case(**dict(common, ny=n, nz=n, length=(1.0, 1.0, 1.0)))
+    u = torch.from_numpy(col).cuda().expand(n, n, n, 5).contiguous()
+    torch.cuda.synchronize()  # the solver reads u on its own stream
+    with capi.Solver(big, precision=1) as s:
+        s.set_state_device(u.data_ptr())
+        info_big = s.step(steps)
+        s.get_state_device(u.data_ptr())
+    torch.cuda.synchronize()
+    assert info_big["health"] == 0 and info_big["iteration"] == info_small["iteration"] == steps
+    assert info_big["time"] == info_small["time"]
+    ref_col = u[0, 0]
+    for k in range(0, n, 64):
+        assert float((u[k:k + 64] - ref_col).abs().amax()) == 0.0, k
+    assert np.array_equal(ref_col.cpu().numpy(), got_small[0, 0])
+    del u, ref_col
+    torch.cuda.empty_cache()
+
+
+@pytest.mark.parametrize("recon,limiter,right", [(3, 0, (0.125, 0.1)), (3, 1, (0.125, 0.1)), (1, 0, (0.9, 0.9)),
+                                                 (2, 0, (0.125, 0.1))], ids=["bj", "venkat", "linear", "eno2"])
+def test_mixed_3d_tile_halo_copies_agree(recon, limiter, right, tslib):
+    """A cell's FP32 working copy and face states are computed by its own CTA
+    and, as halo and ring cells, by the neighbouring CTAs along other code
+    paths; they must agree bit for bit.  A shock tube along x (Sod; a weak
+    jump for the unlimited reconstruction), uniform in y and z (96 x 40 x 24
+    cells: several tiles along x and y, several z chunks), advanced 20 stages
+    in one call (the pending update carried from stage to stage): every
+    (y, z) column is the same bit for bit, and equals the run of a 96 x 2 x 2
+    grid of the same spacing."""
+    from turbostructred_gb300 import capi
+    n, ny, nz, steps, gamma = 96, 40, 24, 20, 1.4
+    sym = (capi.BC_SYMMETRY, 0.0, (0.0, 0.0, 0.0), 0.0)
+    common = dict(ndims=3, nx=n, periodic=(0, 0, 0), recon=recon, limiter=limiter, solver=1, cfl=0.4,
+                  max_iter=10**6, max_time=1e30, bc=[sym] * 6)
+    x = (np.arange(n) + 0.5) / n
+    col = np.zeros((n, 5))
+    col[:, 0] = np.where(x < 0.5, 1.0, right[0])
+    col[:, 4] = np.where(x < 0.5, 1.0, right[1]) / (gamma - 1.0)
+    out = {}
+    for m, (a, b) in (("big", (ny, nz)), ("small", (2, 2))):
+        case = capi.make_case(**dict(common, ny=a, nz=b, length=(1.0, a / n, b / n)))
+        with capi.Solver(case, precision=1) as s:
+            s.set_state(np.broadcast_to(col, (b, a, n, 5)).copy())
+            out[m] = (s.step(steps), s.get_state())
+    (ib, big), (isml, small) = out["big"], out["small"]
+    assert ib["health"] == 0 and ib["time"] == isml["time"]
+    assert np.array_equal(big, np.broadcast_to(big[0, 0], big.shape))
+    assert np.array_equal(big[0, 0], small[0, 0])

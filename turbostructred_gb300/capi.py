@@ -119,8 +119,8 @@ class ServerStats(C.Structure):
 
 
 EXPORTS = [
-    "ts_create", "ts_destroy", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
-    "ts_run", "ts_set_tile",
+    "ts_create", "ts_destroy", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_get_state_device",
+    "ts_step", "ts_step_timed", "ts_run", "ts_set_tile",
     "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates", "ts_state_doubles",
     "ts_fill_scenario", "ts_hash_uniform", "ts_last_error", "ts_status_string",
     "ts_batch_create", "ts_batch_destroy", "ts_batch_add", "ts_batch_problem_bytes", "ts_batch_step",
@@ -149,6 +149,7 @@ def load(path: str = LIB_PATH):
     L.ts_destroy.restype = None
     L.ts_set_state.argtypes = [C.c_void_p, P(C.c_double), C.c_int32]
     L.ts_set_state_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
+    L.ts_get_state_device.argtypes = [C.c_void_p, C.c_void_p, C.c_int32]
     L.ts_get_state.argtypes = [C.c_void_p, P(C.c_double), C.c_int32]
     L.ts_step.argtypes = [C.c_void_p, C.c_int32, P(StepInfo)]
     L.ts_step_timed.argtypes = [C.c_void_p, C.c_int32, P(StepInfo), P(Timing)]
@@ -207,8 +208,8 @@ def load(path: str = LIB_PATH):
         getattr(L, name).restype = C.c_int
     L.ts_last_error.restype = C.c_char_p
     L.ts_status_string.restype = C.c_char_p
-    for name in ("ts_create", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_step", "ts_step_timed",
-                 "ts_run",
+    for name in ("ts_create", "ts_set_state", "ts_set_state_device", "ts_get_state", "ts_get_state_device",
+                 "ts_step", "ts_step_timed", "ts_run",
                  "ts_get_step_info", "ts_set_step_info", "ts_synchronize", "ts_grid_coordinates",
                  "ts_fill_scenario"):
         getattr(L, name).restype = C.c_int
@@ -411,6 +412,9 @@ class Solver:
         check(self.lib.ts_set_state(self.h, v.ctypes.data_as(C.POINTER(C.c_double)), layout))
 
     def set_state_device(self, ptr: int, layout: int = LAYOUT_INTERIOR):
+        """The state from device memory at `ptr`; whatever wrote it must have
+        completed (e.g. torch.cuda.synchronize()): the solver reads it on its
+        own stream."""
         check(self.lib.ts_set_state_device(self.h, C.c_void_p(ptr), layout))
 
     def get_state(self, layout: int = LAYOUT_INTERIOR, out: np.ndarray | None = None) -> np.ndarray:
@@ -419,6 +423,11 @@ class Solver:
             out = np.empty(shape)
         check(self.lib.ts_get_state(self.h, out.ctypes.data_as(C.POINTER(C.c_double)), layout))
         return out
+
+    def get_state_device(self, ptr: int, layout: int = LAYOUT_INTERIOR):
+        """The state into device memory at `ptr` (on the solver's device), in
+        the layout of get_state."""
+        check(self.lib.ts_get_state_device(self.h, C.c_void_p(ptr), layout))
 
     def step(self, n: int = 1) -> dict:
         si = StepInfo()

@@ -384,26 +384,36 @@ ts_status ts_set_state_device(ts_handle* h, const double* values, int32_t layout
     return set_state_impl(h, values, layout, true);
 }
 
-ts_status ts_get_state(ts_handle* h, double* values, int32_t layout) {
+static ts_status get_state_impl(ts_handle* h, double* values, int32_t layout, bool device_ptr) {
     if (!h || !values) return fail(TS_ERR_INVALID, "NULL argument");
     if (layout != TS_LAYOUT_INTERIOR && layout != TS_LAYOUT_WITH_GHOSTS) return fail(TS_ERR_INVALID, "bad layout");
     DeviceGuard g(h->device);
     const size_t nd = ts_state_doubles(&h->cfg, layout);
     const long long ncell = (long long)(nd / NV);
-    ts_status s = h->ensure_stage(nd);
-    if (s != TS_OK) return s;
+    ts_status s;
+    if (!device_ptr && (s = h->ensure_stage(nd)) != TS_OK) return s;
     if (h->cfg.precision == TS_PRECISION_MIXED) {
         if ((s = h->pull_ctl()) != TS_OK) return s;
         mixed_materialize(h->mb, h->ph, h->stream);
         h->ctl_h->dt_apply = 0.0;  // the device copy is cleared by the apply pass
     }
+    double* dst = device_ptr ? values : h->stage_d;
     const int blk = 256;
-    k_gather<<<(unsigned)((ncell + blk - 1) / blk), blk, 0, h->stream>>>(h->stage_d, h->L, h->state_planes(),
+    k_gather<<<(unsigned)((ncell + blk - 1) / blk), blk, 0, h->stream>>>(dst, h->L, h->state_planes(),
                                                                           layout == TS_LAYOUT_WITH_GHOSTS, ncell);
     TS_CUDA(cudaGetLastError());
-    TS_CUDA(cudaMemcpyAsync(values, h->stage_d, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    if (!device_ptr)
+        TS_CUDA(cudaMemcpyAsync(values, h->stage_d, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TS_CUDA(cudaStreamSynchronize(h->stream));
     return TS_OK;
+}
+
+ts_status ts_get_state(ts_handle* h, double* values, int32_t layout) {
+    return get_state_impl(h, values, layout, false);
+}
+
+ts_status ts_get_state_device(ts_handle* h, double* values, int32_t layout) {
+    return get_state_impl(h, values, layout, true);
 }
 
 ts_status ts_step(ts_handle* h, int32_t n_steps, ts_step_info* info) {

@@ -222,19 +222,23 @@ __host__ __device__ __forceinline__ int kind_of(const MixPhys& mp) {
 // variable from its value w0 and neighbours nm/np along x, y, z: the
 // reconstruction of Linear2PointsStencil.h:66-97, ENO2PointsStencil.h:20-58
 // and Linear2psLim.h:63-132 with the Barth-Jespersen and Venkatakrishnan
-// limiters (Limiters.h:28-115), in FP32.
+// limiters (Limiters.h:28-115), in FP32: dd[ax] the unlimited half-slope
+// (explicitly rounded) and lim the limiter factor (1 without a limiter).  The
+// caller forms the face states as fma(+-dd, lim, w0) on every code path, so a
+// ring cell's states are the same bits in every CTA that computes them.
 template <int KIND>
 __device__ __forceinline__ void half_slopes(float w0, const float nm[3], const float np[3], const AxisGeo g[3],
-                                            float eps2, float dd[3]) {
+                                            float eps2, float dd[3], float& lim) {
+    lim = 1.0f;
     if (KIND == K_ENO2) {
 #pragma unroll
         for (int ax = 0; ax < 3; ++ax) {
             const float gl = (w0 - nm[ax]) * g[ax].il, gr = (np[ax] - w0) * g[ax].ir;
-            dd[ax] = (fabsf(gl) < fabsf(gr) ? gl : gr) * g[ax].hh;
+            dd[ax] = __fmul_rn(fabsf(gl) < fabsf(gr) ? gl : gr, g[ax].hh);
         }
     } else {
 #pragma unroll
-        for (int ax = 0; ax < 3; ++ax) dd[ax] = (np[ax] - nm[ax]) * g[ax].ks;
+        for (int ax = 0; ax < 3; ++ax) dd[ax] = __fmul_rn(np[ax] - nm[ax], g[ax].ks);
     }
     if (KIND == K_LIM_BJ) {
         // the smallest admissible ratio over the 6 face projections +-dd;
@@ -246,9 +250,7 @@ __device__ __forceinline__ void half_slopes(float w0, const float nm[3], const f
             umin = fminf(umin, fminf(nm[ax], np[ax]));
             dmax = fmaxf(dmax, fabsf(dd[ax]));
         }
-        const float lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) dd[ax] *= lim;
+        lim = fminf(1.0f, fminf(umax - w0, w0 - umin) / dmax);
     }
     if (KIND == K_LIM_VK) {
         float umax = w0, umin = w0;
@@ -257,7 +259,6 @@ __device__ __forceinline__ void half_slopes(float w0, const float nm[3], const f
             umax = fmaxf(umax, fmaxf(nm[ax], np[ax]));
             umin = fminf(umin, fminf(nm[ax], np[ax]));
         }
-        float lim = 1.0f;
         if (umax - umin > 0.0f) {
             const float iun = 2.0f / (umax - umin);
 #pragma unroll
@@ -273,8 +274,6 @@ __device__ __forceinline__ void half_slopes(float w0, const float nm[3], const f
                 }
             }
         }
-#pragma unroll
-        for (int ax = 0; ax < 3; ++ax) dd[ax] *= lim;
     }
 }
 
@@ -402,8 +401,10 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
     int sk, zs;
     resolve(j, d.kn[2], d.kper[2], 4, sk, zs);
     const float cfz = dtf * __ldg(&d.kgeo[2][sk + d.kgoff[2]].ih);
-    // element offsets fit 32 bits (5 planes < 2^32, checked on the host)
-    const unsigned int plane = (unsigned int)d.L.plane;
+    // offsets within a variable plane fit 32 bits (a plane holds < 2^31
+    // elements, checked on the host); the stride between the five planes is
+    // 64-bit (five planes of a 1024^3 grid exceed 2^32 elements)
+    const size_t plane = (size_t)d.L.plane;
     const unsigned int zoff = (unsigned int)d.kbase + (unsigned int)sk * (unsigned int)d.kstr[2];
     const int slot = T::wslot(j);
     const bool own_plane = j >= it.z0 && j < it.z1;
@@ -424,18 +425,20 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
             // periodic halo cell of an edge tile: not in the staged box
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
-                u[v] = __ldg(Uin + (zoff + (unsigned int)c.goff + v * plane));
-                r[v] = __ldg(Rin + (zoff + (unsigned int)c.goff + v * plane));
+                u[v] = __ldg(Uin + (zoff + (unsigned int)c.goff) + v * plane);
+                r[v] = __ldg(Rin + (zoff + (unsigned int)c.goff) + v * plane);
             }
         }
         const float cf = c.cfxy * cfz;
-        float inc[NV], w[NV];
-#pragma unroll
-        for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
+        float w[NV];
+        // the working copy as explicit FMAs (never split by the compiler): a
+        // cell's copy must be the same bits in the CTA that owns it (position
+        // 0) and in every CTA that converts it as a halo cell (position 1),
+        // whose unrolled code could otherwise be contracted differently
         const double e4 = stiff ? u[4] - mp.einf_d : u[4];  // shifted energy (uniform choice)
 #pragma unroll
-        for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
-        w[4] = f64_to_f32(e4) + inc[4];
+        for (int v = 0; v < 4; ++v) w[v] = __fmaf_rn(cf, r[v], f64_to_f32(u[v]));
+        w[4] = __fmaf_rn(cf, r[4], f64_to_f32(e4));
         if (c.xs >= 0 || c.ys >= 0 || zs >= 0) {
             // a halo cell beyond a non-periodic side: the BC of the boundary
             // face of its row (source cell indices recovered from the box or
@@ -460,7 +463,7 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
 #pragma unroll
             for (int v = 0; v < NV; ++v) {
                 pu.u[v] = u[v];
-                pu.inc[v] = inc[v];
+                pu.inc[v] = __fmul_rn(cf, r[v]);  // dt R / V in FP32, added to U^n in FP64
             }
             if (pu.on && !(w[4] == w[4])) health |= TS_HEALTH_NAN;
         }
@@ -471,12 +474,12 @@ __device__ __forceinline__ void convert(const ProbDesc& d, const Item3& it, cons
 __device__ __forceinline__ void apply_pending(const ProbDesc& d, double* __restrict__ Uout, const PendingU& pu,
                                               unsigned int& health) {
     if (!pu.on) return;
-    const unsigned int plane = (unsigned int)d.L.plane;
+    const size_t plane = (size_t)d.L.plane;
     double un[NV];
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         un[v] = pu.u[v] + f32_to_f64(pu.inc[v]);
-        __stcs(Uout + (pu.off + v * plane), un[v]);
+        __stcs(Uout + pu.off + v * plane, un[v]);
     }
     // rho > 0 tested on the bit pattern (no FP64 comparison)
     const long long b = __double_as_longlong(un[0]);
@@ -535,23 +538,28 @@ __device__ __forceinline__ void reconstruct(const ProbDesc& d, const Item3& it, 
 #pragma unroll
         for (int v = 0; v < NV; ++v) {
             const float w0 = smw[T::w(s0, v, box)];
-            float nm[3], np[3], dd[3] = {0.0f, 0.0f, 0.0f};
+            float nm[3], np[3], dd[3] = {0.0f, 0.0f, 0.0f}, lim = 1.0f;
             nm[0] = smw[T::w(s0, v, box - 1)];
             np[0] = smw[T::w(s0, v, box + 1)];
             nm[1] = smw[T::w(s0, v, box - T::BX)];
             np[1] = smw[T::w(s0, v, box + T::BX)];
             nm[2] = smw[T::w(sm1, v, box)];
             np[2] = smw[T::w(sp1, v, box)];
-            if (KIND != K_PWC) half_slopes<KIND>(w0, nm, np, g, eps2, dd);
+            if (KIND != K_PWC) half_slopes<KIND>(w0, nm, np, g, eps2, dd, lim);
+            // face states as explicit FMAs (never split or re-fused by the
+            // compiler): a ring cell's state is computed by its own CTA and
+            // by the neighbouring CTA along different code paths, and must
+            // agree
             if (p == 0) {
-                fv[T::fvx(v, it.cy, it.cx + 1)] = w0 + dd[0];
-                fv[T::fvy(v, it.cy + 1, it.cx)] = w0 + dd[1];
-                urx.v[v] = w0 - dd[0];
-                ury.v[v] = w0 - dd[1];
-                ulz.v[v] = w0 + dd[2];
-                urz.v[v] = w0 - dd[2];
+                fv[T::fvx(v, it.cy, it.cx + 1)] = __fmaf_rn(dd[0], lim, w0);
+                fv[T::fvy(v, it.cy + 1, it.cx)] = __fmaf_rn(dd[1], lim, w0);
+                urx.v[v] = __fmaf_rn(-dd[0], lim, w0);
+                ury.v[v] = __fmaf_rn(-dd[1], lim, w0);
+                ulz.v[v] = __fmaf_rn(dd[2], lim, w0);
+                urz.v[v] = __fmaf_rn(-dd[2], lim, w0);
             } else {
-                fv[fdst + v * fstride] = w0 + fsg * (fax ? dd[1] : dd[0]);
+                const float dsel = fax ? dd[1] : dd[0];
+                fv[fdst + v * fstride] = __fmaf_rn(fsg > 0.0f ? dsel : -dsel, lim, w0);
             }
         }
     }
@@ -707,9 +715,9 @@ __device__ __forceinline__ void residual3(const ProbDesc& d, const Item3& it, co
         for (int v = 0; v < NV; ++v) nrm[v] += vol * fabsf(R[v]);
     }
     const unsigned int o = (unsigned int)it.own_off + (unsigned int)k * (unsigned int)d.kstr[2];
-    const unsigned int plane = (unsigned int)d.L.plane;
+    const size_t plane = (size_t)d.L.plane;
 #pragma unroll
-    for (int v = 0; v < NV; ++v) __stcs(Rout + (o + v * plane), R[v]);
+    for (int v = 0; v < NV; ++v) __stcs(Rout + o + v * plane, R[v]);
 }
 
 // One work item: the tile column (i0, j0) over planes [z0, z1).  Planes
@@ -929,8 +937,6 @@ bool mix3d_tile_info(int tx, int ty, int solver, int recon, int limiter, size_t*
 ts_status mix3d_make_maps(const ProbDesc& d, int tx, int ty, Mix3dMaps& maps, std::string& err) {
     const Layout& L = d.L;
     if (L.nd != 3 || L.gx != HB3 || L.gy != HB3 || L.gz != HB3) { err = "3D layout expected"; return TS_ERR_INVALID; }
-    // the kernel addresses the five variable planes with 32-bit element offsets
-    if ((unsigned long long)L.plane * NV >= (1ULL << 32)) { err = "grid too large for the 3D mixed kernel"; return TS_ERR_INVALID; }
     const int bx = tx + 2 * HB3, by = ty + 2 * HB3;
     ts_status s;
     for (int b = 0; b < 2; ++b) {
