@@ -307,3 +307,35 @@ def test_mixed_3d_tile_halo_copies_agree(recon, limiter, right, tslib):
     assert ib["health"] == 0 and ib["time"] == isml["time"]
     assert np.array_equal(big, np.broadcast_to(big[0, 0], big.shape))
     assert np.array_equal(big[0, 0], small[0, 0])
+
+
+@pytest.mark.parametrize("axis", [0, 1], ids=["tube_x", "tube_y"])
+def test_mixed_2d_tiles_and_chunks_agree(axis, tslib):
+    """The 2D kernel on a shock tube along x (across one-row tiles) or along
+    y (the marching axis, across row chunks), uniform along the other axis:
+    after 20 stages in one call every row (column) is the same bit for bit,
+    and equals the run of a grid two cells wide of the same spacing."""
+    from turbostructred_gb300 import capi
+    n, m, steps, gamma = 300, 70, 20, 1.4
+    sym = (capi.BC_SYMMETRY, 0.0, (0.0, 0.0, 0.0), 0.0)
+    x = (np.arange(n) + 0.5) / n
+    col = np.zeros((n, 5))
+    col[:, 0] = np.where(x < 0.5, 1.0, 0.125)
+    col[:, 4] = np.where(x < 0.5, 1.0, 0.1) / (gamma - 1.0)
+    out = {}
+    for name, w in (("wide", m), ("narrow", 2)):
+        dims = dict(nx=n, ny=w, length=(1.0, w / n, 1.0)) if axis == 0 else dict(nx=w, ny=n, length=(w / n, 1.0, 1.0))
+        case = capi.make_case(ndims=2, periodic=(0, 0, 1), recon=3, solver=3, cfl=0.4, max_iter=10**6,
+                              max_time=1e30, bc=[sym] * 6, **dims)
+        st = np.broadcast_to(col, (1, w, n, 5)).copy() if axis == 0 else \
+            np.broadcast_to(col[:, None, :], (1, n, w, 5)).copy()
+        with capi.Solver(case, precision=1) as s:
+            s.set_state(st)
+            out[name] = (s.step(steps), s.get_state())
+    (iw, wide), (inr, narrow) = out["wide"], out["narrow"]
+    assert iw["health"] == 0 and iw["time"] == inr["time"]
+    line = (lambda a, k: a[0, k]) if axis == 0 else (lambda a, k: a[0, :, k])
+    ref = line(wide, 0)
+    for k in range(m):
+        assert np.array_equal(line(wide, k), ref), k
+    assert np.array_equal(ref, line(narrow, 0))

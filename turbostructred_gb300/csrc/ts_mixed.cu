@@ -198,10 +198,15 @@ __device__ __forceinline__ void store(const ProbDesc& d, float* sm, double* __re
     const float cf = bp.cfxy * cfz;
     float inc[NV], w[NV];
 #pragma unroll
-    for (int v = 0; v < NV; ++v) inc[v] = cf * pf.r[v];
+    // explicitly rounded products and FMAs (never split or re-fused by the
+    // compiler): store() is inlined at several call sites, and a row's
+    // working copy must be the same bits in the CTA that owns the row and in
+    // the CTA that loads it as a halo row of its chunk
+    for (int v = 0; v < NV; ++v) inc[v] = __fmul_rn(cf, pf.r[v]);
 #pragma unroll
-    for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(pf.u[v]) + inc[v];
-    w[4] = (mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf.u[4] - mp.einf_d) : f64_to_f32(pf.u[4])) + inc[4];
+    for (int v = 0; v < 4; ++v) w[v] = __fmaf_rn(cf, pf.r[v], f64_to_f32(pf.u[v]));
+    w[4] = __fmaf_rn(cf, pf.r[4],
+                     mp.eos == TS_EOS_STIFFENED_GAS ? f64_to_f32(pf.u[4] - mp.einf_d) : f64_to_f32(pf.u[4]));
     // BC of the boundary face of this ghost's row (the x sides' faces are
     // numbered by the plane, the marching sides' by x)
     if (bp.xs >= 0) bc32(mp, bc_id32(mp, bp.xs, sk), 0, w);
@@ -801,10 +806,10 @@ __global__ void __launch_bounds__(512, 1) k_mix_tail(const ProbDesc* __restrict_
             const float cf = bp.cfxy * (s_dtf * gz.ih);
             float inc[NV], w[NV];
 #pragma unroll
-            for (int v = 0; v < NV; ++v) inc[v] = cf * r[v];
+            for (int v = 0; v < NV; ++v) inc[v] = __fmul_rn(cf, r[v]);  // as store()
 #pragma unroll
-            for (int v = 0; v < 4; ++v) w[v] = f64_to_f32(u[v]) + inc[v];
-            w[4] = (stiff ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4])) + inc[4];
+            for (int v = 0; v < 4; ++v) w[v] = __fmaf_rn(cf, r[v], f64_to_f32(u[v]));
+            w[4] = __fmaf_rn(cf, r[4], stiff ? f64_to_f32(u[4] - mp.einf_d) : f64_to_f32(u[4]));
 #pragma unroll
             for (int v = 0; v < NV; ++v) sm[T::w(0, v, bp.box)] = w[v];
 #pragma unroll
