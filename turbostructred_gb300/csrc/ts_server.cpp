@@ -35,7 +35,7 @@ using Clock = std::chrono::steady_clock;
 
 // Page-locked host buffers for request states, kept by size and reused: the
 // worker's uploads and read-backs then run as DMA transfers instead of
-// through the driver's pageable staging (about 5 GB/s measured on the served
+// through CUDA's staging of pageable memory (about 5 GB/s measured on the served
 // stream, slow enough that the copies of one pass outlasted the chunk of
 // stages in flight and left the GPU idle).  Past kPinnedCap bytes of pinned
 // buffers, or when pinning fails, a buffer is ordinary memory.
