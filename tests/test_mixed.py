@@ -4,7 +4,8 @@ accumulation and dt) against the FP64 reference results.
 Tolerance: density L1 error relative to the FP64 result <= 1e-5 (the bar the
 mixed path is built to), momentum/energy L1 <= 1e-4; checked on the
 reference's own fixtures and on oracle runs.  Results are independent of the
-kernel's tile shape, bit for bit.
+tile shape and the z / row chunking bit for bit in 1D and 3D and of the row
+chunking in 2D; 2D tiles of other widths agree to FP32 rounding.
 """
 import numpy as np
 import pytest
@@ -112,12 +113,12 @@ def test_mixed_tile_and_chunk_independent(nd, tslib):
     if nd == 3:
         case = O.make_case(ndims=3, nx=37, ny=29, nz=21, periodic=(1, 0, 0), recon=3, solver=1, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, SYM, SYM])
-        tiles = [(32, 8, 0), (16, 16, 0), (32, 8, 1), (32, 8, 3), (16, 16, 7), (32, 8, 21)]
+        tiles = [(32, 8, 0), (16, 16, 0), (32, 16, 0), (32, 8, 1), (32, 8, 3), (16, 16, 7), (32, 8, 21)]
         scen, params = 2, [1.0, 0.1, 10.0, 0.2, 0.01]
     elif nd == 2:
         case = O.make_case(ndims=2, nx=70, ny=45, periodic=(1, 0, 1), recon=3, solver=3, cfl=0.4,
                            bc=[NAT, NAT, SYM, NAT, NAT, NAT])
-        tiles = [(260, 1, 0), (132, 1, 0), (68, 1, 0), (260, 1, 4), (68, 1, 1)]
+        tiles = [(260, 1, 0), (260, 1, 4), (260, 1, 45), (132, 1, 0), (68, 1, 0), (68, 1, 1)]
         scen, params = 1, [2.0, 1.0, 0.5, 2.5, 0.01]
     else:
         case = O.make_case(ndims=1, nx=1000, periodic=(0, 1, 1), recon=3, cfl=0.5, bc=[NAT] * 6)
@@ -126,10 +127,16 @@ def test_mixed_tile_and_chunk_independent(nd, tslib):
     outs = [run(case, full, 9, 1, tile=t)[0] for t in tiles]
     # the same launch configuration is deterministic bit for bit
     assert np.array_equal(run(case, full, 9, 1, tile=tiles[0])[0], outs[0])
-    # other tiles and z chunkings are other compiled instances (the compiler
-    # may contract FP32 multiply-adds differently): equal to FP32 rounding
-    for o in outs[1:]:
-        assert float(np.abs(o - outs[0]).max() / np.abs(outs[0]).max()) <= 1e-5
+    # every face is solved from the same bits by whichever CTA and role
+    # computes it (measured: 3D tiles and z chunks, 1D tiles, 2D row chunks
+    # of one tile width bit for bit); 2D tiles of other widths are other
+    # compiled instances of the row kernel and agree to FP32 rounding
+    # (measured 1.5e-7 relative)
+    for t, o in zip(tiles[1:], outs[1:]):
+        if nd != 2 or t[0] == tiles[0][0]:
+            assert np.array_equal(o, outs[0]), t
+        else:
+            assert float(np.abs(o - outs[0]).max() / np.abs(outs[0]).max()) <= 1e-5, t
 
 
 def test_mixed_get_state_midway_is_seamless(tslib):
