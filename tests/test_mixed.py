@@ -346,3 +346,29 @@ def test_mixed_2d_tiles_and_chunks_agree(axis, tslib):
     for k in range(m):
         assert np.array_equal(line(wide, k), ref), k
     assert np.array_equal(ref, line(narrow, 0))
+
+
+@pytest.mark.parametrize("precision", [0, 1], ids=["fp64", "mixed"])
+def test_state_through_pinned_host_memory(precision, tslib):
+    """ts_set_state / ts_get_state on page-locked host buffers (read and
+    written in place by the scatter and gather kernels) give the same state,
+    bit for bit, as on ordinary host memory."""
+    torch = pytest.importorskip("torch")
+    import ctypes as C
+    from turbostructred_gb300 import capi
+    case = capi.make_case(ndims=3, nx=40, ny=24, nz=20, periodic=(0, 0, 0), recon=3, solver=1, cfl=0.4,
+                          bc=[SYM] * 6)
+    ic = capi.fill_scenario(case, capi.SCENARIO_BLAST, 5, [1.0, 0.1, 10.0, 0.15, 0.01])
+    lib = capi.load()
+    P = C.POINTER(C.c_double)
+    with capi.Solver(case, precision=precision) as s:
+        s.set_state(ic)
+        s.step(7)
+        plain = s.get_state()
+    pin_in = torch.from_numpy(ic.reshape(-1).copy()).pin_memory()
+    pin_out = torch.zeros(ic.size, dtype=torch.float64).pin_memory()
+    with capi.Solver(case, precision=precision) as s:
+        capi.check(lib.ts_set_state(s.h, C.cast(pin_in.data_ptr(), P), capi.LAYOUT_INTERIOR))
+        s.step(7)
+        capi.check(lib.ts_get_state(s.h, C.cast(pin_out.data_ptr(), P), capi.LAYOUT_INTERIOR))
+    assert np.array_equal(pin_out.numpy().reshape(plain.shape), plain)

@@ -618,11 +618,13 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
         if ((s = take(sizeof(float) * NV * L.plane, (void**)&d.R[k])) != TS_OK) { undo(); return s; }
     }
     b->place(slot);
-    // initial state: host -> staging -> U[0]; no pending residual.  All on the
-    // upload stream; the main stream waits for it before its next work, so
-    // stages already queued there keep running meanwhile.
+    // initial state: host -> staging -> U[0] (page-locked host memory is read
+    // in place); no pending residual.  All on the upload stream; the main
+    // stream waits for it before its next work, so stages already queued
+    // there keep running meanwhile.
     const size_t nvals = (size_t)L.cells() * NV;
-    if (b->ustage_doubles < nvals) {
+    const double* pinned = static_cast<const double*>(pinned_device_ptr(values));
+    if (!pinned && b->ustage_doubles < nvals) {
         TB_CUDA(cudaStreamSynchronize(b->ustream));
         cudaFree(b->ustage);
         b->ustage = nullptr;
@@ -631,8 +633,8 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
         b->ustage_doubles = nvals;
     }
     cudaStream_t us = b->ustream;
-    TB_CUDA(cudaMemcpyAsync(b->ustage, values, nvals * sizeof(double), cudaMemcpyHostToDevice, us));
-    k_b_scatter<<<(unsigned)((L.cells() + 255) / 256), 256, 0, us>>>(b->ustage, L, d.U[0]);
+    if (!pinned) TB_CUDA(cudaMemcpyAsync(b->ustage, values, nvals * sizeof(double), cudaMemcpyHostToDevice, us));
+    k_b_scatter<<<(unsigned)((L.cells() + 255) / 256), 256, 0, us>>>(pinned ? pinned : b->ustage, L, d.U[0]);
     TB_CUDA(cudaMemsetAsync(d.R[0], 0, sizeof(float) * NV * L.plane, us));
     Ctl& c = b->h_ctl[slot];
     std::memset(&c, 0, sizeof c);
@@ -737,7 +739,12 @@ ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* in
     const bool finished = b->h_ctl[slot].stop_req != 0;
     cudaStream_t st = finished ? b->dstream : b->stream;
     mixed_apply(b->d_desc, slot, L.cells(), st);
-    if (values) {
+    double* pinned = values ? static_cast<double*>(pinned_device_ptr(values)) : nullptr;
+    if (values && pinned) {
+        // page-locked host memory: gathered in place
+        k_b_gather<<<blocks, 256, 0, st>>>(pinned, b->d_desc, slot);
+        TB_CUDA(cudaGetLastError());
+    } else if (values) {
         const size_t nvals = (size_t)L.cells() * NV;
         if (b->dstage_doubles < nvals) {
             cudaFree(b->dstage);

@@ -362,9 +362,13 @@ static ts_status set_state_impl(ts_handle* h, const double* values, int32_t layo
         if ((s = h->push_ctl()) != TS_OK) return s;
     }
     if (!device_ptr) {
-        if ((s = h->ensure_stage(nd)) != TS_OK) return s;
-        TS_CUDA(cudaMemcpyAsync(h->stage_d, values, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
-        src = h->stage_d;
+        if (const void* pd = pinned_device_ptr(values)) {
+            src = static_cast<const double*>(pd);  // page-locked: read in place
+        } else {
+            if ((s = h->ensure_stage(nd)) != TS_OK) return s;
+            TS_CUDA(cudaMemcpyAsync(h->stage_d, values, nd * sizeof(double), cudaMemcpyHostToDevice, h->stream));
+            src = h->stage_d;
+        }
     }
     const int blk = 256;
     k_scatter<<<(unsigned)((ncell + blk - 1) / blk), blk, 0, h->stream>>>(src, h->L, h->state_planes(),
@@ -391,18 +395,21 @@ static ts_status get_state_impl(ts_handle* h, double* values, int32_t layout, bo
     const size_t nd = ts_state_doubles(&h->cfg, layout);
     const long long ncell = (long long)(nd / NV);
     ts_status s;
-    if (!device_ptr && (s = h->ensure_stage(nd)) != TS_OK) return s;
+    // page-locked host memory is written in place, like device memory
+    double* pinned = device_ptr ? nullptr : static_cast<double*>(pinned_device_ptr(values));
+    const bool staged = !device_ptr && !pinned;
+    if (staged && (s = h->ensure_stage(nd)) != TS_OK) return s;
     if (h->cfg.precision == TS_PRECISION_MIXED) {
         if ((s = h->pull_ctl()) != TS_OK) return s;
         mixed_materialize(h->mb, h->ph, h->stream);
         h->ctl_h->dt_apply = 0.0;  // the device copy is cleared by the apply pass
     }
-    double* dst = device_ptr ? values : h->stage_d;
+    double* dst = device_ptr ? values : (pinned ? pinned : h->stage_d);
     const int blk = 256;
     k_gather<<<(unsigned)((ncell + blk - 1) / blk), blk, 0, h->stream>>>(dst, h->L, h->state_planes(),
                                                                           layout == TS_LAYOUT_WITH_GHOSTS, ncell);
     TS_CUDA(cudaGetLastError());
-    if (!device_ptr)
+    if (staged)
         TS_CUDA(cudaMemcpyAsync(values, h->stage_d, nd * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
     TS_CUDA(cudaStreamSynchronize(h->stream));
     return TS_OK;

@@ -2,6 +2,8 @@
 // GB300-native explicit FVM step.  Not part of the C ABI.
 #pragma once
 
+#include <cuda_runtime.h>
+
 #include <cstddef>
 #include <cstdint>
 #include <string>
@@ -16,6 +18,19 @@
 #endif
 
 namespace ts {
+
+// The device address of page-locked host memory (cudaHostAlloc,
+// cudaHostRegister, a pinned PyTorch tensor), or nullptr for any other
+// pointer.  Kernels read and write such memory in place over the host link,
+// so a state in it needs no staging copy through device memory.
+inline void* pinned_device_ptr(const void* p) {
+    cudaPointerAttributes a;
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
 
 constexpr int NV = 5;      // rho, rho*u, rho*v, rho*w, rho*E
 constexpr int GHOST = 2;   // ghost layers per active axis in device arrays
