@@ -222,9 +222,10 @@ ts_status ts_get_state_device(ts_handle* h, double* device_values, int32_t layou
 ts_status ts_step(ts_handle* h, int32_t n_steps, ts_step_info* info);
 
 /* Device timing of n steps, for benchmarks: CUDA events recorded on the
-   handle's stream around the whole run and around every kernel launch
-   (launched one by one, not from a graph).  Per-kernel times are averages
-   per launch; names identify the kernels of one step in launch order. */
+   handle's stream around the whole run and around every kernel launch of up
+   to 64 evenly spaced steps (launched one by one, not from a graph).
+   Per-kernel times are averages per launch over those steps; names identify
+   the kernels of one step in launch order. */
 #define TS_MAX_KERNELS 16
 typedef struct ts_timing {
     double total_ms;
