@@ -623,7 +623,7 @@ ts_status ts_batch_add(ts_batch* b, const ts_config* cfg, const double* values, 
     // stream waits for it before its next work, so stages already queued
     // there keep running meanwhile.
     const size_t nvals = (size_t)L.cells() * NV;
-    const double* pinned = static_cast<const double*>(pinned_device_ptr(values));
+    const double* pinned = static_cast<const double*>(pinned_device_ptr(values, b->device));
     if (!pinned && b->ustage_doubles < nvals) {
         TB_CUDA(cudaStreamSynchronize(b->ustream));
         cudaFree(b->ustage);
@@ -739,7 +739,7 @@ ts_status ts_batch_get(ts_batch* b, int32_t id, double* values, ts_step_info* in
     const bool finished = b->h_ctl[slot].stop_req != 0;
     cudaStream_t st = finished ? b->dstream : b->stream;
     mixed_apply(b->d_desc, slot, L.cells(), st);
-    double* pinned = values ? static_cast<double*>(pinned_device_ptr(values)) : nullptr;
+    double* pinned = values ? static_cast<double*>(pinned_device_ptr(values, b->device)) : nullptr;
     if (values && pinned) {
         // page-locked host memory: gathered in place
         k_b_gather<<<blocks, 256, 0, st>>>(pinned, b->d_desc, slot);

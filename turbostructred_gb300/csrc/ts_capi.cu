@@ -363,7 +363,7 @@ static ts_status set_state_impl(ts_handle* h, const double* values, int32_t layo
         if ((s = h->push_ctl()) != TS_OK) return s;
     }
     if (!device_ptr) {
-        if (const void* pd = pinned_device_ptr(values)) {
+        if (const void* pd = pinned_device_ptr(values, h->device)) {
             src = static_cast<const double*>(pd);  // page-locked: read in place
         } else {
             if ((s = h->ensure_stage(nd)) != TS_OK) return s;
@@ -397,7 +397,7 @@ static ts_status get_state_impl(ts_handle* h, double* values, int32_t layout, bo
     const long long ncell = (long long)(nd / NV);
     ts_status s;
     // page-locked host memory is written in place, like device memory
-    double* pinned = device_ptr ? nullptr : static_cast<double*>(pinned_device_ptr(values));
+    double* pinned = device_ptr ? nullptr : static_cast<double*>(pinned_device_ptr(values, h->device));
     const bool staged = !device_ptr && !pinned;
     if (staged && (s = h->ensure_stage(nd)) != TS_OK) return s;
     if (h->cfg.precision == TS_PRECISION_MIXED) {

@@ -19,17 +19,19 @@
 
 namespace ts {
 
-// The device address of page-locked host memory (cudaHostAlloc,
-// cudaHostRegister, a pinned PyTorch tensor), or nullptr for any other
-// pointer.  Kernels read and write such memory in place over the host link,
-// so a state in it needs no staging copy through device memory.
-inline void* pinned_device_ptr(const void* p) {
+// The device address, on `device`, of page-locked host memory allocated or
+// registered against that device (cudaHostAlloc, cudaHostRegister, a pinned
+// PyTorch tensor), or nullptr for any other pointer.  Kernels read and write
+// such memory in place over the host link, so a state in it needs no staging
+// copy through device memory; memory pinned for another device is staged
+// (without cudaHostAllocPortable it is mapped for its own device only).
+inline void* pinned_device_ptr(const void* p, int device) {
     cudaPointerAttributes a;
     if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
         cudaGetLastError();
         return nullptr;
     }
-    return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+    return a.type == cudaMemoryTypeHost && a.device == device ? a.devicePointer : nullptr;
 }
 
 constexpr int NV = 5;      // rho, rho*u, rho*v, rho*w, rho*E
