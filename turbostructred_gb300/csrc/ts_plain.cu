@@ -664,6 +664,27 @@ __device__ void visc_flux(const PlainBufs& b, const Phys& ph, long long cl, long
 }
 
 // Venkatakrishnan l-function (Limiters.h:102-115).
+// Comparisons of doubles on the integer pipe.  GB300 executes FP64 at about
+// two operations per clock per SM, and half of k_recon's FP64-pipe
+// instructions were comparisons (measured with ncu).  dkey is monotone in the
+// value and gives -0 and +0 the same key, so dkey(a) < dkey(b) is exactly
+// a < b, and the sign tests below are exactly x > 0 and x < 0, for every
+// non-NaN a, b, x (a NaN only arises in a run whose health flags stop it).
+__device__ __forceinline__ long long dkey(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 ? (b ^ 0x7FFFFFFFFFFFFFFFLL) + 1 : b;
+}
+__device__ __forceinline__ bool dlt(double a, double b) { return dkey(a) < dkey(b); }
+__device__ __forceinline__ bool dpos(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool dneg(double x) {
+    const long long b = __double_as_longlong(x);
+    return b < 0 && b != (long long)0x8000000000000000ULL;
+}
+// |a| < |b|: the magnitudes' bit patterns order like their values
+__device__ __forceinline__ bool dabs_lt(double a, double b) {
+    return (__double_as_longlong(a) & 0x7FFFFFFFFFFFFFFFLL) < (__double_as_longlong(b) & 0x7FFFFFFFFFFFFFFFLL);
+}
+
 __device__ __forceinline__ double venkat(double um, double ui, double d2, double umax, double umin, double eps2) {
     const double un = 0.5 * (umax - umin);
     um /= un;
@@ -705,7 +726,7 @@ __global__ void k_recon(PlainBufs b, Phys ph) {
             for (int v = 0; v < NV; ++v) {
                 const double gl = (val[v] - nb[2 * a][v]) / (xc - xm);
                 const double gr = (nb[2 * a + 1][v] - val[v]) / (xp - xc);
-                g[a][v] = (fabs(gl) < fabs(gr)) ? gl : gr;
+                g[a][v] = dabs_lt(gl, gr) ? gl : gr;
             }
         } else {
             const double d = xp - xm;
@@ -726,26 +747,28 @@ __global__ void k_recon(PlainBufs b, Phys ph) {
 #pragma unroll
     for (int v = 0; v < NV; ++v) {
         double umax = val[v], umin = val[v];
+        long long kmax = dkey(umax), kmin = kmax;
         for (int f = 0; f < 2 * nd; ++f) {
             const double vn = nb[f][v];
-            if (umax < vn) umax = vn;
-            if (umin > vn) umin = vn;
+            const long long kv = dkey(vn);
+            if (kmax < kv) { umax = vn; kmax = kv; }
+            if (kmin > kv) { umin = vn; kmin = kv; }
         }
         double lmin = 1.0;
-        if (!(umax - umin < 3.0 * 2.2250738585072014e-308)) {
+        if (!dlt(umax - umin, 3.0 * 2.2250738585072014e-308)) {
             for (int f = 0; f < 2 * nd; ++f) {
                 const int a = f >> 1;
                 const double s = (f & 1) ? 0.5 * hcell[a] : -0.5 * hcell[a];
                 const double d2 = (val[v] + g[a][v] * s) - val[v];
                 double lv = 1.0;
                 if (ph.limiter == TS_LIM_VENKATAKRISHNAN) {
-                    if (d2 > 0) lv = venkat(umax, val[v], d2, umax, umin, eps2);
-                    if (d2 < 0) lv = venkat(umin, val[v], d2, umax, umin, eps2);
+                    if (dpos(d2)) lv = venkat(umax, val[v], d2, umax, umin, eps2);
+                    if (dneg(d2)) lv = venkat(umin, val[v], d2, umax, umin, eps2);
                 } else {
-                    if (d2 > 0) { const double r = (umax - val[v]) / d2; lv = (r < 1.0) ? r : 1.0; }
-                    if (d2 < 0) { const double r = (umin - val[v]) / d2; lv = (r < 1.0) ? r : 1.0; }
+                    if (dpos(d2)) { const double r = (umax - val[v]) / d2; lv = dlt(r, 1.0) ? r : 1.0; }
+                    if (dneg(d2)) { const double r = (umin - val[v]) / d2; lv = dlt(r, 1.0) ? r : 1.0; }
                 }
-                if (lmin > lv) lmin = lv;
+                if (dlt(lv, lmin)) lmin = lv;
             }
         }
         b.Lim[vidx(L, v) + c] = lmin;
