@@ -804,10 +804,23 @@ template <int A>
 __global__ void k_flux(PlainBufs b, Phys ph) {
     if (b.ctl->stop_req) return;
     const Layout& L = b.L;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    const int j = blockIdx.y, k = blockIdx.z;
-    const int ilim = (A == 0) ? L.nx + 1 : L.nx;
-    if (i >= ilim) return;
+    int i, j, k;
+    if (A == 0) {
+        // nx + 1 faces per row: one flat index over all rows, so that no
+        // block holds a row's last face alone
+        const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+        const long long row = L.nx + 1;
+        if (t >= row * L.ny * L.nz) return;
+        i = (int)(t % row);
+        const long long r = t / row;
+        j = (int)(r % L.ny);
+        k = (int)(r / L.ny);
+    } else {
+        i = blockIdx.x * blockDim.x + threadIdx.x;
+        j = blockIdx.y;
+        k = blockIdx.z;
+        if (i >= L.nx) return;
+    }
     const int s = (A == 0) ? i : (A == 1 ? j : k);
     const int n = L.n(A);
     const long long st = L.stride(A);
@@ -1071,7 +1084,8 @@ cudaError_t plain_step(const PlainBufs& b, const Phys& ph, cudaStream_t st, cuda
         if (ph.nd > 2) { k_vgrad_bc<2><<<ghost_grid(2), blk, 0, st>>>(b, ph); mark("k_vgrad_bc_z"); }
     }
     if (ph.recon != TS_RECON_PIECEWISE_CONSTANT) { k_recon<<<cells, blk, 0, st>>>(b, ph); mark("k_recon"); }
-    k_flux<0><<<dim3((L.nx + 1 + kPlainBlock - 1) / kPlainBlock, L.ny, L.nz), blk, 0, st>>>(b, ph);
+    const long long xfaces = (long long)(L.nx + 1) * L.ny * L.nz;
+    k_flux<0><<<dim3((unsigned)((xfaces + kPlainBlock - 1) / kPlainBlock)), blk, 0, st>>>(b, ph);
     mark("k_flux_x");
     if (ph.nd > 1) { k_flux<1><<<dim3(cells.x, L.ny + 1, L.nz), blk, 0, st>>>(b, ph); mark("k_flux_y"); }
     if (ph.nd > 2) { k_flux<2><<<dim3(cells.x, L.ny, L.nz + 1), blk, 0, st>>>(b, ph); mark("k_flux_z"); }
