@@ -765,8 +765,18 @@ __global__ void k_recon(PlainBufs b, Phys ph) {
                     if (dpos(d2)) lv = venkat(umax, val[v], d2, umax, umin, eps2);
                     if (dneg(d2)) lv = venkat(umin, val[v], d2, umax, umin, eps2);
                 } else {
-                    if (dpos(d2)) { const double r = (umax - val[v]) / d2; lv = dlt(r, 1.0) ? r : 1.0; }
-                    if (dneg(d2)) { const double r = (umin - val[v]) / d2; lv = dlt(r, 1.0) ? r : 1.0; }
+                    // r = (umax - u) / d2 (or umin) only matters below 1: where
+                    // the exact quotient is >= 1, the rounded one is too (RN is
+                    // monotone and 1 is representable), so lv = 1 without the
+                    // division, bit for bit
+                    if (dpos(d2)) {
+                        const double a = umax - val[v];
+                        if (dlt(a, d2)) { const double r = a / d2; lv = dlt(r, 1.0) ? r : 1.0; }
+                    }
+                    if (dneg(d2)) {
+                        const double a = umin - val[v];
+                        if (dlt(d2, a)) { const double r = a / d2; lv = dlt(r, 1.0) ? r : 1.0; }
+                    }
                 }
                 if (dlt(lv, lmin)) lmin = lv;
             }
